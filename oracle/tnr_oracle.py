@@ -1,0 +1,655 @@
+"""CPU FP64 oracle for TNRKit's coarse-graining hot path (TEST INFRASTRUCTURE ONLY).
+
+This module is the oracle: a NumPy/SciPy restatement of the reference algorithm,
+operation for operation.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import it, and only as the checker or as the
+timed CPU restatement.  The product path (``tnrkit.jl_gb300``) never calls it.
+
+Reference: TNRKit.jl v0.5.1 (pure Julia).  The arithmetic the reference delegates
+to third-party packages that are not vendored with it is restated here from
+their published behaviour:
+
+* TensorKit 0.16.2 (``Project.toml:33``): dense ``Trivial`` tensors are
+  column-major arrays ``T[i1,i2,i3,i4]``; ``permute``/``transpose`` of bosonic
+  legs only reorder axes; abelian (Z_N) tensors are block diagonal in the total
+  charge of the row legs.
+* MatrixAlgebraKit 0.6.1 (``Project.toml:29``): ``svd_trunc``/``eigh_trunc!``
+  with ``truncrank(chi)`` keep the ``min(chi, n)`` values largest in absolute
+  value, globally across charge blocks; the returned truncation error is the
+  2-norm of the discarded values; ``project_hermitian!`` replaces ``M`` by
+  ``(M + M')/2``.
+
+Parity pins (the reference cannot run in this container: no Julia):
+* ``README.md:78-93``: BTRG, Z2 Ising at beta_c, truncrank(16), maxiter(25),
+  26 norms -> f = -2.1096504926141826902647832, |f - f_Onsager|/|f| = 3.1e-7.
+* ``test/schemes.jl:18-23,57-62,94-99,376-383`` and ``test/models.jl:5-39``:
+  free energies against Onsager / published values at the stated rtol.
+Ties between equal singular values at the truncation cut are resolved by a
+stable sort here; the reference's tie order is not visible (parity unpinned at
+exact ties only).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# ---------------------------------------------------------------------------
+# constants  (src/models/ising.jl:1-2,8)
+# ---------------------------------------------------------------------------
+ISING_BETA_C = math.log(1.0 + math.sqrt(2.0)) / 2.0
+F_ONSAGER = -2.10965114460820745966777928351108478082549327543540531781696107967700291143188081390114126499095041781
+ISING_BETA_C_3D = 1.0 / 4.51152469
+F_BENCHMARK_3D = -3.507           # test/schemes.jl:10
+EPS = np.finfo(np.float64).eps
+
+
+def potts_beta_c(q):
+    """src/models/potts.jl:204"""
+    return math.log(1.0 + math.sqrt(q))
+
+
+# ---------------------------------------------------------------------------
+# Tensors with optional abelian charges
+# ---------------------------------------------------------------------------
+@dataclass
+class Tensor:
+    """Dense FP64 array plus, for Z_N-symmetric tensors, one signed-charge vector per leg.
+
+    ``q[l][i]`` is the charge that basis index ``i`` of leg ``l`` contributes to
+    the conservation law ``sum_l q[l][i_l] == 0 (mod N)``.  Codomain legs carry
+    ``+charge``, domain legs ``-charge``; a permute keeps the signed charges and
+    a conjugate negates them.  ``N == 1`` means no symmetry (``Trivial``).
+    """
+
+    a: np.ndarray
+    nout: int                      # number of codomain legs
+    q: list = field(default=None)  # list of int arrays or None
+    N: int = 1
+
+    @property
+    def ndim(self):
+        return self.a.ndim
+
+    def copy(self):
+        return Tensor(self.a.copy(), self.nout,
+                      None if self.q is None else [x.copy() for x in self.q], self.N)
+
+
+def _charges(spec, *ts):
+    """Output-leg charges of a contraction; checks that contracted legs carry
+    opposite signed charges (the flow rule of a symmetric contraction).
+    A tensor passed as ``('c', t)`` enters conjugated: its charges are negated."""
+    ins, out = spec.split('->')
+    seen, N = {}, 1
+    for lab, t in zip(ins.split(','), ts):
+        neg = isinstance(t, tuple)
+        t = t[1] if neg else t
+        N = max(N, t.N)
+        if t.q is None:
+            continue
+        for c, qq in zip(lab, t.q):
+            qq = (-qq) % t.N if neg else qq % t.N
+            if c in seen and c not in out:
+                assert np.array_equal((seen[c] + qq) % t.N, np.zeros_like(qq)), f"charge flow mismatch on leg {c}"
+            seen.setdefault(c, qq)
+    if N == 1:
+        return None, 1
+    return [seen[c] for c in out], N
+
+
+def _ein(spec, *ts, path=None):
+    """Contract Tensors with an einsum spec; output charges follow the leg labels.
+
+    ``path`` is an explicit pairwise order (numpy ``einsum_path`` form) so every
+    contraction runs at the cost the reference's network has (chi^6 / chi^7)."""
+    arrs = [(t[1] if isinstance(t, tuple) else t).a for t in ts]
+    q, N = _charges(spec, *ts)
+    opt = ['einsum_path'] + list(path) if path is not None else True
+    return np.einsum(spec, *arrs, optimize=opt), q, N
+
+
+def permute(t: Tensor, perm, nout):
+    """TensorKit ``permute``/``transpose`` of bosonic legs: an axis reorder."""
+    q = None if t.q is None else [t.q[p] for p in perm]
+    return Tensor(np.ascontiguousarray(np.transpose(t.a, perm)), nout, q, t.N)
+
+
+# ---------------------------------------------------------------------------
+# truncated decompositions (MatrixAlgebraKit 0.6.1, called at
+# src/utility/projectors.jl:215, src/schemes/btrg.jl:167,178,
+# src/schemes/hotrg.jl:103,110,139,146, src/schemes/hotrg3d.jl:93,96)
+# ---------------------------------------------------------------------------
+def _row_col_keys(t: Tensor, nrow):
+    """Charge of each matrix row / column of the (rows <- cols) reshape."""
+    if t.q is None:
+        return None, None
+    N = t.N
+    rk = np.zeros(1, dtype=np.int64)
+    for qq in t.q[:nrow]:
+        rk = (rk[:, None] + qq[None, :]).reshape(-1) % N
+    ck = np.zeros(1, dtype=np.int64)
+    for qq in t.q[nrow:]:
+        ck = (ck[:, None] + qq[None, :]).reshape(-1) % N
+    return rk, (-ck) % N
+
+
+def _select_global(vals_per_block, chi):
+    """Keep the ``chi`` largest |values| over all blocks (truncrank(chi), by=abs, rev=true)."""
+    allv = []
+    for b, v in enumerate(vals_per_block):
+        for i, x in enumerate(v):
+            allv.append((abs(x), b, i))
+    # stable: ties keep block order then index order
+    order = sorted(range(len(allv)), key=lambda j: -allv[j][0])
+    keep = order[:min(chi, len(allv))]
+    kept = [[] for _ in vals_per_block]
+    for j in keep:
+        _, b, i = allv[j]
+        kept[b].append(i)
+    # truncation error = 2-norm of the discarded values
+    disc = [allv[j][0] for j in order[min(chi, len(allv)):]]
+    err = float(np.sqrt(np.sum(np.square(disc)))) if disc else 0.0
+    return [sorted(k) for k in kept], err
+
+
+def svd_trunc(t: Tensor, nrow, chi):
+    """``U, S, V, eps = svd_trunc(t; trunc=truncrank(chi))`` on the rows<-cols reshape.
+
+    Returns U (row legs + bond), s (descending per kept value), Vh (bond + col
+    legs), the truncation error, and the bond charges (U side, V side)."""
+    dims = t.a.shape
+    rdim = int(np.prod(dims[:nrow]))
+    M = t.a.reshape(rdim, -1)
+    cdim = M.shape[1]
+    rk, ck = _row_col_keys(t, nrow)
+    if rk is None:
+        sectors = [(np.arange(rdim), np.arange(cdim), 0)]
+    else:
+        sectors = []
+        for c in range(t.N):
+            r = np.nonzero(rk == c)[0]
+            cc = np.nonzero(ck == c)[0]
+            if len(r) and len(cc):
+                sectors.append((r, cc, c))
+    decs, vals = [], []
+    for r, cc, c in sectors:
+        u, s, vh = np.linalg.svd(M[np.ix_(r, cc)], full_matrices=False)
+        decs.append((u, s, vh))
+        vals.append(s)
+    kept, err = _select_global(vals, chi)
+    # assemble in descending order of value
+    cols = []
+    for b, idx in enumerate(kept):
+        for i in idx:
+            cols.append((vals[b][i], b, i))
+    cols.sort(key=lambda x: -x[0])
+    k = len(cols)
+    U = np.zeros((rdim, k))
+    Vh = np.zeros((k, cdim))
+    s = np.zeros(k)
+    bond = np.zeros(k, dtype=np.int64)
+    for j, (_, b, i) in enumerate(cols):
+        r, cc, c = sectors[b]
+        u, sv, vh = decs[b]
+        U[r, j] = u[:, i]
+        Vh[j, cc] = vh[i, :]
+        s[j] = sv[i]
+        bond[j] = c
+    U = U.reshape(dims[:nrow] + (k,))
+    Vh = Vh.reshape((k,) + dims[nrow:])
+    if t.q is None:
+        return U, s, Vh, err, None
+    return U, s, Vh, err, ((-bond) % t.N, bond % t.N)
+
+
+def eigh_trunc(t: Tensor, nrow, chi):
+    """``_, U, eps = eigh_trunc!(project_hermitian!(MM); trunc=truncrank(chi))``."""
+    dims = t.a.shape
+    rdim = int(np.prod(dims[:nrow]))
+    M = t.a.reshape(rdim, rdim)
+    M = 0.5 * (M + M.T)                        # project_hermitian! (real data)
+    rk, _ = _row_col_keys(t, nrow)
+    if rk is None:
+        sectors = [(np.arange(rdim), 0)]
+    else:
+        sectors = [(np.nonzero(rk == c)[0], c) for c in range(t.N)]
+        sectors = [x for x in sectors if len(x[0])]
+    decs, vals = [], []
+    for r, c in sectors:
+        w, v = np.linalg.eigh(M[np.ix_(r, r)])
+        decs.append(v)
+        vals.append(w)
+    kept, err = _select_global(vals, chi)
+    cols = []
+    for b, idx in enumerate(kept):
+        for i in idx:
+            cols.append((vals[b][i], b, i))
+    cols.sort(key=lambda x: -abs(x[0]))
+    k = len(cols)
+    U = np.zeros((rdim, k))
+    lam = np.zeros(k)
+    bond = np.zeros(k, dtype=np.int64)
+    for j, (_, b, i) in enumerate(cols):
+        r, c = sectors[b]
+        U[r, j] = decs[b][:, i]
+        lam[j] = vals[b][i]
+        bond[j] = c
+    U = U.reshape(dims[:nrow] + (k,))
+    q = None if t.q is None else list(t.q[:nrow]) + [(-bond) % t.N]
+    return Tensor(U, nrow, q, t.N), lam, err
+
+
+# ---------------------------------------------------------------------------
+# models  (src/models/ising.jl, potts.jl, clock.jl)
+# ---------------------------------------------------------------------------
+def _leg_charges(d, nout, nleg, N):
+    if N == 1:
+        return None
+    base = np.arange(d, dtype=np.int64) % N
+    return [base.copy() if l < nout else (-base) % N for l in range(nleg)]
+
+
+def classical_ising(beta=ISING_BETA_C, symmetry="Z2", h=0.0):
+    """src/models/ising.jl:10-15,44-67.  Trivial and Z2 give the same dense array at h=0."""
+    x, y = math.cosh(beta), math.sinh(beta)
+    if symmetry == "Z2":
+        assert h == 0.0, "External magnetic field is not compatible with Z2 symmetry"
+    b = np.array([[math.sqrt(x), 0.0], [0.0, math.sqrt(y)]])
+    init = np.zeros((2, 2, 2, 2))
+    for i, j, k, l in np.ndindex(2, 2, 2, 2):
+        init[i, j, k, l] = math.cosh(h * beta) if (i + j + k + l) % 2 == 0 else math.sinh(h * beta)
+    # T[-1 -2; -3 -4] := 2 init[1 2; 3 4] b[-1;1] b[-2;2] b[3;-3] b[4;-4]
+    a = 2.0 * np.einsum('abcd,ia,jb,ck,dl->ijkl', init, b, b, b, b)
+    N = 2 if symmetry == "Z2" else 1
+    return Tensor(a, 2, _leg_charges(2, 2, 4, N), N)
+
+
+def classical_ising_3D(beta=ISING_BETA_C_3D, symmetry="Z2", J=1.0):
+    """src/models/ising.jl:130-165 (Z2 branch; the Trivial branch is the same model in a
+    different basis).  Legs: D (x) U' <- N (x) E (x) S' (x) W'."""
+    if symmetry == "Z2":
+        x, y = math.cosh(beta * J), math.sinh(beta * J)
+        W = np.array([[math.sqrt(x), math.sqrt(y)], [math.sqrt(x), -math.sqrt(y)]])
+        t = np.einsum('ai,aj,ak,al,am,an->ijklmn', W, W, W, W, W, W)
+        # permute(t, ((1, 4), (5, 6, 2, 3)))
+        a = np.ascontiguousarray(np.transpose(t, (0, 3, 4, 5, 1, 2)))
+        base = np.arange(2, dtype=np.int64)
+        return Tensor(a, 2, [base.copy() for _ in range(6)], 2)
+    K = beta * J
+    tm = np.array([[math.exp(K), math.exp(-K)], [math.exp(-K), math.exp(K)]])
+    w, v = np.linalg.eigh(tm)
+    qm = v @ np.diag(np.sqrt(w)) @ v.T
+    O = np.zeros((2,) * 6)
+    O[(0,) * 6] = 1.0
+    O[(1,) * 6] = 1.0
+    a = np.einsum('abcdef,ia,jb,kc,ld,me,nf->ijklmn', O, qm, qm, qm, qm, qm, qm)
+    return Tensor(a, 2, None, 1)
+
+
+def _fourier_real_zn(A, q, conj_first_two=True):
+    """(P'(x)P') A (P(x)P) with P[k,c] = w^{kc}/sqrt(q); real part (potts.jl:236-246, clock.jl:322-339)."""
+    w = np.exp(2j * np.pi / q)
+    P = np.array([[w ** (k * c) for c in range(q)] for k in range(q)]) / math.sqrt(q)
+    U = np.einsum('ijkl,ia,jb,kc,ld->abcd', A.astype(complex), P.conj(), P.conj(), P, P)
+    return np.real(U)
+
+
+def classical_potts(q=3, beta=None, symmetry="ZN"):
+    """src/models/potts.jl:187-195,228-246."""
+    if beta is None:
+        beta = potts_beta_c(q)
+    A = np.zeros((q, q, q, q))
+    for i, j, k, l in np.ndindex(q, q, q, q):
+        E = -(int(i == j) + int(j == l) + int(k == l) + int(k == i))
+        A[i, j, k, l] = math.exp(-beta * E)
+    if symmetry == "Trivial":
+        return Tensor(A, 2, None, 1)
+    a = _fourier_real_zn(A, q)
+    t = Tensor(a, 2, _leg_charges(q, 2, 4, q), q)
+    return _project_symmetric(t)
+
+
+def classical_clock(q=6, beta=1.0, symmetry="ZN"):
+    """src/models/clock.jl:1-12,316-339 (Trivial and Z_q branches)."""
+    A = np.zeros((q, q, q, q))
+
+    def clock(i, j):
+        return -math.cos(2 * math.pi / q * (i - j))
+    for i, j, k, l in np.ndindex(q, q, q, q):
+        E = clock(i, j) + clock(j, l) + clock(l, k) + clock(k, i)
+        A[i, j, k, l] = math.exp(-beta * E)
+    if symmetry == "Trivial":
+        return Tensor(A, 2, None, 1)
+    a = _fourier_real_zn(A, q)
+    t = Tensor(a, 2, _leg_charges(q, 2, 4, q), q)
+    return _project_symmetric(t)
+
+
+def _project_symmetric(t: Tensor):
+    """Zero the entries that break charge conservation (TensorKit keeps only symmetric blocks)."""
+    if t.q is None:
+        return t
+    tot = np.zeros((1,) * t.ndim, dtype=np.int64)
+    for l, qq in enumerate(t.q):
+        shape = [1] * t.ndim
+        shape[l] = len(qq)
+        tot = tot + qq.reshape(shape)
+    mask = (tot % t.N) == 0
+    assert np.max(np.abs(t.a[~mask]), initial=0.0) < 1e-10 * np.max(np.abs(t.a))
+    return Tensor(np.where(mask, t.a, 0.0), t.nout, t.q, t.N)
+
+
+def random_hotrg_tensor(chi, seed, decay=6.0):
+    """Seeded dense 4-leg test tensor: N(0,1) entries weighted per leg by exp(-k/decay),
+    Frobenius-normalised (the single-step HOTRG workload)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = rng.standard_normal((chi,) * 4)
+    s = np.exp(-np.arange(chi) / decay)
+    a = a * s[:, None, None, None] * s[None, :, None, None] * s[None, None, :, None] * s[None, None, None, :]
+    a /= np.linalg.norm(a)
+    return Tensor(a, 2, None, 1)
+
+
+# ---------------------------------------------------------------------------
+# schemes
+# ---------------------------------------------------------------------------
+class TRG:
+    """src/schemes/trg.jl:85-92"""
+    scalefactor = 2.0
+
+    def __init__(self, T: Tensor):
+        assert T.ndim == 4
+        self.T = T.copy()
+        self.svals = []          # kept singular values of every decomposition, in order
+
+
+class BTRG:
+    """src/schemes/btrg.jl:132-154: S1 = id(space(T,2)), S2 = id(space(T,1)), k = -1/2."""
+    scalefactor = 2.0
+
+    def __init__(self, T: Tensor, k=-0.5):
+        assert T.ndim == 4
+        self.T = T.copy()
+        self.S1 = np.ones(T.a.shape[1])      # diagonal bond tensors
+        self.S2 = np.ones(T.a.shape[0])
+        self.k = float(k)
+        self.svals = []
+
+
+class HOTRG:
+    """src/schemes/hotrg.jl:27-34"""
+    scalefactor = 4.0
+
+    def __init__(self, T: Tensor):
+        assert T.ndim == 4
+        self.T = T.copy()
+        self.svals = []
+        self.eps = []
+
+
+class HOTRG_3D:
+    """src/schemes/hotrg3d.jl:27-34"""
+    scalefactor = 8.0
+
+    def __init__(self, T: Tensor):
+        assert T.ndim == 6
+        self.T = T.copy()
+        self.svals = []
+        self.eps = []
+
+
+def SVD12(T: Tensor, chi):
+    """src/utility/projectors.jl:211-217: U*sqrt(s), sqrt(s)*V."""
+    U, s, Vh, _, bq = svd_trunc(T, 2, chi)
+    r = np.sqrt(s)
+    A = Tensor(U * r, 2, None if bq is None else [T.q[0], T.q[1], bq[0]], T.N)
+    B = Tensor(r[:, None, None] * Vh, 1, None if bq is None else [bq[1], T.q[2], T.q[3]], T.N)
+    return A, B, s
+
+
+def step_trg(scheme: TRG, chi):
+    """src/schemes/trg.jl:94-100"""
+    T = scheme.T
+    A, B, s1 = SVD12(T, chi)
+    Tp = permute(T, (1, 3, 0, 2), 2)                       # transpose(T, ((2,4),(1,3)))
+    C, D, s2 = SVD12(Tp, chi)
+    # T[-1 -2; -3 -4] := D[-2; 1 2] B[-1; 4 1] C[4 3; -3] A[3 2; -4]
+    a, q, N = _ein('bpq,arp,rsc,sqd->abcd', D, B, C, A, path=[(0, 1), (0, 1), (0, 1)])
+    scheme.T = Tensor(a, 2, q, N)
+    scheme.svals += [s1, s2]
+
+
+def pseudopow(s, a, tol=EPS ** 0.75):
+    """src/schemes/btrg.jl:156-164"""
+    out = s.copy()
+    m = s >= tol
+    out[m] = s[m] ** a
+    return out
+
+
+def step_btrg(scheme: BTRG, chi):
+    """src/schemes/btrg.jl:166-200"""
+    T = scheme.T
+    k = scheme.k
+    U, s, Vh, _, bq = svd_trunc(T, 2, chi)
+    sa, sb = pseudopow(s, (1 - k) / 2), pseudopow(s, k)
+    A = Tensor(U * sa, 2, None if bq is None else [T.q[0], T.q[1], bq[0]], T.N)
+    B = Tensor(sa[:, None, None] * Vh, 1, None if bq is None else [bq[1], T.q[2], T.q[3]], T.N)
+    S1n = sb
+    P = permute(T, (2, 0, 3, 1), 2)                         # permute(T, ((3,1),(4,2)))
+    U2, s2, Vh2, _, bq2 = svd_trunc(P, 2, chi)
+    sa2, sb2 = pseudopow(s2, (1 - k) / 2), pseudopow(s2, k)
+    C = Tensor(U2 * sa2, 2, None if bq2 is None else [P.q[0], P.q[1], bq2[0]], T.N)
+    D = Tensor(sa2[:, None, None] * Vh2, 1, None if bq2 is None else [bq2[1], P.q[2], P.q[3]], T.N)
+    S2n = sb2
+    S1, S2 = scheme.S1, scheme.S2
+    # T[-1 -2; -3 -4] := D[-1;4 7] S1[1;7] B[-2;1 3] S2[3;2] C[8 2;-4] S1[8;5] A[6 5;-3] S2[4;6]
+    # diagonal S1/S2: fold them into D's leg 7 and C's leg 8 / B's leg 3 and D's leg 4 equivalents
+    Dd = Tensor(D.a * S1[None, None, :], D.nout, D.q, D.N)            # D[-1;4 7] S1[7]
+    Dd = Tensor(Dd.a * S2[None, :, None], Dd.nout, Dd.q, Dd.N)        # S2[4;6] (diag: 4 == 6)
+    Bd = Tensor(B.a * S2[None, None, :], B.nout, B.q, B.N)            # S2[3;2]  (3 == 2)
+    Cd = Tensor(C.a * S1[:, None, None], C.nout, C.q, C.N)            # S1[8;5]  (8 == 5)
+    # now D[-1;4 1] B[-2;1 2] C[5 2;-4] A[4 5;-3]
+    a, q, N = _ein('axp,bpy,zyd,xzc->abcd', Dd, Bd, Cd, A, path=[(0, 1), (0, 1), (0, 1)])
+    scheme.T = Tensor(a, 2, q, N)
+    scheme.S1, scheme.S2 = S1n, S2n
+    scheme.svals += [s, s2]
+
+
+def _hotrg_xproj(A1: Tensor, A2: Tensor, chi):
+    """src/schemes/hotrg.jl:82-116"""
+    a, q, N = _ein('aeij,bkel,cfij,dkfl->abcd', A2, A1, ('c', A2), ('c', A1), path=[(0, 2), (0, 1), (0, 1)])
+    U, lam, eps = eigh_trunc(Tensor(a, 2, q, N), 2, chi)
+    a, q, N = _ein('jeia,lkeb,jfic,lkfd->abcd', ('c', A2), ('c', A1), A2, A1, path=[(0, 2), (0, 1), (0, 1)])
+    U2, lam2, eps2 = eigh_trunc(Tensor(a, 2, q, N), 2, chi)
+    if eps > eps2:
+        return U2, lam2, eps2, (eps, eps2)
+    return U, lam, eps, (eps, eps2)
+
+
+def _hotrg_yproj(A1: Tensor, A2: Tensor, chi):
+    """src/schemes/hotrg.jl:118-152"""
+    a, q, N = _ein('iajp,pblk,icjr,rdlk->abcd', A1, A2, ('c', A1), ('c', A2), path=[(0, 2), (0, 1), (0, 1)])
+    U, lam, eps = eigh_trunc(Tensor(a, 2, q, N), 2, chi)
+    a, q, N = _ein('ijap,plbk,ijcr,rldk->abcd', ('c', A1), ('c', A2), A1, A2, path=[(0, 2), (0, 1), (0, 1)])
+    U2, lam2, eps2 = eigh_trunc(Tensor(a, 2, q, N), 2, chi)
+    if eps > eps2:
+        return U2, lam2, eps2, (eps, eps2)
+    return U, lam, eps, (eps, eps2)
+
+
+def _hotrg_step_y(A1, A2, Ux):
+    """src/schemes/hotrg.jl:42-60: conj(Ux[1 2;-1]) Ux[3 4;-4] A2[1 5;-3 3] A1[2 -2;5 4]"""
+    a, q, N = _ein('ija,kld,iegk,jbel->abgd', ('c', Ux), Ux, A2, A1, path=[(0, 2), (1, 2), (0, 1)])
+    return Tensor(a, 2, q, N)
+
+
+def _hotrg_step_x(A1, A2, Uy):
+    """src/schemes/hotrg.jl:62-80: A1[-1 1;3 5] A2[5 2;4 -4] conj(Uy[1 2;-2]) Uy[3 4;-3]"""
+    a, q, N = _ein('aike,ejld,ijb,klc->abcd', A1, A2, ('c', Uy), Uy, path=[(0, 2), (0, 2), (0, 1)])
+    return Tensor(a, 2, q, N)
+
+
+def step_hotrg(scheme: HOTRG, chi):
+    """src/schemes/hotrg.jl:154-160"""
+    T = scheme.T
+    Ux, lx, ex, pair = _hotrg_xproj(T, T, chi)
+    T = _hotrg_step_y(T, T, Ux)
+    Uy, ly, ey, pair2 = _hotrg_yproj(T, T, chi)
+    T = _hotrg_step_x(T, T, Uy)
+    scheme.T = T
+    scheme.svals += [lx, ly]
+    scheme.eps += [pair, pair2]
+
+
+def _mmdag_3d(A1, A2):
+    """src/schemes/hotrg3d.jl:48-65 (bosonic: the twists are identities)."""
+    a, q, N = _ein('zwYXyx,vwYXyu->xzvu', A2, ('c', A2))
+    M1 = Tensor(a, 4, q, N)
+    a, q, N = _ein('xzvu,pzYXyr,pvYXys->rxsu', M1, A1, ('c', A1))
+    return Tensor(0.5 * (a + np.transpose(a, (2, 3, 0, 1))), 2, q, N)
+
+
+def _mdagm_3d(A1, A2):
+    """src/schemes/hotrg3d.jl:67-84"""
+    a, q, N = _ein('zwYxyX,vwYuyX->xzvu', ('c', A2), A2)
+    M1 = Tensor(a, 4, q, N)
+    a, q, N = _ein('xzvu,pzYryX,pvYsyX->rxsu', M1, ('c', A1), A1)
+    return Tensor(0.5 * (a + np.transpose(a, (2, 3, 0, 1))), 2, q, N)
+
+
+def _hotrg3d_xproj(A1, A2, chi):
+    """src/schemes/hotrg3d.jl:86-98"""
+    U, lam, eps = eigh_trunc(_mmdag_3d(A1, A2), 2, chi)
+    U2, lam2, eps2 = eigh_trunc(_mdagm_3d(A1, A2), 2, chi)
+    if eps > eps2:
+        return U2, lam2, eps2, (eps, eps2)
+    return U, lam, eps, (eps, eps2)
+
+
+def _hotrg3d_yproj(A1, A2, chi):
+    """src/schemes/hotrg3d.jl:100-106"""
+    perm = (0, 1, 3, 2, 5, 4)
+    return _hotrg3d_xproj(permute(A1, perm, 2), permute(A2, perm, 2), chi)
+
+
+def _step_hotrg3d(A1, A2, Ux, Uy, max_entries=1 << 28):
+    """src/schemes/hotrg3d.jl:108-117:
+    T[-1 -2;-3 -4 -5 -6] = conj(Ux[x1 x2;-6]) Ux[x1' x2';-4] conj(Uy[y1 y2;-5]) Uy[y1' y2';-3]
+                           A1[-1 z; y1' x1' y1 x1] A2[z -2; y2' x2' y2 x2]
+    Contracted in an order whose largest intermediate has chi^8 entries (leading
+    cost chi^11), sliced over the open leg -1 so no intermediate exceeds
+    ``max_entries`` entries."""
+    specs = ('azPQyx,QRd->azPyxRd', 'azPyxRd,PSc->azyxRdSc', 'azyxRdSc,zbSRuv->ayxdcbuv',
+             'ayxdcbuv,xvf->aydcbuf', 'aydcbuf,yue->abcdef')
+    # output charges: follow the labels through the whole network
+    q, N = _charges('azPQyx,QRd,PSc,zbSRuv,xvf,yue->abcdef', A1, Ux, Uy, A2, ('c', Ux), ('c', Uy))
+    da = A1.a.shape[0]
+    per_a = int(np.prod(A1.a.shape[1:])) * max(Ux.a.shape[1], 1) * Uy.a.shape[1] * Uy.a.shape[2] * Ux.a.shape[2]
+    chunk = max(1, min(da, max_entries // max(per_a, 1)))
+    out = None
+    for a0 in range(0, da, chunk):
+        X = np.einsum(specs[0], A1.a[a0:a0 + chunk], Ux.a, optimize=True)
+        Y = np.einsum(specs[1], X, Uy.a, optimize=True)
+        del X
+        Z = np.einsum(specs[2], Y, A2.a, optimize=True)
+        del Y
+        W = np.einsum(specs[3], Z, Ux.a, optimize=True)
+        del Z
+        part = np.einsum(specs[4], W, Uy.a, optimize=True)
+        if out is None:
+            out = np.empty((da,) + part.shape[1:])
+        out[a0:a0 + chunk] = part
+    return Tensor(out, 2, q, N)
+
+
+def step_hotrg3d(scheme: HOTRG_3D, chi):
+    """src/schemes/hotrg3d.jl:120-135"""
+    for _ in range(3):
+        T = scheme.T
+        Ux, lx, ex, p1 = _hotrg3d_xproj(T, T, chi)
+        Uy, ly, ey, p2 = _hotrg3d_yproj(T, T, chi)
+        T = _step_hotrg3d(T, T, Ux, Uy)
+        scheme.T = permute(T, (5, 3, 1, 2, 0, 4), 2)      # permute(T, ((6,4),(2,3,1,5)))
+        scheme.svals += [lx, ly]
+        scheme.eps += [p1, p2]
+
+
+def step(scheme, chi):
+    """``step!(scheme, truncrank(chi))`` dispatch (src/schemes/tnrscheme.jl:2)."""
+    if isinstance(scheme, TRG):
+        step_trg(scheme, chi)
+    elif isinstance(scheme, BTRG):
+        step_btrg(scheme, chi)
+    elif isinstance(scheme, HOTRG):
+        step_hotrg(scheme, chi)
+    elif isinstance(scheme, HOTRG_3D):
+        step_hotrg3d(scheme, chi)
+    else:
+        raise TypeError(type(scheme))
+    return scheme
+
+
+def finalize(scheme):
+    """src/utility/finalize.jl:4-14,62-66: trace norm, then T /= n."""
+    T = scheme.T.a
+    if isinstance(scheme, (TRG, HOTRG)):
+        n = abs(np.einsum('abba->', T))                 # T[1 2; 2 1]
+    elif isinstance(scheme, BTRG):
+        # T[1 2; 4 3] S1[4; 2] S2[3; 1] with diagonal S1, S2
+        n = abs(_btrg_trace(T, scheme.S1, scheme.S2))
+    elif isinstance(scheme, HOTRG_3D):
+        n = abs(np.einsum('aabcbc->', T))               # T[1 1; 2 3 2 3]
+    else:
+        raise TypeError(type(scheme))
+    scheme.T.a = T / n
+    return float(n)
+
+
+def _btrg_trace(T, S1, S2):
+    """sum_{a,b} T[a,b,b,a] S1[b] S2[a] for diagonal S1 (leg 2) and S2 (leg 1)."""
+    d1, d2 = T.shape[0], T.shape[1]
+    ia = np.arange(d1)[:, None]
+    ib = np.arange(d2)[None, :]
+    return float(np.sum(T[ia, ib, ib, ia] * S1[None, :] * S2[:, None]))
+
+
+@dataclass
+class truncrank:
+    """MatrixAlgebraKit ``truncrank(howmany)``"""
+    howmany: int
+
+
+@dataclass
+class maxiter:
+    """src/utility/stopping.jl:3-5,18: continue while steps < n."""
+    n: int
+
+    def __call__(self, steps, data):
+        return steps < self.n
+
+
+def run(scheme, trunc: truncrank, crit: maxiter, finalize_beginning=True, verbosity=0):
+    """src/schemes/tnrscheme.jl:33-57 with the default Finalizer (finalize!, Float64)."""
+    data = []
+    if finalize_beginning:
+        data.append(finalize(scheme))
+    steps = 0
+    go = True
+    while go:
+        step(scheme, trunc.howmany)
+        data.append(finalize(scheme))
+        steps += 1
+        go = crit(steps, data)
+    return data
+
+
+def free_energy(data, beta, scalefactor=2.0, initial_size=1.0):
+    """src/utility/free_energy.jl:13-20"""
+    lnz = 0.0
+    x = 1.0 - math.log(initial_size) / math.log(scalefactor)
+    for i, z in enumerate(data, start=1):
+        lnz += math.log(z) * scalefactor ** (x - i)
+    return -lnz / beta

@@ -1,0 +1,96 @@
+"""Pins the CPU oracle against the reference's own golden values and test tolerances.
+
+Golden values: README.md:78-93 (BTRG, Z2 Ising, chi=16, 25 iterations) and the
+free-energy tolerances of test/schemes.jl and test/models.jl.
+"""
+import math
+
+import numpy as np
+import pytest
+
+
+def _f(o, scheme, chi, n, beta, sf):
+    data = o.run(scheme, o.truncrank(chi), o.maxiter(n))
+    return data, o.free_energy(data, beta, scalefactor=sf)
+
+
+@pytest.mark.parametrize("symmetry", ["Z2", "Trivial"])
+def test_readme_btrg_golden(oracle, symmetry):
+    # README.md:78-93: 26 norms, f = -2.1096504926141826902647832, rel. err 3.1e-7
+    o = oracle
+    data, f = _f(o, o.BTRG(o.classical_ising(o.ISING_BETA_C, symmetry)), 16, 25, o.ISING_BETA_C, 2.0)
+    assert len(data) == 26
+    assert f == pytest.approx(-2.1096504926141826902647832, rel=1e-14, abs=0)
+    assert abs((f - o.F_ONSAGER) / o.F_ONSAGER) == pytest.approx(3.1e-7, rel=0.01)
+
+
+@pytest.mark.parametrize("cls,chi,sf,rtol", [
+    ("TRG", 24, 2.0, 2e-6),     # test/schemes.jl:18-23
+    ("BTRG", 24, 2.0, 6e-8),    # test/schemes.jl:57-62
+    ("HOTRG", 16, 4.0, 6e-7),   # test/schemes.jl:94-99
+])
+def test_schemes_onsager(oracle, cls, chi, sf, rtol):
+    o = oracle
+    _, f = _f(o, getattr(o, cls)(o.classical_ising()), chi, 25, o.ISING_BETA_C, sf)
+    assert f == pytest.approx(o.F_ONSAGER, rel=rtol)
+
+
+def test_models_trg16(oracle):
+    # test/models.jl:5-39 (the Trivial / Z_N models on the hot path), TRG chi=16, rtol 1e-3
+    o = oracle
+    b3 = 2.0 * math.log(math.sqrt(3) + 1) / 3
+    b4 = math.log(math.sqrt(2) + 1)
+    cases = [
+        (o.classical_ising(symmetry="Trivial"), o.ISING_BETA_C, o.F_ONSAGER),
+        (o.classical_ising(), o.ISING_BETA_C, o.F_ONSAGER),
+        (o.classical_clock(3, b3, "Trivial"), b3, -4.17924244901635),
+        (o.classical_clock(3, b3), b3, -4.17924244901635),
+        (o.classical_clock(4, b4, "Trivial"), b4, 2 * o.F_ONSAGER),
+        (o.classical_clock(4, b4), b4, 2 * o.F_ONSAGER),
+        (o.classical_potts(3, symmetry="Trivial"), o.potts_beta_c(3), -4.119552029995684),
+        (o.classical_potts(3), o.potts_beta_c(3), -4.119552029995684),
+    ]
+    for T, beta, ans in cases:
+        _, f = _f(o, o.TRG(T), 16, 25, beta, 2.0)
+        assert f == pytest.approx(ans, rel=1e-3)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("symmetry,ans", [("Z2", -3.507), ("Trivial", -3.508)])
+def test_hotrg3d_chi8(oracle, symmetry, ans):
+    # test/schemes.jl:376-383 and test/models.jl:29-32,80-86: chi=8, 25 iterations, sf=8, rtol 1e-3
+    o = oracle
+    _, f = _f(o, o.HOTRG_3D(o.classical_ising_3D(symmetry=symmetry)), 8, 25, o.ISING_BETA_C_3D, 8.0)
+    assert f == pytest.approx(ans, rel=1e-3)
+
+
+def test_symmetric_equals_dense(oracle):
+    """Z2 block-sparse and dense decompositions give the same norms (no ties at the cut here)."""
+    o = oracle
+    for cls in ("TRG", "HOTRG"):
+        d1 = o.run(getattr(o, cls)(o.classical_ising(symmetry="Z2")), o.truncrank(12), o.maxiter(8))
+        d2 = o.run(getattr(o, cls)(o.classical_ising(symmetry="Trivial")), o.truncrank(12), o.maxiter(8))
+        np.testing.assert_allclose(d1, d2, rtol=1e-11)
+
+
+def test_free_energy_formula(oracle):
+    # src/utility/free_energy.jl:13-20
+    o = oracle
+    data = [2.0, 3.0, 5.0]
+    f = o.free_energy(data, 0.5, scalefactor=4.0, initial_size=2.0)
+    x = 1 - math.log(2.0) / math.log(4.0)
+    ref = -sum(math.log(z) * 4.0 ** (x - i) for i, z in enumerate(data, 1)) / 0.5
+    assert f == pytest.approx(ref, rel=1e-15)
+
+
+def test_pseudopow(oracle):
+    # src/schemes/btrg.jl:156-164: values below eps^(3/4) are left unchanged
+    o = oracle
+    s = np.array([4.0, 1e-13, 0.25])
+    np.testing.assert_allclose(o.pseudopow(s, -0.5), [0.5, 1e-13, 2.0])
+
+
+def test_maxiter(oracle):
+    # src/utility/stopping.jl:18
+    c = oracle.maxiter(3)
+    assert c(2, None) and not c(3, None)
