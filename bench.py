@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Free-energy solves/s of the batched beta sweep (BTRG, 2D Ising) on GB300.
+
+Workload (one "step" = one pass over the batch): n independent BTRG solves of the 2D
+Ising partition-function tensor (Trivial symmetry) at beta ~ U[0.30, 0.60] and
+chi ~ U{8, 16, 24, 32, 48} drawn from a recorded seed, 30 iterations each, norms ->
+free energy (scalefactor 2).  ``value`` is whole-job solves/s with the initial
+tensors already in HBM; ``e2e`` is the same through the public API from host
+arrays (host->device copy of the inputs and device->host read of the norms inside
+the timed region).  ``--impl reference`` times the CPU restatement of the
+reference (the oracle) on this host's cores on a bounded sample of the workload.
+
+Multi-GPU: replicas only (every rank runs its own batch; no collective on the data
+path); the barrier and the max over ranks use gloo.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+CHIS = (8, 16, 24, 32, 48)
+METRIC = "free-energy solves/s & p99 latency vs plain FP64 GPU path at |Δf/f|≤1e-7"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="split", choices=["split", "f64"])
+    p.add_argument("--instances", type=int, default=256)
+    p.add_argument("--maxiter", type=int, default=30)
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--plain-sample", type=int, default=32,
+                   help="instances of the batch also solved on the plain FP64 path (solves/s and |df/f|)")
+    p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(n, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    betas = rng.uniform(0.30, 0.60, n)
+    chis = rng.choice(np.array(CHIS), n)
+    return betas, chis
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas; gloo for barrier / max)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(self.local))
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.p = None
+        self.lines = []
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (NumPy/SciPy FP64 restatement) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_solve_times(maxiter, budget):
+    """Per-chi seconds of one full BTRG solve on the host, from a bounded sample:
+    each chi runs steps until its share of the budget is spent, and the remaining
+    steps are extrapolated at the cost of the last (full-size) step."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tnr_oracle as o
+    per = {}
+    share = budget / len(CHIS)
+    for chi in CHIS:
+        s = o.BTRG(o.classical_ising(0.45, "Trivial"))
+        t0 = time.perf_counter()
+        o.finalize(s)
+        last = 0.0
+        done = 0
+        while done < maxiter:
+            ts = time.perf_counter()
+            o.step(s, chi)
+            o.finalize(s)
+            last = time.perf_counter() - ts
+            done += 1
+            if time.perf_counter() - t0 > share and s.T.a.shape[0] == chi:
+                break
+        spent = time.perf_counter() - t0
+        per[chi] = spent + (maxiter - done) * last
+        per[chi] = (per[chi], done)
+    return per
+
+
+def cpu_baseline(chis, maxiter, budget):
+    per = cpu_solve_times(maxiter, budget)
+    total = sum(per[int(c)][0] for c in chis)
+    sample = "oracle BTRG per chi in {8,16,24,32,48}: %s steps run (of %d), rest extrapolated at the last full-size " \
+             "step's cost; summed over the %d instances" % (
+                 ",".join("%d:%d" % (c, per[c][1]) for c in CHIS), maxiter, len(chis))
+    return len(chis) / total, sample
+
+
+def threads_used():
+    try:
+        from threadpoolctl import threadpool_info
+        n = [i.get("num_threads") for i in threadpool_info() if i.get("internal_api") in ("openblas", "mkl")]
+        if n:
+            return int(max(n))
+    except Exception:
+        pass
+    return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def fp64_gemm_peak_tflops():
+    """cuBLAS DGEMM throughput on this GPU (denominator for FP64 kernels only)."""
+    try:
+        import torch
+        a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        return 3 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    except Exception:
+        return None
+
+
+def run_ours(args, d):
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as ge
+    ge.build()
+    tnr = ge.package()
+    prec = tnr.PREC_SPLIT if args.precision == "split" else tnr.PREC_F64
+    betas, chis = workload(args.instances, args.seed + d.rank)
+    n = len(betas)
+    maxit = [args.maxiter] * n
+    tensors = [tnr.classical_ising("Trivial", float(b)) for b in betas]
+
+    def make(precision):
+        return [tnr.BTRG(T, precision=precision) for T in tensors]
+
+    for _ in range(args.warmup):
+        tnr.run_batch(make(prec), chis, maxit)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+
+    # timed region: device span of each batch (CUDA events), tensors already resident
+    dev_ms, lats, results = [], [], None
+    l0 = tnr.kernel_launches()
+    clk = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    for _ in range(args.steps):
+        schemes = make(prec)
+        d.barrier()
+        tm = {}
+        results = tnr.run_batch(schemes, chis, maxit, timing=tm)
+        dev_ms.append(tm["device_ms"])
+        lats.extend(list(tm["latency_ms"]))
+        for s in schemes:
+            s.close()
+    clocks = clk.stop()
+    launches = tnr.kernel_launches() - l0
+    t_max = d.max(sum(dev_ms) / 1000.0)
+    total = d.sum(n * args.steps)
+    value = total / t_max
+    f_ours = [tnr.free_energy(r, float(b)) for r, b in zip(results, betas)]
+
+    # end to end through the public API: host arrays in, norms out, free energies on host
+    d.barrier()
+    t0 = time.perf_counter()
+    schemes = make(prec)                                   # host -> device copy of the inputs
+    norms = tnr.run_batch(schemes, chis, maxit)            # device -> host read of the norms
+    fe = [tnr.free_energy(r, float(b)) for r, b in zip(norms, betas)]
+    e2e_s = d.max(time.perf_counter() - t0)
+    for s in schemes:
+        s.close()
+    e2e = {"value": d.sum(n) / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(sum(T.array.nbytes for T in tensors)),
+           "d2h_bytes_per_step": int(sum(8 * len(r) for r in norms))}
+
+    # plain FP64 GPU path on a sample of the same batch: solves/s and |df/f|
+    plain = None
+    m = min(args.plain_sample, n)
+    if prec != tnr.PREC_F64 and m > 0:
+        idx = list(range(m))
+        sch = [tnr.BTRG(tensors[i], precision=tnr.PREC_F64) for i in idx]
+        tm = {}
+        ref = tnr.run_batch(sch, [chis[i] for i in idx], [args.maxiter] * m, timing=tm)
+        f_ref = [tnr.free_energy(r, float(betas[i])) for r, i in zip(ref, idx)]
+        rel = [abs(f_ours[i] - f_ref[j]) / abs(f_ref[j]) for j, i in enumerate(idx)]
+        # scale the sample's time to the whole batch by the per-chi mix of the sample
+        plain = {"solves_per_s_sample": m / (tm["device_ms"] / 1000.0), "sample_instances": m,
+                 "max_rel_df": max(rel), "median_rel_df": statistics.median(rel)}
+    elif prec == tnr.PREC_F64:
+        plain = {"solves_per_s_sample": value, "sample_instances": n, "max_rel_df": 0.0, "note": "this run is the plain path"}
+
+    # roofline of the dominant kernel class: one extra profiled pass of the same workload
+    tnr.profile_reset()
+    tnr.profile_enable(True)
+    schemes = make(prec)
+    tnr.run_batch(schemes, chis, maxit)
+    tnr.profile_enable(False)
+    prof = tnr.profile_read()
+    tnr.profile_reset()
+    for s in schemes:
+        s.close()
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    g = prof["gemm_bulk"]
+    roof = None
+    if g[0]:
+        per_launch_flops = g[2] / g[0]
+        avg_s = g[1] / g[0] / 1000.0
+        achieved = per_launch_flops / avg_s / 1e12
+        if prec == tnr.PREC_SPLIT:
+            peak, src = peaks.get("bf16_tflops"), "bf16_tflops of measured (MEASURED_PEAKS.json, burst)"
+        else:
+            peak, src = fp64_gemm_peak_tflops(), "cuBLAS DGEMM 4096^3 measured in this run (FP64 kernel)"
+        roof = {"kernel": "gemm_bulk", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if peak else None, "traffic": None, "peak_source": src,
+                "launches": g[0], "flops_per_launch": per_launch_flops, "avg_launch_ms": g[1] / g[0],
+                "note": "algorithmic flops 2*m*n*k per launch / CUDA-event launch duration, profiled pass"}
+    shares = {k: {"launches": v[0], "ms": round(v[1], 3), "work": v[2]} for k, v in prof.items()}
+
+    lats_sorted = sorted(lats)
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": d.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16x3 split (fp32 accumulate) + f64" if prec == tnr.PREC_SPLIT else "f64",
+        "data": "synthetic (analytic Ising tensors, seeded beta/chi draws)",
+        "config": {"workload": "btrg_beta_sweep: %d BTRG solves, 2D Ising (Trivial), beta~U[0.30,0.60], "
+                               "chi~U{8,16,24,32,48}, maxiter %d, seed %d" % (n, args.maxiter, args.seed),
+                   "instances_per_gpu": n, "maxiter": args.maxiter, "precision": args.precision,
+                   "l2": "working set > L2: every instance keeps chi^4 tensors and chi^6-flop intermediates "
+                         "resident; batch state is several GB"},
+        "p50_ms": float(np.percentile(lats_sorted, 50)), "p99_ms": float(np.percentile(lats_sorted, 99)),
+        "latency_note": "per-solve completion time from batch start (all solves submitted together)",
+        "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "kernel_classes": shares,
+        "dominant_class": dom[0], "plain_f64": plain,
+        "f_check": {"instance0_beta": float(betas[0]), "instance0_chi": int(chis[0]), "f": f_ours[0]},
+    }
+    return out, chis
+
+
+def main():
+    args = parse()
+    d = Dist()
+    if args.impl == "reference":
+        if d.rank != 0:
+            return
+        betas, chis = workload(args.instances, args.seed)
+        vals = []
+        for i in range(args.warmup + args.steps):
+            v, sample = cpu_baseline(chis, args.maxiter, args.cpu_budget / 2)
+            if i >= args.warmup:
+                vals.append(v)
+        v = statistics.median(vals)
+        cores = threads_used()
+        line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": d.world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0 * args.instances / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": "btrg_beta_sweep: %d BTRG solves, 2D Ising (Trivial), beta~U[0.30,0.60], "
+                                       "chi~U{8,16,24,32,48}, maxiter %d, seed %d" % (args.instances, args.maxiter,
+                                                                                       args.seed)},
+                "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+                "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "reference is pure Julia (not runnable here); the timed CPU path is the oracle "
+                        "(NumPy/SciPy FP64 restatement of the reference's algorithm)"}
+        print(json.dumps(line), flush=True)
+        return
+    out, chis = run_ours(args, d)
+    if d.rank == 0:
+        if not args.no_cpu_baseline:
+            v, sample = cpu_baseline(chis, args.maxiter, args.cpu_budget)
+            out["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": threads_used(), "kind": "port",
+                                   "sample": sample}
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,170 @@
+/*
+ * tnr_gb300.h -- C ABI of the GB300 (sm_103a) coarse-graining engine.
+ *
+ * Drop-in boundary for the hot path of TNRKit.jl v0.5.1: the scheme structs
+ * TRG / BTRG / HOTRG / HOTRG_3D, step!(scheme, truncrank(chi)),
+ * finalize!(scheme), run!(scheme, truncrank(chi), maxiter(n)) and
+ * free_energy(data, beta).  A Julia `ccall` layer (or Python ctypes) holds an
+ * opaque handle in place of the scheme's tensors; the tensors stay resident in
+ * GPU memory between calls.  Plain pointers and sizes only.
+ *
+ * Tensor layout: column-major, first leg fastest, exactly TensorKit's dense
+ * storage of a TensorMap V1 (x) V2 <- V3 (x) V4 (the array T[i1,i2,i3,i4]).
+ * Leg order: 2D = (left, down, up, right); 3D = (D, U', N, E, S', W').
+ *
+ * Status codes: every function returns TNR_OK (0) or a TNR_ERR_* code and
+ * never aborts the process; tnr_last_error() gives the message.
+ * Threading: a handle is single-owner and bound to one CUDA stream; calls on
+ * different handles may come from different threads.
+ */
+#ifndef TNR_GB300_H
+#define TNR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TNR_OK                 0
+#define TNR_ERR_INVALID_ARG    1  /* bad argument (reference: ArgumentError / SpaceMismatch) */
+#define TNR_ERR_OOM            2  /* device allocation failed                                */
+#define TNR_ERR_NOT_CONVERGED  3  /* an iterative solver hit its iteration cap               */
+#define TNR_ERR_CUDA           4  /* CUDA runtime error                                      */
+#define TNR_ERR_ADMISSION      5  /* request refused: HBM footprint above the admission cap  */
+#define TNR_ERR_NONFINITE      6  /* NaN/Inf in inputs or produced by a step                 */
+#define TNR_ERR_UNSUPPORTED    7  /* configuration not supported by this build               */
+#define TNR_ERR_NO_DEVICE      8  /* no usable sm_103 GPU                                    */
+
+/* ---- scheme kinds (reference: src/schemes/{trg,btrg,hotrg,hotrg3d}.jl) --- */
+#define TNR_TRG       1   /* trg.jl:85-100     */
+#define TNR_BTRG      2   /* btrg.jl:132-200   */
+#define TNR_HOTRG     3   /* hotrg.jl:27-160   */
+#define TNR_HOTRG_3D  4   /* hotrg3d.jl:27-135 */
+
+/* ---- arithmetic of the bulk contractions -------------------------------- */
+#define TNR_PREC_F64    0  /* plain path: every operation in FP64                      */
+#define TNR_PREC_SPLIT  1  /* contractions as 3xBF16 tcgen05 products, FP32 accumulate;
+                              FP64 small Jacobi, re-orthonormalisation and log-norms  */
+
+typedef struct tnr_handle_s* tnr_handle;
+
+typedef struct tnr_options {
+    int    precision;      /* TNR_PREC_F64 or TNR_PREC_SPLIT                          */
+    double btrg_k;         /* BTRG bond-weight exponent k (btrg.jl:154 default -0.5)   */
+    int    symmetry_n;     /* 1 = Trivial, N = Z_N charges given in leg_charges         */
+    const int32_t* leg_charges; /* sum(dims) ints: charge of each basis index per leg,
+                                   or NULL.  Used to validate charge conservation.     */
+    uint64_t seed;         /* seed of the randomized range finder (0 = default)        */
+    void*  stream;         /* cudaStream_t to run on, or NULL for a private stream      */
+} tnr_options;
+
+/* Fill *opts with defaults (FP64, k=-0.5, Trivial, private stream). */
+void tnr_default_options(tnr_options* opts);
+
+/* Create a scheme from a host tensor.
+ *   kind  : TNR_TRG | TNR_BTRG | TNR_HOTRG (nlegs = 4) or TNR_HOTRG_3D (nlegs = 6)
+ *   dims  : leg dimensions; data: prod(dims) doubles, column-major.
+ * Replaces the constructors TRG(T) (trg.jl:89), BTRG(T, k) (btrg.jl:145-154),
+ * HOTRG(T) (hotrg.jl:31), HOTRG_3D(T) (hotrg3d.jl:31). */
+int tnr_create(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
+               const double* data, const tnr_options* opts);
+
+/* Same, from a device pointer (column-major FP64) already in GPU memory. */
+int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
+                      const double* device_data, const tnr_options* opts);
+
+/* One coarse-graining step with truncrank(chi).
+ * Replaces step!(scheme, trunc) (tnrscheme.jl:2; trg.jl:94, btrg.jl:166,
+ * hotrg.jl:154, hotrg3d.jl:127). */
+int tnr_step(tnr_handle h, int chi);
+
+/* Trace-normalise the tensor and return the norm (synchronises).
+ * Replaces finalize!(scheme) (finalize.jl:4-14,62-66). */
+int tnr_finalize(tnr_handle h, double* norm_out);
+
+/* run!(scheme, truncrank(chi), maxiter(maxiter); finalize_beginning)
+ * (tnrscheme.jl:33-59 with the default Finalizer).  Writes maxiter (+1 when
+ * finalize_beginning) norms into norms_out; *n_out = count written. */
+int tnr_run(tnr_handle h, int chi, int maxiter, int finalize_beginning,
+            double* norms_out, size_t cap, size_t* n_out);
+
+/* free_energy(data, beta; scalefactor, initial_size) (free_energy.jl:13-20). */
+double tnr_free_energy(const double* norms, size_t n, double beta,
+                       double scalefactor, double initial_size);
+
+/* Copy the current tensor to host (column-major); dims_out gets nlegs entries. */
+int tnr_get_tensor(tnr_handle h, double* host_out, size_t cap, int64_t* dims_out, int* nlegs_out);
+
+/* Kept singular values (TRG/BTRG) or kept eigenvalues of the chosen Gram
+ * matrices (HOTRG/HOTRG_3D) of the most recent step, concatenated in the order
+ * the reference computes them; counts[i] = length of decomposition i. */
+int tnr_singular_values(tnr_handle h, double* out, size_t cap, size_t* n_out,
+                        int32_t* counts, size_t counts_cap, size_t* ndec_out);
+
+/* Truncation errors (eps, eps') of the projector choices of the last step
+ * (HOTRG: hotrg.jl:112,148; HOTRG_3D: hotrg3d.jl:97). */
+int tnr_truncation_errors(tnr_handle h, double* out, size_t cap, size_t* n_out);
+
+/* BTRG bond tensors S1 / S2 (diagonals) of the current state. */
+int tnr_btrg_bonds(tnr_handle h, double* s1, size_t cap1, size_t* n1,
+                   double* s2, size_t cap2, size_t* n2);
+
+/* Bytes of device memory the scheme holds now (tensor + workspace). */
+int tnr_device_bytes(tnr_handle h, size_t* bytes_out);
+
+int  tnr_destroy(tnr_handle h);
+int  tnr_last_error(tnr_handle h, char* buf, size_t cap); /* h may be NULL: global */
+const char* tnr_status_string(int status);
+
+/* Device-time measurement on the handle's stream (CUDA events). */
+int tnr_timer_start(tnr_handle h);
+int tnr_timer_stop(tnr_handle h, double* ms_out);
+
+/* ---- batched runs: many independent (model, beta, chi) instances --------- */
+/* Runs run!() on n handles concurrently (one CUDA stream per handle, up to 32
+ * host workers).  norms_out is n*stride doubles; n_out[i] = norms written for
+ * instance i.  device_ms_out (nullable) = device time from the first launch of
+ * the batch to the last completion (CUDA events); latency_ms_out (nullable, n
+ * entries) = host wall time from batch start to completion of instance i.
+ * No reference counterpart: the reference runs one run!() at a time
+ * (tnrscheme.jl:33); this is the batched form of that call. */
+int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter,
+                  int finalize_beginning, double* norms_out, size_t stride,
+                  size_t* n_out, double* device_ms_out, double* latency_ms_out);
+
+/* ---- profiling: CUDA events around every launch of a kernel class -------- */
+#define TNR_PROF_GEMM_BULK 0  /* bulk contraction GEMMs; work = flops               */
+#define TNR_PROF_GEMM_F64  1  /* FP64 GEMMs inside the decompositions; work = flops */
+#define TNR_PROF_JACOBI    2  /* Jacobi eigensolver; work = r^3                     */
+#define TNR_PROF_CHOL      3  /* Cholesky + inverse; work = r^3                     */
+#define TNR_PROF_PERMUTE   4  /* leg permutes; work = bytes read + written          */
+#define TNR_PROF_SPLIT     5  /* FP64 -> 3xBF16 operand split; work = bytes         */
+int tnr_profile_enable(int on);
+int tnr_profile_reset(void);
+int tnr_profile_read(int cls, uint64_t* launches, double* total_ms, double* work);
+
+/* ---- diagnostics: one bulk GEMM through the engine's kernels ------------- */
+/* C (m x n) = op(A) op(B) for `batch` strided problems, host buffers,
+ * column-major.  precision TNR_PREC_SPLIT runs the tcgen05 3xBF16 kernel and
+ * returns TNR_ERR_UNSUPPORTED when that kernel declines the shape; TNR_PREC_F64
+ * runs the FP64 kernel.  No reference counterpart (parity test of the
+ * contraction kernels). */
+int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k,
+                   const double* A, int64_t lda, int64_t strideA,
+                   const double* B, int64_t ldb, int64_t strideB,
+                   double* C, int64_t ldc, int64_t strideC, int batch);
+
+/* ---- library info ------------------------------------------------------- */
+int tnr_device_info(int* sm_count, int* cc_major, int* cc_minor, size_t* hbm_bytes);
+const char* tnr_version(void);
+
+/* Kernel-launch counter of this process (every kernel the library launched). */
+uint64_t tnr_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TNR_GB300_H */

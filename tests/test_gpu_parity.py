@@ -1,0 +1,190 @@
+"""GPU parity of the plain FP64 path against the CPU oracle (through the C ABI).
+
+Bar (plain path): every returned norm within 1e-10 relative, every kept singular
+value / Gram eigenvalue within 1e-10 of the largest one of its decomposition
+(normwise relative: the reference's LAPACK has the same absolute error scale),
+and the README golden free energy of BTRG chi=16.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NORM_RTOL = 1e-10
+SVAL_TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def tnr():
+    import __graft_entry__ as ge
+    ge.build()
+    return ge.package()
+
+
+def _pair(tnr, o, cls, T, To, chi, n, **kw):
+    s = getattr(tnr, cls)(T, **kw)
+    so = getattr(o, cls)(To, **({"k": kw["k"]} if "k" in kw else {}))
+    d = tnr.run(s, tnr.truncrank(chi), tnr.maxiter(n))
+    do = o.run(so, o.truncrank(chi), o.maxiter(n))
+    return s, so, np.array(d), np.array(do)
+
+
+def _check_svals(s, so, nlast):
+    got = s.singular_values()
+    ref = so.svals[-nlast:]
+    assert len(got) == len(ref)
+    for g, r in zip(got, ref):
+        r = np.asarray(r)[:len(g)]
+        assert len(g) == len(r)
+        np.testing.assert_allclose(g, r, rtol=0, atol=SVAL_TOL * max(abs(r[0]), 1e-300))
+
+
+def test_trg_ising_chi16(tnr, oracle):
+    o = oracle
+    s, so, d, do = _pair(tnr, o, "TRG", tnr.classical_ising("Trivial"), o.classical_ising(symmetry="Trivial"), 16, 25)
+    assert len(d) == 26
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+    _check_svals(s, so, 2)
+    f, fo = tnr.free_energy(d, tnr.ising_βc), o.free_energy(do, o.ISING_BETA_C)
+    assert f == pytest.approx(fo, rel=1e-12)
+    assert f == pytest.approx(o.F_ONSAGER, rel=1e-3)       # test/models.jl:5-39
+
+
+def test_btrg_readme_golden(tnr, oracle):
+    # README.md:78-93: BTRG, Z2 Ising at beta_c, truncrank(16), maxiter(25)
+    o = oracle
+    s, so, d, do = _pair(tnr, o, "BTRG", tnr.classical_ising("Z2"), o.classical_ising(symmetry="Z2"), 16, 25)
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+    f = tnr.free_energy(d, tnr.ising_βc)
+    assert f == pytest.approx(-2.1096504926141826902647832, rel=1e-12)
+    _check_svals(s, so, 2)
+    s1, s2 = s.S1, s.S2
+    np.testing.assert_allclose(np.sort(s1), np.sort(so.S1), rtol=1e-8)
+    np.testing.assert_allclose(np.sort(s2), np.sort(so.S2), rtol=1e-8)
+
+
+def test_hotrg_ising_chi16(tnr, oracle):
+    o = oracle
+    s, so, d, do = _pair(tnr, o, "HOTRG", tnr.classical_ising("Z2"), o.classical_ising(symmetry="Trivial"), 16, 12)
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+    _check_svals(s, so, 2)
+
+
+def test_hotrg3d_ising(tnr, oracle):
+    o = oracle
+    s, so, d, do = _pair(tnr, o, "HOTRG_3D", tnr.classical_ising_3D(), o.classical_ising_3D(symmetry="Trivial")
+                         if False else o.classical_ising_3D(), 4, 5)
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+    _check_svals(s, so, 6)
+
+
+# chi chosen so that no exactly degenerate pair (charge sectors c and -c) is cut in these
+# 10 steps: potts3 cuts one at chi = 13, clock6 at chi = 12
+@pytest.mark.parametrize("model,chi", [("potts3", 12), ("clock6", 13)])
+def test_zn_models_trg(tnr, oracle, model, chi):
+    o = oracle
+    if model == "potts3":
+        T, To, beta = tnr.classical_potts(3), o.classical_potts(3), tnr.potts_βc(3)
+    else:
+        T, To, beta = tnr.classical_clock(6, 0.7), o.classical_clock(6, 0.7), 0.7
+    s, so, d, do = _pair(tnr, o, "TRG", T, To, chi, 10)
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+
+
+def test_cut_through_degenerate_pair(tnr, oracle):
+    """Clock Z6 spectra come in exactly degenerate pairs (charge sectors c and -c); truncrank(12)
+    cuts one, so the kept subspace depends on tie-breaking (the reference's order is not
+    visible): parity is unpinned there and only the free energy is held, to 1e-4."""
+    o = oracle
+    s, so, d, do = _pair(tnr, o, "TRG", tnr.classical_clock(6, 0.7), o.classical_clock(6, 0.7), 12, 10)
+    f, fo = tnr.free_energy(d, 0.7), o.free_energy(do, 0.7)
+    assert f == pytest.approx(fo, rel=1e-4)
+
+
+def test_btrg_clock6(tnr, oracle):
+    o = oracle
+    s, so, d, do = _pair(tnr, o, "BTRG", tnr.classical_clock(6, 1.1), o.classical_clock(6, 1.1), 12, 10)
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+
+
+@pytest.mark.parametrize("chi,seed", [(16, 1), (32, 1)])
+def test_hotrg_random_single_step(tnr, oracle, chi, seed):
+    """One HOTRG step on the seeded random chi^4 tensor (the single-step workload, small chi)."""
+    o = oracle
+    T, To = tnr.random_hotrg_tensor(chi, seed), o.random_hotrg_tensor(chi, seed)
+    s = tnr.HOTRG(T)
+    so = o.HOTRG(To)
+    tnr.step(s, tnr.truncrank(chi))
+    o.step(so, chi)
+    n, no = tnr.finalize(s), o.finalize(so)
+    assert n == pytest.approx(no, rel=NORM_RTOL)
+    _check_svals(s, so, 2)
+    eps = s.truncation_errors()
+    ref = np.array([x for pair in so.eps for x in pair])
+    np.testing.assert_allclose(eps, ref, rtol=1e-6)
+
+
+def test_edge_cases(tnr, oracle):
+    o = oracle
+    T, To = tnr.classical_ising("Trivial"), o.classical_ising(symmetry="Trivial")
+    # chi = 1, maxiter(0) runs the body once, finalize_beginning=False
+    s = tnr.TRG(T)
+    d = tnr.run(s, tnr.truncrank(1), tnr.maxiter(0), finalize_beginning=False)
+    do = o.run(o.TRG(To), o.truncrank(1), o.maxiter(0), finalize_beginning=False)
+    assert len(d) == len(do) == 1
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+    # chi above every bond dimension reached: no truncation in the first steps
+    s = tnr.HOTRG(T)
+    d = tnr.run(s, tnr.truncrank(200), tnr.maxiter(2))
+    do = o.run(o.HOTRG(To), o.truncrank(200), o.maxiter(2))
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+    # step / finalize one at a time equals run
+    s = tnr.BTRG(T)
+    so = o.BTRG(To)
+    a = [tnr.finalize(s)] + [(tnr.step(s, tnr.truncrank(8)), tnr.finalize(s))[1] for _ in range(5)]
+    b = o.run(so, o.truncrank(8), o.maxiter(5))
+    np.testing.assert_allclose(a, b, rtol=NORM_RTOL)
+    # invalid chi is refused with a status, the handle stays usable
+    with pytest.raises(tnr.TNRError):
+        tnr.step(s, tnr.truncrank(0))
+    tnr.step(s, tnr.truncrank(8))
+
+
+def test_batch_equals_single(tnr):
+    betas = [0.35, 0.44, 0.52]
+    chis = [8, 12, 16]
+    schemes = [tnr.BTRG(tnr.classical_ising("Trivial", b)) for b in betas]
+    out = tnr.run_batch(schemes, chis, [10, 10, 10])
+    for b, chi, d in zip(betas, chis, out):
+        s = tnr.BTRG(tnr.classical_ising("Trivial", b))
+        ref = tnr.run(s, tnr.truncrank(chi), tnr.maxiter(10))
+        np.testing.assert_allclose(d, ref, rtol=1e-12)
+
+
+@pytest.mark.parametrize("m,n,k,ta,tb,batch", [
+    (256, 256, 256, False, False, 1),
+    (300, 200, 77, False, True, 1),
+    (129, 135, 520, True, False, 1),
+    (2304, 96, 2304, True, True, 1),
+    (64, 4096, 256, False, False, 3),
+])
+def test_split_gemm_tc(tnr, m, n, k, ta, tb, batch):
+    """tcgen05 3xBF16 GEMM (six plane products, FP32 accumulation) against FP64:
+    normwise relative error below 2e-7 (24-bit operands, FP32 accumulator)."""
+    rng = np.random.default_rng(7)
+    sa = (batch, k, m) if ta else (batch, m, k)
+    sb = (batch, n, k) if tb else (batch, k, n)
+    A = rng.standard_normal(sa)
+    B = rng.standard_normal(sb)
+    if batch == 1:
+        A, B = A[0], B[0]
+    got = tnr.debug_gemm(A, B, ta, tb, tnr.PREC_SPLIT)
+    opA = np.swapaxes(A, -1, -2) if ta else A
+    opB = np.swapaxes(B, -1, -2) if tb else B
+    ref = opA @ opB
+    err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert err < 2e-7, err
+    f64 = tnr.debug_gemm(A, B, ta, tb, tnr.PREC_F64)
+    assert np.linalg.norm(f64 - ref) / np.linalg.norm(ref) < 1e-14

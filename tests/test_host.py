@@ -1,0 +1,100 @@
+"""CPU-only checks: the C-ABI library loads and exports every declared symbol,
+error paths return status codes without a GPU, and the host-side model
+constructors match the oracle's."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def tnr():
+    import __graft_entry__ as ge
+    ge.build()
+    return ge.package()
+
+
+def header_symbols():
+    syms = []
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", f)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            syms += re.findall(r"\b(tnr_[a-z0-9_]+)\s*\(", txt)
+    return sorted(set(syms))
+
+
+def test_library_exports_header(tnr):
+    lib = ctypes.CDLL(tnr.LIB_PATH)
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) <= set(tnr.EXPORTS)
+
+
+def test_status_strings(tnr):
+    L = tnr.lib()
+    assert L.tnr_status_string(0) == b"ok"
+    assert L.tnr_status_string(5) == b"admission refused"
+    assert b"sm_103a" in L.tnr_version()
+
+
+def test_free_energy_host(tnr, oracle):
+    data = [1.5, 2.25, 3.0, 0.75]
+    for sf, init in [(2.0, 1.0), (4.0, 1.0), (8.0, 2.0)]:
+        assert tnr.free_energy(data, 0.4, sf, init) == pytest.approx(
+            oracle.free_energy(data, 0.4, sf, init), rel=1e-15)
+
+
+def test_create_rejects_bad_input(tnr):
+    # invalid arguments are refused before any device work
+    with pytest.raises(ValueError):
+        tnr.TRG(np.ones((2, 2, 2)))
+    bad = np.ones((2, 2, 2, 2))
+    bad[0, 0, 0, 0] = np.nan
+    with pytest.raises(tnr.TNRError):
+        tnr.TRG(bad)
+
+
+def test_no_device_is_an_error_not_a_crash(tnr):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(tnr.TNRError) as e:
+        tnr.TRG(tnr.classical_ising())
+    assert e.value.status in (8, 4)
+
+
+@pytest.mark.parametrize("name", ["ising", "ising_triv", "potts3", "clock6", "clock3", "ising3d"])
+def test_models_match_oracle(tnr, oracle, name):
+    o = oracle
+    if name == "ising":
+        a, b = tnr.classical_ising("Z2"), o.classical_ising(symmetry="Z2")
+    elif name == "ising_triv":
+        a, b = tnr.classical_ising("Trivial", 0.37), o.classical_ising(0.37, "Trivial")
+    elif name == "potts3":
+        a, b = tnr.classical_potts(3, 0.8), o.classical_potts(3, 0.8)
+    elif name == "clock6":
+        a, b = tnr.classical_clock(6, 0.9), o.classical_clock(6, 0.9)
+    elif name == "clock3":
+        a, b = tnr.classical_clock(3, 0.9, "Trivial"), o.classical_clock(3, 0.9, "Trivial")
+    else:
+        a, b = tnr.classical_ising_3D(), o.classical_ising_3D()
+    np.testing.assert_allclose(a.array, b.a, rtol=1e-13, atol=1e-14)
+    if b.q is not None:
+        for qa, qb, l in zip(a.charges, b.q, range(b.a.ndim)):
+            # the package stores plain charges; the oracle stores signed ones (domain legs negated)
+            sign = 1 if (l < 2 or b.a.ndim == 6) else -1
+            np.testing.assert_array_equal(qa % b.N, (sign * qb) % b.N)
+
+
+def test_random_hotrg_tensor(tnr, oracle):
+    a = tnr.random_hotrg_tensor(6, 3)
+    b = oracle.random_hotrg_tensor(6, 3)
+    np.testing.assert_allclose(a.array, b.a, rtol=1e-14)
+    assert np.linalg.norm(a.array) == pytest.approx(1.0)

@@ -1,0 +1,395 @@
+"""GB300-native coarse-graining engine with TNRKit.jl's API (host side, Python).
+
+Mirrors the reference's user-facing interface for the hot path:
+
+    T = classical_ising()                 # src/models/ising.jl
+    scheme = BTRG(T)                      # src/schemes/btrg.jl
+    data = run(scheme, truncrank(16), maxiter(25))      # run! (tnrscheme.jl:33-59)
+    f = free_energy(data, ising_βc)       # src/utility/free_energy.jl
+
+Every step runs as sm_103a CUDA inside ``libtnr_gb300.so`` behind the C ABI of
+``include/tnr_gb300.h``; the tensor stays resident in GPU memory between calls.
+There is no CPU fallback: without the library or a GPU the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from .models import (SymTensor, classical_clock, classical_ising, classical_ising_3D, classical_potts,  # noqa: F401
+                     f_onsager, ising_beta_c, ising_beta_c_3D, ising_βc, ising_βc_3D, potts_beta_c, potts_βc,
+                     random_hotrg_tensor)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtnr_gb300.so")
+
+TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D = 1, 2, 3, 4
+PREC_F64, PREC_SPLIT = 0, 1
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "iteration cap reached",
+          4: "CUDA error", 5: "admission refused", 6: "non-finite value", 7: "unsupported", 8: "no device"}
+
+EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step", "tnr_finalize", "tnr_run",
+           "tnr_free_energy", "tnr_get_tensor", "tnr_singular_values", "tnr_truncation_errors", "tnr_btrg_bonds",
+           "tnr_device_bytes", "tnr_destroy", "tnr_last_error", "tnr_status_string", "tnr_timer_start",
+           "tnr_timer_stop", "tnr_run_batch", "tnr_device_info", "tnr_version", "tnr_kernel_launches",
+           "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm"]
+
+
+class TNRError(RuntimeError):
+    """A non-zero status from the C ABI (the reference raises a Julia exception here)."""
+
+    def __init__(self, status, msg):
+        super().__init__("%s (status %d): %s" % (STATUS.get(status, "?"), status, msg))
+        self.status = status
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("btrg_k", C.c_double), ("symmetry_n", C.c_int),
+                ("leg_charges", C.POINTER(C.c_int32)), ("seed", C.c_uint64), ("stream", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the in-tree shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libtnr_gb300.so is not built: run tnrkit.jl_gb300/build.py (nvcc, sm_103a)")
+    L = C.CDLL(LIB_PATH)
+    P, I, D, Z = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+    pd, pi64, pz = C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_size_t)
+    sig = {
+        "tnr_default_options": (None, [C.POINTER(Options)]),
+        "tnr_create": (I, [C.POINTER(P), I, I, pi64, pd, C.POINTER(Options)]),
+        "tnr_create_device": (I, [C.POINTER(P), I, I, pi64, P, C.POINTER(Options)]),
+        "tnr_step": (I, [P, I]),
+        "tnr_finalize": (I, [P, pd]),
+        "tnr_run": (I, [P, I, I, I, pd, Z, pz]),
+        "tnr_free_energy": (D, [pd, Z, D, D, D]),
+        "tnr_get_tensor": (I, [P, pd, Z, pi64, C.POINTER(I)]),
+        "tnr_singular_values": (I, [P, pd, Z, pz, C.POINTER(C.c_int32), Z, pz]),
+        "tnr_truncation_errors": (I, [P, pd, Z, pz]),
+        "tnr_btrg_bonds": (I, [P, pd, Z, pz, pd, Z, pz]),
+        "tnr_device_bytes": (I, [P, pz]),
+        "tnr_destroy": (I, [P]),
+        "tnr_last_error": (I, [P, C.c_char_p, Z]),
+        "tnr_status_string": (C.c_char_p, [I]),
+        "tnr_timer_start": (I, [P]),
+        "tnr_timer_stop": (I, [P, pd]),
+        "tnr_run_batch": (I, [C.POINTER(P), I, C.POINTER(I), C.POINTER(I), I, pd, Z, pz, pd, pd]),
+        "tnr_profile_enable": (I, [I]),
+        "tnr_profile_reset": (I, []),
+        "tnr_profile_read": (I, [I, C.POINTER(C.c_uint64), pd, pd]),
+        "tnr_debug_gemm": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, pd, C.c_int64, C.c_int64, pd, C.c_int64,
+                               C.c_int64, pd, C.c_int64, C.c_int64, I]),
+        "tnr_device_info": (I, [C.POINTER(I), C.POINTER(I), C.POINTER(I), pz]),
+        "tnr_version": (C.c_char_p, []),
+        "tnr_kernel_launches": (C.c_uint64, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _err(h=None):
+    buf = C.create_string_buffer(1024)
+    lib().tnr_last_error(h, buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _check(st, h=None):
+    if st != 0:
+        raise TNRError(st, _err(h))
+
+
+@dataclass
+class truncrank:
+    """MatrixAlgebraKit ``truncrank(howmany)``: keep the ``howmany`` largest values."""
+    howmany: int
+
+
+@dataclass
+class maxiter:
+    """``maxiter(n)`` (src/utility/stopping.jl:3-5,18): continue while steps < n."""
+    n: int
+
+    def __call__(self, steps, data):
+        return steps < self.n
+
+
+def _as_sym(T):
+    if isinstance(T, SymTensor):
+        return T
+    return SymTensor(np.asarray(T, dtype=np.float64), None, 1)
+
+
+class _Scheme:
+    kind = 0
+    nlegs = 4
+    scalefactor = 2.0
+
+    def __init__(self, T, precision=PREC_F64, k=-0.5, seed=0, stream=None):
+        T = _as_sym(T)
+        a = np.asarray(T.array, dtype=np.float64)
+        if a.ndim != self.nlegs:
+            raise ValueError("%s needs a %d-leg tensor" % (type(self).__name__, self.nlegs))
+        L = lib()
+        o = Options()
+        L.tnr_default_options(C.byref(o))
+        o.precision = precision
+        o.btrg_k = k
+        o.seed = seed
+        o.stream = stream
+        keep = None
+        if T.charges is not None and T.N > 1:
+            keep = np.ascontiguousarray(np.concatenate([np.asarray(c, dtype=np.int32) for c in T.charges]))
+            o.symmetry_n = T.N
+            o.leg_charges = keep.ctypes.data_as(C.POINTER(C.c_int32))
+        dims = (C.c_int64 * a.ndim)(*a.shape)
+        data = np.asfortranarray(a)                     # column-major, first leg fastest
+        h = C.c_void_p()
+        st = L.tnr_create(C.byref(h), self.kind, a.ndim, dims, data.ctypes.data_as(C.POINTER(C.c_double)),
+                          C.byref(o))
+        _check(st)
+        self._h = h
+        self.precision = precision
+        self.symmetry_n = T.N
+
+    # --- reference fields -------------------------------------------------
+    @property
+    def T(self):
+        """Current tensor as a host array indexed like the reference (T[i1, i2, ...])."""
+        L = lib()
+        dims = (C.c_int64 * 8)()
+        n = C.c_int()
+        _check(L.tnr_get_tensor(self._h, None, 0, dims, C.byref(n)), self._h)
+        shape = tuple(dims[i] for i in range(n.value))
+        out = np.empty(int(np.prod(shape)), dtype=np.float64)
+        _check(L.tnr_get_tensor(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), out.size, dims, C.byref(n)),
+               self._h)
+        return out.reshape(shape, order="F")
+
+    def singular_values(self):
+        """Kept singular values / Gram eigenvalues of the last step, one array per decomposition."""
+        L = lib()
+        n, nd = C.c_size_t(), C.c_size_t()
+        _check(L.tnr_singular_values(self._h, None, 0, C.byref(n), None, 0, C.byref(nd)), self._h)
+        vals = np.empty(max(n.value, 1))
+        cnt = (C.c_int32 * max(nd.value, 1))()
+        _check(L.tnr_singular_values(self._h, vals.ctypes.data_as(C.POINTER(C.c_double)), vals.size, C.byref(n),
+                                     cnt, nd.value, C.byref(nd)), self._h)
+        out, at = [], 0
+        for i in range(nd.value):
+            out.append(vals[at:at + cnt[i]].copy())
+            at += cnt[i]
+        return out
+
+    def truncation_errors(self):
+        L = lib()
+        n = C.c_size_t()
+        _check(L.tnr_truncation_errors(self._h, None, 0, C.byref(n)), self._h)
+        out = np.empty(max(n.value, 1))
+        _check(L.tnr_truncation_errors(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), out.size, C.byref(n)),
+               self._h)
+        return out[:n.value]
+
+    def device_bytes(self):
+        b = C.c_size_t()
+        _check(lib().tnr_device_bytes(self._h, C.byref(b)), self._h)
+        return b.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tnr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TRG(_Scheme):
+    """Tensor Renormalization Group (src/schemes/trg.jl:85-100); rescales by sqrt(2)."""
+    kind = TNR_TRG
+
+
+class BTRG(_Scheme):
+    """Bond-weighted TRG (src/schemes/btrg.jl:132-200); ``BTRG(T, k=-0.5)``."""
+    kind = TNR_BTRG
+
+    def __init__(self, T, k=-0.5, **kw):
+        super().__init__(T, k=k, **kw)
+        self.k = k
+
+    @property
+    def S1(self):
+        return self._bonds()[0]
+
+    @property
+    def S2(self):
+        return self._bonds()[1]
+
+    def _bonds(self):
+        L = lib()
+        n1, n2 = C.c_size_t(), C.c_size_t()
+        _check(L.tnr_btrg_bonds(self._h, None, 0, C.byref(n1), None, 0, C.byref(n2)), self._h)
+        a, b = np.empty(n1.value), np.empty(n2.value)
+        _check(L.tnr_btrg_bonds(self._h, a.ctypes.data_as(C.POINTER(C.c_double)), a.size, C.byref(n1),
+                                b.ctypes.data_as(C.POINTER(C.c_double)), b.size, C.byref(n2)), self._h)
+        return a, b
+
+
+class HOTRG(_Scheme):
+    """Higher-Order TRG (src/schemes/hotrg.jl:27-160); rescales by 2 (area factor 4)."""
+    kind = TNR_HOTRG
+    scalefactor = 4.0
+
+
+class HOTRG_3D(_Scheme):
+    """3D HOTRG (src/schemes/hotrg3d.jl:27-135); volume factor 8 per step."""
+    kind = TNR_HOTRG_3D
+    nlegs = 6
+    scalefactor = 8.0
+
+
+def step(scheme, trunc):
+    """``step!(scheme, truncrank(chi))``"""
+    _check(lib().tnr_step(scheme._h, int(trunc.howmany)), scheme._h)
+    return scheme
+
+
+def finalize(scheme):
+    """``finalize!(scheme)``: trace norm n, T /= n; returns n."""
+    n = C.c_double()
+    _check(lib().tnr_finalize(scheme._h, C.byref(n)), scheme._h)
+    return n.value
+
+
+def run(scheme, trunc, crit, finalize_beginning=True, verbosity=0):
+    """``run!(scheme, trunc, maxiter(n); finalize_beginning)`` with the default Finalizer.
+
+    Returns the list of norms (n + 1 with ``finalize_beginning``)."""
+    if not isinstance(crit, maxiter):
+        raise TypeError("only maxiter(n) runs on the device path")
+    nsteps = max(crit.n, 1)
+    cap = nsteps + 1
+    out = np.empty(cap)
+    n = C.c_size_t()
+    _check(lib().tnr_run(scheme._h, int(trunc.howmany), int(crit.n), 1 if finalize_beginning else 0,
+                         out.ctypes.data_as(C.POINTER(C.c_double)), cap, C.byref(n)), scheme._h)
+    return list(out[:n.value])
+
+
+run_ = run   # run! in Julia
+
+
+def run_batch(schemes, chis, maxiters, finalize_beginning=True, timing=None):
+    """Runs ``run!`` on many independent schemes concurrently; returns one norm list per scheme.
+
+    If ``timing`` is a dict it receives ``device_ms`` (CUDA-event span of the batch) and
+    ``latency_ms`` (per-instance completion times from batch start)."""
+    n = len(schemes)
+    stride = max(max(int(m), 1) for m in maxiters) + 1
+    out = np.empty(n * stride)
+    cnt = (C.c_size_t * n)()
+    hs = (C.c_void_p * n)(*[s._h for s in schemes])
+    ch = (C.c_int * n)(*[int(x) for x in chis])
+    mi = (C.c_int * n)(*[int(x) for x in maxiters])
+    dev_ms = C.c_double()
+    lat = np.zeros(n)
+    st = lib().tnr_run_batch(hs, n, ch, mi, 1 if finalize_beginning else 0,
+                             out.ctypes.data_as(C.POINTER(C.c_double)), stride, cnt,
+                             C.byref(dev_ms), lat.ctypes.data_as(C.POINTER(C.c_double)))
+    _check(st)
+    if timing is not None:
+        timing["device_ms"] = dev_ms.value
+        timing["latency_ms"] = lat
+    return [list(out[i * stride:i * stride + cnt[i]]) for i in range(n)]
+
+
+PROFILE_CLASSES = {"gemm_bulk": 0, "gemm_f64": 1, "jacobi": 2, "chol": 3, "permute": 4, "split": 5}
+
+
+def profile_enable(on=True):
+    _check(lib().tnr_profile_enable(1 if on else 0))
+
+
+def profile_reset():
+    _check(lib().tnr_profile_reset())
+
+
+def profile_read():
+    """{class: (launches, total_ms, work)} of the launches recorded since the last reset."""
+    out = {}
+    for name, cls in PROFILE_CLASSES.items():
+        n, ms, w = C.c_uint64(), C.c_double(), C.c_double()
+        _check(lib().tnr_profile_read(cls, C.byref(n), C.byref(ms), C.byref(w)))
+        out[name] = (n.value, ms.value, w.value)
+    return out
+
+
+def free_energy(data, beta, scalefactor=2.0, initial_size=1.0):
+    """``free_energy(data, β; scalefactor, initial_size)`` (src/utility/free_energy.jl:13-20)."""
+    a = np.ascontiguousarray(np.asarray(data, dtype=np.float64))
+    return lib().tnr_free_energy(a.ctypes.data_as(C.POINTER(C.c_double)), a.size, float(beta), float(scalefactor),
+                                 float(initial_size))
+
+
+def debug_gemm(A, B, ta=False, tb=False, precision=PREC_SPLIT):
+    """op(A) @ op(B) through the engine's GEMM kernel (batched if A, B are 3-D: [batch, rows, cols])."""
+    A3 = np.atleast_3d(A) if A.ndim == 3 else A[None]
+    B3 = np.atleast_3d(B) if B.ndim == 3 else B[None]
+    batch = A3.shape[0]
+    # column-major storage of each stored matrix, batches contiguous
+    Af = np.ascontiguousarray(np.transpose(A3, (0, 2, 1)))
+    Bf = np.ascontiguousarray(np.transpose(B3, (0, 2, 1)))
+    ar, ac = A3.shape[1:]
+    br, bc = B3.shape[1:]
+    m, k = (ac, ar) if ta else (ar, ac)
+    kb, n = (bc, br) if tb else (br, bc)
+    assert k == kb
+    Cf = np.zeros((batch, n, m))
+    st = lib().tnr_debug_gemm(precision, int(ta), int(tb), m, n, k, Af.ctypes.data_as(C.POINTER(C.c_double)), ar,
+                              ar * ac if batch > 1 else 0, Bf.ctypes.data_as(C.POINTER(C.c_double)), br,
+                              br * bc if batch > 1 else 0, Cf.ctypes.data_as(C.POINTER(C.c_double)), m, m * n, batch)
+    _check(st)
+    out = np.transpose(Cf, (0, 2, 1))
+    return out if A.ndim == 3 else out[0]
+
+
+def device_info():
+    sm, ma, mi, hbm = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+    _check(lib().tnr_device_info(C.byref(sm), C.byref(ma), C.byref(mi), C.byref(hbm)))
+    return {"sm_count": sm.value, "cc": (ma.value, mi.value), "hbm_bytes": hbm.value}
+
+
+def kernel_launches():
+    return int(lib().tnr_kernel_launches())
+
+
+class Timer:
+    """Device time on a scheme's stream (CUDA events)."""
+
+    def __init__(self, scheme):
+        self.s = scheme
+
+    def __enter__(self):
+        _check(lib().tnr_timer_start(self.s._h), self.s._h)
+        return self
+
+    def __exit__(self, *exc):
+        ms = C.c_double()
+        _check(lib().tnr_timer_stop(self.s._h, C.byref(ms)), self.s._h)
+        self.ms = ms.value
+        return False

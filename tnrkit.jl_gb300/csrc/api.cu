@@ -1,0 +1,433 @@
+// C ABI of the engine (include/tnr_gb300.h).  Every entry point catches
+// exceptions and returns a status code; nothing aborts the process.
+#include "schemes.cuh"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <thread>
+
+using namespace tnr;
+
+struct tnr_handle_s {
+    Scheme s;
+};
+
+namespace {
+thread_local std::string g_err;
+
+int fail(tnr_handle h, int code, const std::string& msg) {
+    g_err = msg;
+    if (h) h->s.err = msg;
+    return code;
+}
+
+template <class F>
+int guarded(tnr_handle h, F&& f) {
+    try {
+        f();
+        return TNR_OK;
+    } catch (const Error& e) {
+        return fail(h, e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(h, TNR_ERR_OOM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(h, TNR_ERR_CUDA, e.what());
+    }
+}
+
+void require_device() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        throw Error(TNR_ERR_NO_DEVICE, "no CUDA device available");
+    }
+}
+
+void validate_charges(int kind, int nlegs, const int64_t* dims, const double* host, const tnr_options* o) {
+    if (!o || o->symmetry_n <= 1 || !o->leg_charges || !host) return;
+    // signed charges: codomain legs (2 for every scheme here) +q, domain legs -q
+    const int N = o->symmetry_n;
+    const int nout = 2;
+    std::vector<int64_t> off(nlegs + 1, 0);
+    for (int l = 0; l < nlegs; ++l) off[l + 1] = off[l] + dims[l];
+    int64_t total = 1;
+    for (int l = 0; l < nlegs; ++l) total *= dims[l];
+    double maxabs = 0;
+    for (int64_t e = 0; e < total; ++e) maxabs = std::max(maxabs, std::fabs(host[e]));
+    for (int64_t e = 0; e < total; ++e) {
+        int64_t rem = e;
+        int q = 0;
+        for (int l = 0; l < nlegs; ++l) {
+            int64_t i = rem % dims[l];
+            rem /= dims[l];
+            int ch = o->leg_charges[off[l] + i];
+            q += (l < nout) ? ch : -ch;
+        }
+        q = ((q % N) + N) % N;
+        if (q != 0 && std::fabs(host[e]) > 1e-12 * maxabs)
+            throw Error(TNR_ERR_INVALID_ARG, "tensor violates Z_N charge conservation of the given leg charges");
+    }
+    (void)kind;
+}
+
+int create_common(tnr_handle* out, int kind, int nlegs, const int64_t* dims, const double* data, bool device,
+                  const tnr_options* opts) {
+    tnr_options o;
+    tnr_default_options(&o);
+    if (opts) o = *opts;
+    if (!out) return fail(nullptr, TNR_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (kind < TNR_TRG || kind > TNR_HOTRG_3D) return fail(nullptr, TNR_ERR_INVALID_ARG, "unknown scheme kind");
+    int want = kind == TNR_HOTRG_3D ? 6 : 4;
+    if (nlegs != want || !dims || !data)
+        return fail(nullptr, TNR_ERR_INVALID_ARG, "scheme needs a " + std::to_string(want) + "-leg tensor");
+    for (int l = 0; l < nlegs; ++l)
+        if (dims[l] < 1) return fail(nullptr, TNR_ERR_INVALID_ARG, "leg dimension < 1");
+    if (o.precision != TNR_PREC_F64 && o.precision != TNR_PREC_SPLIT)
+        return fail(nullptr, TNR_ERR_INVALID_ARG, "unknown precision");
+    tnr_handle h = new (std::nothrow) tnr_handle_s();
+    if (!h) return fail(nullptr, TNR_ERR_OOM, "host allocation failed");
+    int st = guarded(h, [&] {
+        require_device();
+        if (!device) {
+            for (int64_t e = 0, t = [&] { int64_t p = 1; for (int l = 0; l < nlegs; ++l) p *= dims[l]; return p; }();
+                 e < t; ++e)
+                TNR_REQUIRE(std::isfinite(data[e]), TNR_ERR_NONFINITE, "non-finite entry in the input tensor");
+            validate_charges(kind, nlegs, dims, data, &o);
+        }
+        Scheme& s = h->s;
+        s.kind = kind;
+        s.btrg_k = o.btrg_k;
+        s.ctx.reset(new Ctx((cudaStream_t)o.stream, o.precision, o.seed));
+        std::vector<int64_t> dv(dims, dims + nlegs);
+        s.T = make_dt(s.ctx->pool.get(), dv);
+        TNR_CUDA(cudaMemcpyAsync(s.T.p(), data, s.T.size() * sizeof(double),
+                                 device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s.ctx->stream));
+        if (kind == TNR_BTRG) {
+            // S1 = id(space(T, 2)), S2 = id(space(T, 1))  (btrg.jl:145-150)
+            s.S1 = make_dt(s.ctx->pool.get(), {dims[1]});
+            s.S2 = make_dt(s.ctx->pool.get(), {dims[0]});
+            std::vector<double> ones((size_t)std::max(dims[0], dims[1]), 1.0);
+            TNR_CUDA(cudaMemcpyAsync(s.S1.p(), ones.data(), dims[1] * sizeof(double), cudaMemcpyHostToDevice, s.ctx->stream));
+            TNR_CUDA(cudaMemcpyAsync(s.S2.p(), ones.data(), dims[0] * sizeof(double), cudaMemcpyHostToDevice, s.ctx->stream));
+        }
+        s.ctx->sync();
+    });
+    if (st != TNR_OK) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return TNR_OK;
+}
+}  // namespace
+
+extern "C" {
+
+void tnr_default_options(tnr_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = TNR_PREC_F64;
+    o->btrg_k = -0.5;
+    o->symmetry_n = 1;
+}
+
+int tnr_create(tnr_handle* out, int kind, int nlegs, const int64_t* dims, const double* data, const tnr_options* opts) {
+    return create_common(out, kind, nlegs, dims, data, false, opts);
+}
+
+int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims, const double* data,
+                      const tnr_options* opts) {
+    return create_common(out, kind, nlegs, dims, data, true, opts);
+}
+
+int tnr_step(tnr_handle h, int chi) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] { h->s.step(chi); });
+}
+
+int tnr_finalize(tnr_handle h, double* norm_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        double n = h->s.finalize();
+        TNR_REQUIRE(std::isfinite(n), TNR_ERR_NONFINITE, "finalize!: non-finite norm");
+        if (norm_out) *norm_out = n;
+    });
+}
+
+int tnr_run(tnr_handle h, int chi, int maxiter, int finalize_beginning, double* norms_out, size_t cap, size_t* n_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        const size_t need = (size_t)std::max(maxiter, 1) + (finalize_beginning ? 1 : 0);
+        TNR_REQUIRE(norms_out && cap >= need, TNR_ERR_INVALID_ARG, "norms_out too small for run!");
+        std::vector<double> v = h->s.run(chi, maxiter, finalize_beginning != 0);
+        std::memcpy(norms_out, v.data(), v.size() * sizeof(double));
+        if (n_out) *n_out = v.size();
+    });
+}
+
+double tnr_free_energy(const double* norms, size_t n, double beta, double scalefactor, double initial_size) {
+    // free_energy.jl:13-20
+    double lnz = 0.0;
+    const double x = 1.0 - std::log(initial_size) / std::log(scalefactor);
+    for (size_t i = 0; i < n; ++i) lnz += std::log(norms[i]) * std::pow(scalefactor, x - (double)(i + 1));
+    return -lnz / beta;
+}
+
+int tnr_get_tensor(tnr_handle h, double* host_out, size_t cap, int64_t* dims_out, int* nlegs_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        if (nlegs_out) *nlegs_out = s.T.rank;
+        if (dims_out)
+            for (int i = 0; i < s.T.rank; ++i) dims_out[i] = s.T.d[i];
+        if (host_out) {
+            TNR_REQUIRE(cap >= (size_t)s.T.size(), TNR_ERR_INVALID_ARG, "host_out too small");
+            TNR_CUDA(cudaMemcpyAsync(host_out, s.T.p(), s.T.size() * sizeof(double), cudaMemcpyDeviceToHost, s.ctx->stream));
+            s.ctx->sync();
+        }
+    });
+}
+
+int tnr_singular_values(tnr_handle h, double* out, size_t cap, size_t* n_out, int32_t* counts, size_t counts_cap,
+                        size_t* ndec_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        if (n_out) *n_out = s.last_vals.size();
+        if (ndec_out) *ndec_out = s.last_counts.size();
+        if (out) {
+            TNR_REQUIRE(cap >= s.last_vals.size(), TNR_ERR_INVALID_ARG, "out too small");
+            std::memcpy(out, s.last_vals.data(), s.last_vals.size() * sizeof(double));
+        }
+        if (counts) {
+            TNR_REQUIRE(counts_cap >= s.last_counts.size(), TNR_ERR_INVALID_ARG, "counts too small");
+            for (size_t i = 0; i < s.last_counts.size(); ++i) counts[i] = s.last_counts[i];
+        }
+    });
+}
+
+int tnr_truncation_errors(tnr_handle h, double* out, size_t cap, size_t* n_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        if (n_out) *n_out = s.last_eps.size();
+        if (out) {
+            TNR_REQUIRE(cap >= s.last_eps.size(), TNR_ERR_INVALID_ARG, "out too small");
+            std::memcpy(out, s.last_eps.data(), s.last_eps.size() * sizeof(double));
+        }
+    });
+}
+
+int tnr_btrg_bonds(tnr_handle h, double* s1, size_t cap1, size_t* n1, double* s2, size_t cap2, size_t* n2) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        TNR_REQUIRE(s.kind == TNR_BTRG, TNR_ERR_INVALID_ARG, "not a BTRG scheme");
+        if (n1) *n1 = (size_t)s.S1.size();
+        if (n2) *n2 = (size_t)s.S2.size();
+        if (s1) {
+            TNR_REQUIRE(cap1 >= (size_t)s.S1.size(), TNR_ERR_INVALID_ARG, "s1 too small");
+            TNR_CUDA(cudaMemcpyAsync(s1, s.S1.p(), s.S1.size() * sizeof(double), cudaMemcpyDeviceToHost, s.ctx->stream));
+        }
+        if (s2) {
+            TNR_REQUIRE(cap2 >= (size_t)s.S2.size(), TNR_ERR_INVALID_ARG, "s2 too small");
+            TNR_CUDA(cudaMemcpyAsync(s2, s.S2.p(), s.S2.size() * sizeof(double), cudaMemcpyDeviceToHost, s.ctx->stream));
+        }
+        s.ctx->sync();
+    });
+}
+
+int tnr_device_bytes(tnr_handle h, size_t* bytes_out) {
+    if (!h || !bytes_out) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
+    *bytes_out = h->s.ctx->pool->held_bytes();
+    return TNR_OK;
+}
+
+int tnr_destroy(tnr_handle h) {
+    if (!h) return TNR_OK;
+    int st = guarded(nullptr, [&] { h->s.ctx->sync(); });
+    delete h;
+    return st;
+}
+
+int tnr_last_error(tnr_handle h, char* buf, size_t cap) {
+    const std::string& m = h ? h->s.err : g_err;
+    if (buf && cap) {
+        size_t n = std::min(cap - 1, m.size());
+        std::memcpy(buf, m.data(), n);
+        buf[n] = 0;
+    }
+    return TNR_OK;
+}
+
+const char* tnr_status_string(int st) {
+    switch (st) {
+        case TNR_OK: return "ok";
+        case TNR_ERR_INVALID_ARG: return "invalid argument";
+        case TNR_ERR_OOM: return "out of device memory";
+        case TNR_ERR_NOT_CONVERGED: return "iteration cap reached";
+        case TNR_ERR_CUDA: return "CUDA error";
+        case TNR_ERR_ADMISSION: return "admission refused";
+        case TNR_ERR_NONFINITE: return "non-finite value";
+        case TNR_ERR_UNSUPPORTED: return "unsupported";
+        case TNR_ERR_NO_DEVICE: return "no device";
+        default: return "unknown status";
+    }
+}
+
+int tnr_timer_start(tnr_handle h) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] { TNR_CUDA(cudaEventRecord(h->s.ctx->ev0, h->s.ctx->stream)); });
+}
+
+int tnr_timer_stop(tnr_handle h, double* ms_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        TNR_CUDA(cudaEventRecord(h->s.ctx->ev1, h->s.ctx->stream));
+        TNR_CUDA(cudaEventSynchronize(h->s.ctx->ev1));
+        float ms = 0;
+        TNR_CUDA(cudaEventElapsedTime(&ms, h->s.ctx->ev0, h->s.ctx->ev1));
+        if (ms_out) *ms_out = ms;
+    });
+}
+
+int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int finalize_beginning, double* norms_out,
+                  size_t stride, size_t* n_out, double* device_ms_out, double* latency_ms_out) {
+    if (!hs || n < 0 || !chi || !maxiter || !norms_out || !n_out)
+        return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL argument");
+    for (int i = 0; i < n; ++i) {
+        if (!hs[i]) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle in batch");
+        size_t need = (size_t)std::max(maxiter[i], 1) + (finalize_beginning ? 1 : 0);
+        if (need > stride) return fail(nullptr, TNR_ERR_INVALID_ARG, "stride too small for run!");
+    }
+    cudaStream_t ts = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<cudaEvent_t> done;
+    int st0 = guarded(nullptr, [&] {
+        if (device_ms_out) {
+            TNR_CUDA(cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking));
+            TNR_CUDA(cudaEventCreate(&e0));
+            TNR_CUDA(cudaEventCreate(&e1));
+            TNR_CUDA(cudaEventRecord(e0, ts));
+            for (int i = 0; i < n; ++i) TNR_CUDA(cudaStreamWaitEvent(hs[i]->s.ctx->stream, e0, 0));
+        }
+    });
+    if (st0 != TNR_OK) return st0;
+    // one host worker per concurrent instance; each handle runs on its own stream
+    const int workers = std::min(n, 32);
+    std::vector<int> status(n, TNR_OK);
+    std::atomic<int> next{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&] {
+        cudaSetDevice(dev);
+        for (;;) {
+            int i = next.fetch_add(1);
+            if (i >= n) break;
+            status[i] = tnr_run(hs[i], chi[i], maxiter[i], finalize_beginning, norms_out + (size_t)i * stride, stride,
+                                n_out + i);
+            if (latency_ms_out)
+                latency_ms_out[i] =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
+    };
+    std::vector<std::thread> th;
+    for (int w = 0; w < workers; ++w) th.emplace_back(work);
+    for (auto& t : th) t.join();
+    int st1 = guarded(nullptr, [&] {
+        if (device_ms_out) {
+            for (int i = 0; i < n; ++i) {
+                cudaEvent_t e;
+                TNR_CUDA(cudaEventCreate(&e));
+                TNR_CUDA(cudaEventRecord(e, hs[i]->s.ctx->stream));
+                TNR_CUDA(cudaStreamWaitEvent(ts, e, 0));
+                done.push_back(e);
+            }
+            TNR_CUDA(cudaEventRecord(e1, ts));
+            TNR_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            TNR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            *device_ms_out = ms;
+        }
+    });
+    for (auto e : done) cudaEventDestroy(e);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (ts) cudaStreamDestroy(ts);
+    for (int i = 0; i < n; ++i)
+        if (status[i] != TNR_OK) {
+            g_err = "instance " + std::to_string(i) + ": " + hs[i]->s.err;
+            return status[i];
+        }
+    return st1;
+}
+
+int tnr_profile_enable(int on) {
+    g_prof_on.store(on != 0);
+    return TNR_OK;
+}
+
+int tnr_profile_reset(void) {
+    return guarded(nullptr, [&] { prof_reset(); });
+}
+
+int tnr_profile_read(int cls, uint64_t* launches, double* total_ms, double* work) {
+    if (cls < 0 || cls >= PROF_NCLASS) return fail(nullptr, TNR_ERR_INVALID_ARG, "unknown profile class");
+    return guarded(nullptr, [&] { prof_read(cls, launches, total_ms, work); });
+}
+
+int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k, const double* A, int64_t lda,
+                   int64_t sA, const double* B, int64_t ldb, int64_t sB, double* C, int64_t ldc, int64_t sC, int batch) {
+    if (!A || !B || !C || m < 1 || n < 1 || k < 1 || batch < 1) return fail(nullptr, TNR_ERR_INVALID_ARG, "bad gemm");
+    return guarded(nullptr, [&] {
+        require_device();
+        Ctx c(nullptr, precision, 0);
+        // extents of the host buffers (last element + 1)
+        auto extent = [](bool t, int64_t rows, int64_t cols, int64_t ld, int64_t stride, int nb) {
+            int64_t r = t ? cols : rows, cc = t ? rows : cols;   // stored shape
+            return (nb - 1) * stride + (cc - 1) * ld + r;
+        };
+        const int64_t eA = extent(ta, m, k, lda, sA, batch), eB = extent(tb, k, n, ldb, sB, batch);
+        const int64_t eC = (batch - 1) * sC + (n - 1) * ldc + m;
+        Buf dA(c.pool.get(), eA * 8), dB(c.pool.get(), eB * 8), dC(c.pool.get(), eC * 8);
+        TNR_CUDA(cudaMemcpyAsync(dA.d(), A, eA * 8, cudaMemcpyHostToDevice, c.stream));
+        TNR_CUDA(cudaMemcpyAsync(dB.d(), B, eB * 8, cudaMemcpyHostToDevice, c.stream));
+        TNR_CUDA(cudaMemsetAsync(dC.d(), 0, eC * 8, c.stream));
+        Batch2 bt;
+        bt.n1 = batch; bt.sA1 = sA; bt.sB1 = sB; bt.sC1 = sC;
+        if (precision == TNR_PREC_SPLIT) {
+            bool ran = gemm_split_tc(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), ldc, bt);
+            TNR_REQUIRE(ran, TNR_ERR_UNSUPPORTED, "split kernel declined this shape");
+        } else {
+            gemm_f64(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), ldc, bt);
+        }
+        TNR_CUDA(cudaMemcpyAsync(C, dC.d(), eC * 8, cudaMemcpyDeviceToHost, c.stream));
+        int st = c.read_status_and_clear();
+        TNR_REQUIRE(st == 0, TNR_ERR_CUDA, "kernel status word " + std::to_string(st));
+    });
+}
+
+int tnr_device_info(int* sm, int* major, int* minor, size_t* hbm) {
+    return guarded(nullptr, [&] {
+        require_device();
+        int dev = 0;
+        TNR_CUDA(cudaGetDevice(&dev));
+        cudaDeviceProp p;
+        TNR_CUDA(cudaGetDeviceProperties(&p, dev));
+        if (sm) *sm = p.multiProcessorCount;
+        if (major) *major = p.major;
+        if (minor) *minor = p.minor;
+        if (hbm) *hbm = p.totalGlobalMem;
+    });
+}
+
+const char* tnr_version(void) { return "tnr-gb300 0.1.0 (sm_103a)"; }
+
+uint64_t tnr_kernel_launches(void) { return g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,257 @@
+// Shared declarations of the GB300 coarse-graining engine (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <map>
+#include <string>
+#include <vector>
+#include <stdexcept>
+#include <atomic>
+#include <memory>
+
+#include "../../include/tnr_gb300.h"
+
+namespace tnr {
+
+// ---------------------------------------------------------------------------
+// errors: C++ exceptions inside the library, status codes at the C ABI
+// ---------------------------------------------------------------------------
+struct Error : public std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define TNR_CUDA(call)                                                              \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            throw ::tnr::Error(e_ == cudaErrorMemoryAllocation ? TNR_ERR_OOM        \
+                                                               : TNR_ERR_CUDA,      \
+                               std::string(#call) + ": " + cudaGetErrorString(e_)); \
+        }                                                                           \
+    } while (0)
+
+#define TNR_REQUIRE(cond, code, msg)                 \
+    do {                                             \
+        if (!(cond)) throw ::tnr::Error((code), (msg)); \
+    } while (0)
+
+// every kernel launch goes through this counter (reported by tnr_kernel_launches)
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(int n = 1) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+inline void check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        throw Error(TNR_ERR_CUDA, std::string("launch ") + what + ": " + cudaGetErrorString(e));
+    count_launch();
+}
+
+// device status word bits written by iterative kernels (never trap, never spin forever)
+enum : int {
+    ST_JACOBI_NOCONV = 1,
+    ST_CHOL_BREAKDOWN = 2,
+    ST_NONFINITE = 4,
+};
+
+int sm_count();
+
+// ---------------------------------------------------------------------------
+// per-kernel-class profiler: CUDA events around launches, algorithmic work units
+// ---------------------------------------------------------------------------
+enum ProfClass : int {
+    PROF_GEMM_BULK = 0,   // bulk contraction GEMMs (FP64 DFMA or split tcgen05), work = flops
+    PROF_GEMM_F64 = 1,    // FP64 GEMMs of the decompositions, work = flops
+    PROF_JACOBI = 2,      // small Jacobi eigensolver, work = r^3
+    PROF_CHOL = 3,        // Cholesky + inverse, work = r^3
+    PROF_PERMUTE = 4,     // leg permutes, work = bytes moved
+    PROF_SPLIT = 5,       // FP64 -> BF16 split conversion, work = bytes moved
+    PROF_NCLASS = 6
+};
+extern std::atomic<bool> g_prof_on;
+int prof_start(cudaStream_t s);
+void prof_stop(int rec, cudaStream_t s, int cls, double work);
+void prof_reset();
+void prof_read(int cls, uint64_t* launches, double* ms, double* work);
+
+// ---------------------------------------------------------------------------
+// caching device allocator (stream-ordered reuse on one stream)
+// ---------------------------------------------------------------------------
+class Pool {
+  public:
+    explicit Pool(cudaStream_t s) : stream_(s) {}
+    ~Pool();
+    void* get(size_t bytes);
+    void put(void* p);
+    size_t held_bytes() const { return held_; }
+    void trim();
+
+  private:
+    cudaStream_t stream_;
+    std::multimap<size_t, void*> free_;
+    std::map<void*, size_t> size_of_;
+    size_t held_ = 0;
+};
+
+// RAII handle on a pool block
+class Buf {
+  public:
+    Buf() = default;
+    Buf(Pool* pool, size_t bytes) : pool_(pool), bytes_(bytes) { p_ = bytes ? pool->get(bytes) : nullptr; }
+    Buf(const Buf&) = delete;
+    Buf& operator=(const Buf&) = delete;
+    Buf(Buf&& o) noexcept { *this = std::move(o); }
+    Buf& operator=(Buf&& o) noexcept {
+        release();
+        pool_ = o.pool_; p_ = o.p_; bytes_ = o.bytes_;
+        o.p_ = nullptr; o.bytes_ = 0;
+        return *this;
+    }
+    ~Buf() { release(); }
+    void release() {
+        if (p_ && pool_) pool_->put(p_);
+        p_ = nullptr; bytes_ = 0;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p_); }
+    double* d() const { return static_cast<double*>(p_); }
+    size_t bytes() const { return bytes_; }
+
+  private:
+    Pool* pool_ = nullptr;
+    void* p_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// ---------------------------------------------------------------------------
+// dense FP64 device tensor, column-major (first leg fastest)
+// ---------------------------------------------------------------------------
+constexpr int MAXR = 8;
+
+struct DT {
+    Buf buf;
+    int rank = 0;
+    int64_t d[MAXR] = {0};
+    double* p() const { return buf.d(); }
+    int64_t size() const {
+        int64_t s = 1;
+        for (int i = 0; i < rank; ++i) s *= d[i];
+        return rank ? s : 0;
+    }
+    std::vector<int64_t> dims() const { return std::vector<int64_t>(d, d + rank); }
+};
+
+DT make_dt(Pool* pool, const std::vector<int64_t>& dims);
+
+// ---------------------------------------------------------------------------
+// per-handle execution context
+// ---------------------------------------------------------------------------
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int precision = TNR_PREC_F64;
+    uint64_t seed = 0x9e3779b97f4a7c15ull;
+    uint64_t call_counter = 0;     // varies the random sketch between calls
+    std::unique_ptr<Pool> pool;
+    int* d_status = nullptr;       // device status word
+    double* d_scalar = nullptr;    // small device scratch (norms, reductions)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // statistics of the last decompositions
+    int last_iters = 0;
+    bool bulk_call = false;        // the FP64 GEMM in flight serves a bulk contraction
+    Ctx(cudaStream_t s, int prec, uint64_t seed_);
+    ~Ctx();
+    void sync();
+    int read_status_and_clear();
+};
+
+// ---------------------------------------------------------------------------
+// kernels / primitives (launch wrappers)
+// ---------------------------------------------------------------------------
+// out = alpha * permute(in) with out.d[k] = in.d[perm[k]]; alpha from *scale_ptr if given
+void permute(Ctx& c, const double* in, const int64_t* in_dims, int rank, const int* perm,
+             double* out, const double* scale_ptr = nullptr);
+
+// two-level strided batch: batch index b = b1 + n1 * b2, offsets b1*s*1 + b2*s*2
+struct Batch2 {
+    int n1 = 1, n2 = 1;
+    int64_t sA1 = 0, sB1 = 0, sC1 = 0, sA2 = 0, sB2 = 0, sC2 = 0;
+};
+
+// C = alpha * op(A) op(B) + beta * C  (column-major, strided batch)
+void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+              int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt);
+void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt);
+void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
+              const double* A, int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB,
+              double beta, double* C, int64_t ldc, int64_t sC, int batch = 1);
+
+// bulk-contraction GEMM in the context's precision (FP64 or split 3xBF16 on tcgen05)
+void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
+               const double* A, int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB,
+               double beta, double* C, int64_t ldc, int64_t sC, int batch = 1);
+
+// split 3xBF16 tcgen05 GEMM (FP32 accumulate in TMEM); returns false if the shape is unsupported
+bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
+                   const double* A, int64_t lda, const double* B, int64_t ldb,
+                   double beta, double* C, int64_t ldc, const Batch2& bt);
+
+// symmetric eigendecomposition of an r x r matrix (r <= 128), eigenvalues sorted by |lambda| desc
+void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam);
+// G <- Cholesky factor inverse: on exit Linv (lower) with (G + shift I) = L L^T; returns via status
+void chol_inv(Ctx& c, double* G, int r, double shift);
+// FP32 versions (one SM runs FP32 at 64x its FP64 rate): results returned in FP64 buffers
+void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam);
+void chol_inv_f32(Ctx& c, double* G, int r, double shift);
+void add_identity(Ctx& c, double* X, int r, double alpha);
+void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r);
+void fill_normal(Ctx& c, double* x, int64_t n, uint64_t seed);
+void col_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);
+void row_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);
+void col_norms(Ctx& c, const double* X, int64_t m, int64_t n, int64_t ldx, double* out);
+void gram_unit_diag(Ctx& c, double* G, int r, double* dscale);
+void sum_squares(Ctx& c, const double* x, int64_t n, double* out);
+void scale_inplace(Ctx& c, double* x, int64_t n, const double* inv_scale_ptr);
+void fill_identity(Ctx& c, double* x, int64_t m, int64_t n);
+void copy_f64(Ctx& c, double* dst, const double* src, int64_t n);
+
+// trace norms (finalize.jl:4-14,62-66): writes |trace| into *out
+void trace2d(Ctx& c, const double* T, const int64_t* d, double* out);
+void trace_btrg(Ctx& c, const double* T, const int64_t* d, const double* S1, const double* S2, double* out);
+void trace3d(Ctx& c, const double* T, const int64_t* d, double* out);
+// pseudopow of a diagonal (btrg.jl:156-164): out = s >= tol ? s^a : s
+void pseudopow(Ctx& c, const double* s, int n, double a, double* out);
+void check_finite(Ctx& c, const double* x, int64_t n);
+
+// ---------------------------------------------------------------------------
+// truncated decompositions
+// ---------------------------------------------------------------------------
+struct TsvdOut {
+    int k = 0;
+    double fro2 = 0;        // ||M||_F^2
+    double err = 0;         // 2-norm of the discarded values
+    int iters = 0;
+    std::vector<double> vals;  // kept values (host copy)
+};
+
+// M (m x n, ld = m, column-major): U (m x k), s (k), Vt (k x n)
+TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt);
+// symmetric M (n x n): U (n x k) eigenvectors of the k largest |eigenvalues|, lam (k)
+TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lam);
+
+// ---------------------------------------------------------------------------
+// generic pairwise contraction (permute + GEMM + permute)
+// ---------------------------------------------------------------------------
+// labels are small ints; out_labels gives the output leg order
+DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::vector<int>& lA,
+            const double* B, const std::vector<int64_t>& dB, const std::vector<int>& lB,
+            const std::vector<int>& lOut, bool bulk = true);
+inline DT contract(Ctx& c, const DT& A, const std::vector<int>& lA, const DT& B,
+                   const std::vector<int>& lB, const std::vector<int>& lOut, bool bulk = true) {
+    return contract(c, A.p(), A.dims(), lA, B.p(), B.dims(), lB, lOut, bulk);
+}
+DT permuted(Ctx& c, const DT& A, const std::vector<int>& perm);
+
+}  // namespace tnr

@@ -1,0 +1,163 @@
+// FP64 GEMM on the CUDA cores (DFMA): the plain path of every contraction and the
+// FP64 pieces of the truncated decompositions.  Column-major, op(A)/op(B) in {N,T},
+// strided batch, deterministic split-K for skinny outputs (Gram matrices).
+#include "common.cuh"
+
+#include <algorithm>
+
+namespace tnr {
+
+constexpr int BM = 64, BN = 64, BK = 16;
+
+// one CTA: 64x64 tile of C, 256 threads, 4x4 outputs per thread
+__global__ void __launch_bounds__(256)
+k_dgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* __restrict__ A,
+        int64_t lda, const double* __restrict__ B, int64_t ldb, double beta,
+        double* __restrict__ C, int64_t ldc, Batch2 bt, int ksplit, int64_t kchunk, double* __restrict__ part) {
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int64_t i0 = blockIdx.x * (int64_t)BM, j0 = blockIdx.y * (int64_t)BN;
+    int bz = blockIdx.z;
+    int ks = bz % ksplit;
+    int b = bz / ksplit;
+    int b1 = b % bt.n1, b2 = b / bt.n1;
+    A += b1 * bt.sA1 + b2 * bt.sA2;
+    B += b1 * bt.sB1 + b2 * bt.sB2;
+    const int64_t kbeg = ks * kchunk, kend = min(k, kbeg + kchunk);
+
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+    for (int64_t kk0 = kbeg; kk0 < kend; kk0 += BK) {
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            int e = threadIdx.x + 256 * l;
+            int ii, kk;
+            double v = 0.0;
+            if (!ta) { ii = e % BM; kk = e / BM; } else { kk = e % BK; ii = e / BK; }
+            int64_t gi = i0 + ii, gk = kk0 + kk;
+            if (gi < m && gk < kend) v = ta ? A[gk + gi * lda] : A[gi + gk * lda];
+            As[kk][ii] = v;
+            int jj;
+            double w = 0.0;
+            if (!tb) { kk = e % BK; jj = e / BK; } else { jj = e % BN; kk = e / BN; }
+            int64_t gj = j0 + jj;
+            gk = kk0 + kk;
+            if (gj < n && gk < kend) w = tb ? B[gj + gk * ldb] : B[gk + gj * ldb];
+            Bs[kk][jj] = w;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], bb[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][tx + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bb[j] = Bs[kk][ty + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    if (ksplit > 1) {
+        double* P = part + (int64_t)ks * m * n;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int64_t gi = i0 + tx + 16 * i, gj = j0 + ty + 16 * j;
+                if (gi < m && gj < n) P[gi + gj * m] = acc[i][j];
+            }
+        return;
+    }
+    C += b1 * bt.sC1 + b2 * bt.sC2;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int64_t gi = i0 + tx + 16 * i, gj = j0 + ty + 16 * j;
+            if (gi < m && gj < n) {
+                double v = alpha * acc[i][j];
+                if (beta != 0.0) v = fma(beta, C[gi + gj * ldc], v);
+                C[gi + gj * ldc] = v;
+            }
+        }
+}
+
+// C = alpha * sum_s P[s] + beta * C (fixed summation order: deterministic)
+__global__ void k_splitk_reduce(const double* __restrict__ P, int ks, int64_t m, int64_t n, double alpha,
+                                double beta, double* C, int64_t ldc) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int i = 0; i < ks; ++i) s += P[e + (int64_t)i * m * n];
+        int64_t gi = e % m, gj = e / m;
+        double v = alpha * s;
+        if (beta != 0.0) v = fma(beta, C[gi + gj * ldc], v);
+        C[gi + gj * ldc] = v;
+    }
+}
+
+void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+              int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
+    const int batch = bt.n1 * bt.n2;
+    if (m <= 0 || n <= 0 || batch <= 0) return;
+    TNR_REQUIRE(k > 0, TNR_ERR_INVALID_ARG, "gemm with k = 0");
+    int64_t gm = (m + BM - 1) / BM, gn = (n + BN - 1) / BN;
+    TNR_REQUIRE(gn <= 65535, TNR_ERR_UNSUPPORTED, "gemm: n too large for the grid");
+    int ksplit = 1;
+    int64_t tiles = gm * gn * batch;
+    if (batch == 1 && tiles < sm_count() && k >= 64) {
+        // small outputs (Gram matrices, r x r products): spread K over the SMs
+        ksplit = (int)std::min<int64_t>({k / 32, (2 * sm_count()) / tiles, 64});
+        if (ksplit < 2) ksplit = 1;
+    }
+    int64_t kchunk = ksplit > 1 ? ((k + ksplit - 1) / ksplit + BK - 1) / BK * BK : k;
+    if (ksplit > 1) ksplit = (int)((k + kchunk - 1) / kchunk);
+    TNR_REQUIRE((int64_t)batch * ksplit <= 65535, TNR_ERR_UNSUPPORTED, "gemm: batch too large");
+    Buf part;
+    if (ksplit > 1) part = Buf(c.pool.get(), (size_t)ksplit * m * n * sizeof(double));
+    dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)(batch * ksplit));
+    int rec = prof_start(c.stream);
+    k_dgemm<<<grid, 256, 0, c.stream>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt, ksplit,
+                                        kchunk, part.d());
+    check_launch("dgemm");
+    if (ksplit > 1) {
+        int g = (int)std::min<int64_t>((m * n + 255) / 256, (int64_t)sm_count() * 8);
+        k_splitk_reduce<<<g, 256, 0, c.stream>>>(part.d(), ksplit, m, n, alpha, beta, C, ldc);
+        check_launch("splitk_reduce");
+    }
+    prof_stop(rec, c.stream, c.bulk_call ? PROF_GEMM_BULK : PROF_GEMM_F64, 2.0 * m * n * k * batch);
+}
+
+void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+              int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C,
+              int64_t ldc, int64_t sC, int batch) {
+    Batch2 bt;
+    bt.n1 = batch; bt.sA1 = sA; bt.sB1 = sB; bt.sC1 = sC;
+    gemm_f64(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
+}
+
+void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
+    if (c.precision == TNR_PREC_SPLIT && gemm_split_tc(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt))
+        return;
+    c.bulk_call = true;
+    gemm_f64(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
+    c.bulk_call = false;
+}
+
+void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+               int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C,
+               int64_t ldc, int64_t sC, int batch) {
+    Batch2 bt;
+    bt.n1 = batch; bt.sA1 = sA; bt.sB1 = sB; bt.sC1 = sC;
+    gemm_bulk(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
+}
+
+}  // namespace tnr

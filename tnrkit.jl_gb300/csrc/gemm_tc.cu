@@ -1,0 +1,384 @@
+// Split-precision GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// C (FP64) = alpha * op(A) op(B) + beta * C with every FP64 operand split into three
+// BF16 planes x = x0 + x1 + x2 (each the BF16 rounding of the previous residual).
+// Six plane products x_i y_j with i + j <= 2 are accumulated in one FP32
+// accumulator in tensor memory (TMEM): about 24 bits of each operand and FP32
+// accumulation.  Smallest terms first, the leading x0 y0 last.
+//
+//  * split pass: FP64 -> BF16 planes in a K-major [batch][plane][rows][Kp] layout
+//    (shared-memory tiled transpose where the source is not K-contiguous);
+//  * GEMM: 128 x BN tile per CTA, TMA loads with 128-byte swizzle into a
+//    STAGES-deep mbarrier pipeline, one thread issues tcgen05.mma (kind::f16,
+//    M=128, K=16), tcgen05.commit frees stages, the four warps read the FP32
+//    accumulator with tcgen05.ld and write FP64 C (coalesced along the rows).
+// Every wait is bounded by a 2-second global-timer limit and reports through the
+// context status word instead of hanging.
+#include "common.cuh"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <mutex>
+
+namespace tnr {
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3, NTHREADS = 128;
+constexpr int TILE_A_BYTES = BM * BK * 2;   // 16 KB
+constexpr int TILE_B_BYTES = BN * BK * 2;   // 16 KB
+constexpr int STAGE_BYTES = TILE_A_BYTES + TILE_B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int NTERMS = 6;
+constexpr int ST_TC_TIMEOUT = 8;
+
+// plane pairs, smallest contributions first
+__constant__ int c_pa[NTERMS] = {2, 1, 0, 1, 0, 0};
+__constant__ int c_pb[NTERMS] = {0, 1, 2, 0, 1, 0};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: gives up after 2 s, records the timeout and returns false
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > 2000000000ull) {
+            atomicOr(status, ST_TC_TIMEOUT);
+            return false;
+        }
+        __nanosleep(40);
+    }
+}
+
+__device__ __forceinline__ void tma_load_4d(const CUtensorMap* map, uint64_t* bar, void* dst, int c0, int c1, int c2,
+                                            int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
+    d |= (uint64_t)1 << 16;                          // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                          // descriptor version (fixed 0b001)
+    d |= (uint64_t)2 << 61;                          // swizzle: 128 B
+    return d;
+}
+
+// instruction descriptor: kind::f16, A/B = BF16, D = F32, both K-major, M = 128, N = BN
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcArgs {
+    int64_t m, n;
+    int nkb;            // K blocks of 64
+    double alpha, beta;
+    double* C;
+    int64_t ldc;
+    int n1;             // batch level 1 size (b = b1 + n1 * b2)
+    int64_t sC1, sC2;
+    int a_batched, b_batched;
+    int* status;
+};
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t pad = ((raw + 1023) & ~1023u) - raw;
+    unsigned char* tiles = smem_raw + pad;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + STAGES * STAGE_BYTES);
+    uint64_t* full = bars;                   // STAGES
+    uint64_t* empty = bars + STAGES;         // STAGES
+    uint64_t* accum = bars + 2 * STAGES;     // 1
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile_m = blockIdx.x, tile_n = blockIdx.y, b = blockIdx.z;
+    const int niter = NTERMS * a.nkb;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0) {
+        // TMA producer
+        const int ab = a.a_batched ? b : 0, bb = a.b_batched ? b : 0;
+        for (int it = 0; it < niter && ok; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+            ok = mbar_wait(&empty[s], ph ^ 1u, a.status);
+            if (!ok) break;
+            const int t = it / a.nkb, kb = it % a.nkb;
+            unsigned char* sa = tiles + s * STAGE_BYTES;
+            unsigned char* sb = sa + TILE_A_BYTES;
+            mbar_expect_tx(&full[s], STAGE_BYTES);
+            tma_load_4d(&tmA, &full[s], sa, kb * BK, tile_m * BM, c_pa[t], ab);
+            tma_load_4d(&tmB, &full[s], sb, kb * BK, tile_n * BN, c_pb[t], bb);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        for (int it = 0; it < niter && ok; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+            ok = mbar_wait(&full[s], ph, a.status);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
+            const uint32_t sb = sa + TILE_A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk)
+                mma_bf16(tmem, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (it > 0 || kk > 0) ? 1u : 0u);
+            mma_commit(&empty[s]);
+        }
+        mma_commit(accum);
+    }
+    __syncwarp();
+    // epilogue: all four warps, TMEM lanes 32w..32w+31 = tile rows
+    ok = mbar_wait(accum, 0, a.status) && ok;
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int b1 = b % a.n1, b2 = b / a.n1;
+    double* C = a.C + b1 * a.sC1 + b2 * a.sC2;
+    const int64_t row = (int64_t)tile_m * BM + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        if (row < a.m) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int64_t col = (int64_t)tile_n * BN + c0 + j;
+                if (col < a.n) {
+                    double* p = C + row + col * a.ldc;
+                    double r = a.alpha * (double)v[j];
+                    if (a.beta != 0.0) r = fma(a.beta, *p, r);
+                    *p = ok ? r : 0.0;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    }
+}
+
+// FP64 operand -> three BF16 planes, K-major: dst[b][plane][row][Kp] (Kp >= K, zero padded).
+// Source element (row i, k) of batch (b1, b2) at src[b1*s1 + b2*s2 + i*si + k*sk].
+struct SplitArgs {
+    const double* src;
+    int64_t rows, K, Kp, si, sk, s1, s2;
+    int n1, nb;
+    __nv_bfloat16* dst;
+};
+
+__global__ void k_split_planes(SplitArgs a) {
+    __shared__ double tile[32][33];
+    const int64_t tr = (a.rows + 31) / 32, tk = (a.Kp + 31) / 32;
+    const int64_t ntiles = tr * tk * a.nb;
+    const bool kfast = (a.sk == 1);
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t bi = t / (tr * tk), rem = t % (tr * tk);
+        const int64_t i0 = (rem / tk) * 32, k0 = (rem % tk) * 32;
+        const int b1 = (int)(bi % a.n1), b2 = (int)(bi / a.n1);
+        const double* S = a.src + b1 * a.s1 + b2 * a.s2;
+        __syncthreads();
+        for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+            // coalesced along whichever index is contiguous in the source
+            int64_t i = kfast ? i0 + y : i0 + threadIdx.x;
+            int64_t k = kfast ? k0 + threadIdx.x : k0 + y;
+            double v = (i < a.rows && k < a.K) ? S[i * a.si + k * a.sk] : 0.0;
+            if (kfast) tile[y][threadIdx.x] = v;       // tile[i][k]
+            else tile[threadIdx.x][y] = v;
+        }
+        __syncthreads();
+        for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+            const int64_t i = i0 + y, k = k0 + threadIdx.x;
+            if (i < a.rows && k < a.Kp) {
+                const double x = tile[y][threadIdx.x];
+                const __nv_bfloat16 p0 = __double2bfloat16(x);
+                const double r1 = x - (double)__bfloat162float(p0);
+                const __nv_bfloat16 p1 = __double2bfloat16(r1);
+                const double r2 = r1 - (double)__bfloat162float(p1);
+                const __nv_bfloat16 p2 = __double2bfloat16(r2);
+                const int64_t plane = a.rows * a.Kp;
+                __nv_bfloat16* D = a.dst + bi * 3 * plane + i * a.Kp + k;
+                D[0] = p0;
+                D[plane] = p1;
+                D[2 * plane] = p2;
+            }
+        }
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// planes [nb][3][rows][Kp] bf16 -> 4D map {Kp, rows, 3, nb}, box {64, box_rows, 1, 1}
+void make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t Kp, int nb, int box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    TNR_REQUIRE(fn, TNR_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[4] = {(cuuint64_t)Kp, (cuuint64_t)rows, 3, (cuuint64_t)nb};
+    cuuint64_t strides[3] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * 2 * rows, (cuuint64_t)Kp * 2 * rows * 3};
+    cuuint32_t box[4] = {BK, (cuuint32_t)box_rows, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    TNR_REQUIRE(r == CUDA_SUCCESS, TNR_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+void split_operand(Ctx& c, const double* src, int64_t rows, int64_t K, int64_t Kp, int64_t si, int64_t sk,
+                   int64_t s1, int64_t s2, int n1, int nb, __nv_bfloat16* dst) {
+    SplitArgs sa{src, rows, K, Kp, si, sk, s1, s2, n1, nb, dst};
+    int64_t ntiles = ((rows + 31) / 32) * ((Kp + 31) / 32) * nb;
+    int g = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 16);
+    int rec = prof_start(c.stream);
+    k_split_planes<<<g, dim3(32, 8), 0, c.stream>>>(sa);
+    check_launch("split_planes");
+    prof_stop(rec, c.stream, PROF_SPLIT, (double)rows * K * nb * 8 + (double)rows * Kp * nb * 6);
+}
+
+}  // namespace
+
+bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                   int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
+    const int batch = bt.n1 * bt.n2;
+    // tiny products stay on the FP64 path (the early coarse-graining steps carry the largest weights)
+    if (m < 64 || n < 16 || k < 16 || (double)m * n * k * batch < (double)(1 << 22)) return false;
+    if (batch > 65535 || (m + BM - 1) / BM > 2147483647 || (n + BN - 1) / BN > 65535) return false;
+    if (!encode_fn()) return false;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_gemm_split_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    });
+    const int64_t Kp = (k + 7) / 8 * 8;
+    const bool a_b = (bt.sA1 != 0 || bt.sA2 != 0) && batch > 1;
+    const bool b_b = (bt.sB1 != 0 || bt.sB2 != 0) && batch > 1;
+    const int nbA = a_b ? batch : 1, nbB = b_b ? batch : 1;
+    Buf pa(c.pool.get(), (size_t)nbA * 3 * m * Kp * 2), pb(c.pool.get(), (size_t)nbB * 3 * n * Kp * 2);
+    // op(A)(i, kk): ta ? A[kk + i*lda] : A[i + kk*lda];  op(B)(kk, j) as rows j: tb ? B[j + kk*ldb] : B[kk + j*ldb]
+    split_operand(c, A, m, k, Kp, ta ? lda : 1, ta ? 1 : lda, a_b ? bt.sA1 : 0, a_b ? bt.sA2 : 0, a_b ? bt.n1 : 1, nbA,
+                  pa.as<__nv_bfloat16>());
+    split_operand(c, B, n, k, Kp, tb ? 1 : ldb, tb ? ldb : 1, b_b ? bt.sB1 : 0, b_b ? bt.sB2 : 0, b_b ? bt.n1 : 1, nbB,
+                  pb.as<__nv_bfloat16>());
+    CUtensorMap mA, mB;
+    make_map(&mA, pa.as<void>(), m, Kp, nbA, BM);
+    make_map(&mB, pb.as<void>(), n, Kp, nbB, BN);
+    TcArgs args;
+    args.m = m;
+    args.n = n;
+    args.nkb = (int)((Kp + BK - 1) / BK);
+    args.alpha = alpha;
+    args.beta = beta;
+    args.C = C;
+    args.ldc = ldc;
+    args.n1 = bt.n1;
+    args.sC1 = bt.sC1;
+    args.sC2 = bt.sC2;
+    args.a_batched = a_b;
+    args.b_batched = b_b;
+    args.status = c.d_status;
+    dim3 grid((unsigned)((m + BM - 1) / BM), (unsigned)((n + BN - 1) / BN), (unsigned)batch);
+    int rec = prof_start(c.stream);
+    k_gemm_split_tc<<<grid, NTHREADS, SMEM_BYTES, c.stream>>>(mA, mB, args);
+    check_launch("gemm_split_tc");
+    prof_stop(rec, c.stream, PROF_GEMM_BULK, 2.0 * m * n * k * batch);
+    return true;
+}
+
+}  // namespace tnr

@@ -1,0 +1,241 @@
+// Small dense FP64 linear algebra on one CTA: parallel-ordering (round-robin)
+// two-sided Jacobi eigensolver and Cholesky factor + triangular inverse.
+// Both keep the matrix in shared memory; every loop has a fixed iteration cap
+// and reports failure through the context status word (no trap, no spin).
+#include "common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+
+namespace tnr {
+
+constexpr int JMAX = 160;           // largest matrix held in shared memory
+constexpr int JTHREADS = 512;
+constexpr int JMAX_SWEEPS = 40;
+
+template <class T>
+__device__ __forceinline__ T& SG(T* G, int ld, int i, int j) { return G[i + j * ld]; }
+
+template <class T> struct JTol;
+template <> struct JTol<double> { static constexpr double rel = 1e-15; };
+template <> struct JTol<float> { static constexpr double rel = 2e-7; };
+
+// Parallel (round-robin ordering) two-sided Jacobi in shared memory, arithmetic type T.
+// Input G is FP64 (symmetrised on load); W (FP64, r x r) and lam (FP64) are sorted by |lambda|.
+template <class T>
+__global__ void __launch_bounds__(JTHREADS)
+k_jacobi(const double* __restrict__ Gin, int64_t ldg, int r, double* __restrict__ Wout,
+         double* __restrict__ lam, T* __restrict__ Ww, int* status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ld = r + 1;
+    T* G = reinterpret_cast<T*>(smem_raw);  // r x r, leading dim r+1
+    T* cs = G + (size_t)ld * r;             // JMAX/2 + 1 each
+    T* sn = cs + (JMAX / 2 + 1);
+    int* pp = (int*)(sn + (JMAX / 2 + 1));
+    int* qq = pp + (JMAX / 2 + 1);
+    __shared__ int rot_count;
+    __shared__ T fro;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int R = r + (r & 1), n = R - 1, npair = R / 2;
+
+    // load (symmetrised) and W = I
+    for (int e = tid; e < r * r; e += nt) {
+        int i = e % r, j = e / r;
+        SG(G, ld, i, j) = (T)(0.5 * (Gin[i + j * ldg] + Gin[j + i * ldg]));
+        Ww[e] = (i == j) ? T(1) : T(0);
+    }
+    __syncthreads();
+    if (tid < 32) {
+        T acc = 0;
+        for (int e = tid; e < r * r; e += 32) {
+            T v = SG(G, ld, e % r, e / r);
+            acc = fma(v, v, acc);
+        }
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (tid == 0) fro = sqrt(acc);
+    }
+    __syncthreads();
+    const T abs_floor = (T)1e-30 * fro;
+    const T reltol = (T)JTol<T>::rel;
+    int sweep = 0;
+    bool converged = (r <= 1);
+    for (; sweep < JMAX_SWEEPS && !converged; ++sweep) {
+        if (tid == 0) rot_count = 0;
+        __syncthreads();
+        for (int t = 0; t < n; ++t) {
+            // pair schedule: player n (the even fill-in) meets t; (t+i, t-i) mod n for i >= 1
+            for (int i = tid; i < npair; i += nt) {
+                int p, q;
+                if (i == 0) { p = n; q = t; }
+                else { p = (t + i) % n; q = (t - i + n) % n; }
+                if (p > q) { int tmp = p; p = q; q = tmp; }
+                T c = 1, s = 0;
+                if (q < r) {
+                    T apq = SG(G, ld, p, q), app = SG(G, ld, p, p), aqq = SG(G, ld, q, q);
+                    if (fabs(apq) > fmax(reltol * sqrt(fabs(app * aqq)), abs_floor)) {
+                        T tau = (aqq - app) / (T(2) * apq);
+                        T tt;
+                        if (fabs(tau) > (T)1e18) tt = T(0.5) / tau;
+                        else tt = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + sqrt(T(1) + tau * tau));
+                        c = rsqrt(T(1) + tt * tt);
+                        s = tt * c;
+                        atomicAdd(&rot_count, 1);
+                    }
+                }
+                pp[i] = p; qq[i] = (q < r) ? q : -1; cs[i] = c; sn[i] = s;
+            }
+            __syncthreads();
+            // G <- G J (columns p, q) and W <- W J
+            for (int e = tid; e < npair * r; e += nt) {
+                int i = e / r, j = e % r;
+                int q = qq[i];
+                T s = sn[i];
+                if (q < 0 || s == T(0)) continue;
+                int p = pp[i];
+                T c = cs[i];
+                T gp = SG(G, ld, j, p), gq = SG(G, ld, j, q);
+                SG(G, ld, j, p) = c * gp - s * gq;
+                SG(G, ld, j, q) = s * gp + c * gq;
+                T wp = Ww[j + p * r], wq = Ww[j + q * r];
+                Ww[j + p * r] = c * wp - s * wq;
+                Ww[j + q * r] = s * wp + c * wq;
+            }
+            __syncthreads();
+            // G <- J^T G (rows p, q)
+            for (int e = tid; e < npair * r; e += nt) {
+                int i = e / r, j = e % r;
+                int q = qq[i];
+                T s = sn[i];
+                if (q < 0 || s == T(0)) continue;
+                int p = pp[i];
+                T c = cs[i];
+                T gp = SG(G, ld, p, j), gq = SG(G, ld, q, j);
+                SG(G, ld, p, j) = c * gp - s * gq;
+                SG(G, ld, q, j) = s * gp + c * gq;
+            }
+            __syncthreads();
+            for (int i = tid; i < npair; i += nt) {
+                int q = qq[i];
+                if (q >= 0 && sn[i] != T(0)) { SG(G, ld, pp[i], q) = T(0); SG(G, ld, q, pp[i]) = T(0); }
+            }
+            __syncthreads();
+        }
+        converged = (rot_count == 0);
+        __syncthreads();
+    }
+    if (!converged && tid == 0) atomicOr(status, ST_JACOBI_NOCONV);
+    // sort by |lambda| descending (stable by index)
+    for (int i = tid; i < r; i += nt) {
+        T li = SG(G, ld, i, i);
+        if (!isfinite(li)) atomicOr(status, ST_NONFINITE);
+        int rank = 0;
+        for (int j = 0; j < r; ++j) {
+            T lj = fabs(SG(G, ld, j, j));
+            rank += (lj > fabs(li)) || (lj == fabs(li) && j < i);
+        }
+        lam[rank] = (double)li;
+        for (int j = 0; j < r; ++j) Wout[j + (int64_t)rank * r] = (double)Ww[j + (int64_t)i * r];
+    }
+}
+
+template <class T>
+static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {
+    TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "jacobi_eigh: r out of range");
+    const size_t aux = 2 * (JMAX / 2 + 1) * (sizeof(T) + sizeof(int));
+    size_t smem = (size_t)(r + 1) * r * sizeof(T) + aux;
+    static std::once_flag once;
+    std::call_once(once, [aux] {
+        size_t maxs = (size_t)(JMAX + 1) * JMAX * sizeof(T) + aux;
+        cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxs);
+    });
+    Buf ww(c.pool.get(), (size_t)r * r * sizeof(T));
+    int nt = r <= 32 ? 128 : (r <= 64 ? 256 : JTHREADS);
+    int rec = prof_start(c.stream);
+    k_jacobi<T><<<1, nt, smem, c.stream>>>(G, ldg, r, W, lam, ww.as<T>(), c.d_status);
+    check_launch("jacobi");
+    prof_stop(rec, c.stream, PROF_JACOBI, (double)r * r * r);
+}
+
+void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {
+    launch_jacobi<double>(c, G, ldg, r, W, lam);
+}
+
+void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {
+    launch_jacobi<float>(c, G, ldg, r, W, lam);
+}
+
+// Cholesky of (G + shift I) = L L^T in shared memory, then L^{-1} (lower) written over G.
+template <class T>
+__global__ void __launch_bounds__(512)
+k_chol_inv(double* G, int r, double shift, int* status) {
+    extern __shared__ __align__(16) unsigned char smem_c[];
+    T* S = reinterpret_cast<T*>(smem_c);
+    const int ld = r + 1;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    __shared__ int bad;
+    if (tid == 0) bad = 0;
+    for (int e = tid; e < r * r; e += nt) {
+        int i = e % r, j = e / r;
+        S[i + j * ld] = (T)((i >= j) ? G[e] + (i == j ? shift : 0.0) : 0.0);
+    }
+    __syncthreads();
+    for (int k = 0; k < r; ++k) {
+        if (tid == 0) {
+            T d = S[k + k * ld];
+            if (!(d > T(0)) || !isfinite(d)) { bad = 1; d = (T)1e-30; }
+            S[k + k * ld] = sqrt(d);
+        }
+        __syncthreads();
+        T dk = S[k + k * ld];
+        for (int i = k + 1 + tid; i < r; i += nt) S[i + k * ld] /= dk;
+        __syncthreads();
+        int m = r - k - 1;
+        for (int e = tid; e < m * m; e += nt) {
+            int i = k + 1 + e % m, j = k + 1 + e / m;
+            if (i >= j) S[i + j * ld] -= S[i + k * ld] * S[j + k * ld];
+        }
+        __syncthreads();
+    }
+    // inverse of the lower-triangular L: column j of L^{-1} by forward substitution,
+    // one warp per column (lanes split the inner products), result kept in S's upper part
+    T* X = S + (size_t)ld * r;   // r x r scratch (column-major, ld r+1)
+    const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+    for (int j = warp; j < r; j += nw) {
+        for (int i = 0; i < r; ++i) {
+            if (i < j) { if (lane == 0) X[i + j * ld] = T(0); continue; }
+            T acc = T(0);
+            for (int kk = j + lane; kk < i; kk += 32) acc += S[i + kk * ld] * X[kk + j * ld];
+            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) X[i + j * ld] = ((i == j ? T(1) : T(0)) - acc) / S[i + i * ld];
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < r * r; e += nt) {
+        int i = e % r, j = e / r;
+        G[e] = (double)X[i + j * ld];
+    }
+    if (tid == 0 && bad) atomicOr(status, ST_CHOL_BREAKDOWN);
+}
+
+template <class T>
+static void launch_chol(Ctx& c, double* G, int r, double shift) {
+    TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "chol_inv: r out of range");
+    size_t smem = 2 * (size_t)(r + 1) * r * sizeof(T);
+    TNR_REQUIRE(smem <= 227 * 1024, TNR_ERR_UNSUPPORTED, "chol_inv: matrix too large for shared memory");
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_chol_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)std::min<size_t>(2 * (JMAX + 1) * JMAX * sizeof(T), 227 * 1024));
+    });
+    int rec = prof_start(c.stream);
+    k_chol_inv<T><<<1, 512, smem, c.stream>>>(G, r, shift, c.d_status);
+    check_launch("chol_inv");
+    prof_stop(rec, c.stream, PROF_CHOL, (double)r * r * r);
+}
+
+void chol_inv(Ctx& c, double* G, int r, double shift) { launch_chol<double>(c, G, r, shift); }
+void chol_inv_f32(Ctx& c, double* G, int r, double shift) { launch_chol<float>(c, G, r, shift); }
+
+}  // namespace tnr

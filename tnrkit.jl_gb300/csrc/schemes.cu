@@ -1,0 +1,422 @@
+// Coarse-graining steps and normalisation of TRG, BTRG, HOTRG and HOTRG_3D on
+// device-resident tensors (column-major, first leg fastest).
+#include "schemes.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace tnr {
+
+namespace {
+enum { La = 0, Lb, Lc, Ld, Le, Lf, Lg, Lh, Li, Lj, Lk, Ll, Lm, Ln, Lo, Lp, Lq, Lr, Ls, Lt, Lu, Lv, Lw, Lx, Ly, Lz };
+
+std::vector<double> dvec_to_host(Ctx& c, const double* d, int64_t n) {
+    std::vector<double> h((size_t)n);
+    if (n) TNR_CUDA(cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    return h;
+}
+}  // namespace
+
+// T[..., i_leg, ...] *= v[i_leg]
+__global__ void k_scale_leg(double* T, int64_t total, int64_t stride, int64_t dim, const double* v) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+        T[e] *= v[(e / stride) % dim];
+}
+
+static void scale_leg(Ctx& c, DT& T, int leg, const double* v) {
+    int64_t stride = 1;
+    for (int i = 0; i < leg; ++i) stride *= T.d[i];
+    int64_t total = T.size();
+    if (!total) return;
+    int g = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 8);
+    k_scale_leg<<<g, 256, 0, c.stream>>>(T.p(), total, stride, T.d[leg], v);
+    check_launch("scale_leg");
+}
+
+void Scheme::record(const TsvdOut& r) {
+    last_vals.insert(last_vals.end(), r.vals.begin(), r.vals.end());
+    last_counts.push_back((int)r.vals.size());
+}
+
+// SVD12 (src/utility/projectors.jl:211-217): M4 as (d1 d2) x (d3 d4) -> A = U sqrt(s), B = sqrt(s) V
+static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B) {
+    Ctx& c = *s.ctx;
+    int64_t m = M4.d[0] * M4.d[1], n = M4.d[2] * M4.d[3];
+    int k = (int)std::min<int64_t>(chi, std::min(m, n));
+    A = make_dt(c.pool.get(), {M4.d[0], M4.d[1], (int64_t)k});
+    B = make_dt(c.pool.get(), {(int64_t)k, M4.d[2], M4.d[3]});
+    Buf sv(c.pool.get(), (size_t)k * sizeof(double));
+    TsvdOut r = tsvd(c, M4.p(), m, n, k, A.p(), sv.d(), B.p());
+    col_scale(c, A.p(), m, k, m, sv.d(), 1);
+    row_scale(c, B.p(), k, n, k, sv.d(), 1);
+    s.record(r);
+}
+
+// step!(::TRG) (src/schemes/trg.jl:94-100)
+static void step_trg(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    DT& T = s.T;
+    TNR_REQUIRE(T.d[0] == T.d[3] && T.d[1] == T.d[2], TNR_ERR_INVALID_ARG, "TRG needs d1 == d4 and d2 == d3");
+    DT A, B, C, D;
+    svd12(s, T, chi, A, B);                         // A[i1,i2,k], B[k,i3,i4]
+    DT Tp = permuted(c, T, {1, 3, 0, 2});           // transpose(T, ((2,4),(1,3)))
+    svd12(s, Tp, chi, C, D);                        // C[i2,i4,k'], D[k',i1,i3]
+    Tp = DT();
+    // T[-1 -2;-3 -4] = D[-2;1 2] B[-1;4 1] C[4 3;-3] A[3 2;-4]
+    //   D[b,p,q] B[a,r,p] C[r,s,c] A[s,q,d]
+    DT X = contract(c, D, {Lb, Lp, Lq}, B, {La, Lr, Lp}, {La, Lb, Lq, Lr});
+    DT Y = contract(c, C, {Lr, Ls, Lc}, A, {Ls, Lq, Ld}, {Lq, Lr, Lc, Ld});
+    A = DT(); B = DT(); C = DT(); D = DT();
+    s.T = contract(c, X, {La, Lb, Lq, Lr}, Y, {Lq, Lr, Lc, Ld}, {La, Lb, Lc, Ld});
+}
+
+// step!(::BTRG) (src/schemes/btrg.jl:166-200)
+static void step_btrg(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    DT& T = s.T;
+    TNR_REQUIRE(T.d[0] == T.d[3] && T.d[1] == T.d[2], TNR_ERR_INVALID_ARG, "BTRG needs d1 == d4 and d2 == d3");
+    const double kexp = s.btrg_k;
+    const int64_t d1 = T.d[0], d2 = T.d[1], d3 = T.d[2], d4 = T.d[3];
+    // first SVD: T as (d1 d2) x (d3 d4)
+    int64_t m = d1 * d2, n = d3 * d4;
+    int k1 = (int)std::min<int64_t>(chi, std::min(m, n));
+    DT A = make_dt(c.pool.get(), {d1, d2, (int64_t)k1});
+    DT B = make_dt(c.pool.get(), {(int64_t)k1, d3, d4});
+    DT S1n = make_dt(c.pool.get(), {(int64_t)k1});
+    {
+        Buf sv(c.pool.get(), (size_t)k1 * sizeof(double)), sa(c.pool.get(), (size_t)k1 * sizeof(double));
+        TsvdOut r = tsvd(c, T.p(), m, n, k1, A.p(), sv.d(), B.p());
+        pseudopow(c, sv.d(), k1, (1.0 - kexp) / 2.0, sa.d());
+        pseudopow(c, sv.d(), k1, kexp, S1n.p());
+        col_scale(c, A.p(), m, k1, m, sa.d(), 0);
+        row_scale(c, B.p(), k1, n, k1, sa.d(), 0);
+        s.record(r);
+    }
+    // second SVD: permute(T, ((3,1),(4,2))) as (d3 d1) x (d4 d2)
+    DT P = permuted(c, T, {2, 0, 3, 1});
+    int64_t m2 = d3 * d1, n2 = d4 * d2;
+    int k2 = (int)std::min<int64_t>(chi, std::min(m2, n2));
+    DT C = make_dt(c.pool.get(), {d3, d1, (int64_t)k2});
+    DT D = make_dt(c.pool.get(), {(int64_t)k2, d4, d2});
+    DT S2n = make_dt(c.pool.get(), {(int64_t)k2});
+    {
+        Buf sv(c.pool.get(), (size_t)k2 * sizeof(double)), sa(c.pool.get(), (size_t)k2 * sizeof(double));
+        TsvdOut r = tsvd(c, P.p(), m2, n2, k2, C.p(), sv.d(), D.p());
+        pseudopow(c, sv.d(), k2, (1.0 - kexp) / 2.0, sa.d());
+        pseudopow(c, sv.d(), k2, kexp, S2n.p());
+        col_scale(c, C.p(), m2, k2, m2, sa.d(), 0);
+        row_scale(c, D.p(), k2, n2, k2, sa.d(), 0);
+        s.record(r);
+    }
+    P = DT();
+    // T[-1 -2;-3 -4] = D[-1;4 7] S1[1;7] B[-2;1 3] S2[3;2] C[8 2;-4] S1[8;5] A[6 5;-3] S2[4;6]
+    // with diagonal S1 (dim d2) and S2 (dim d1):  D[a,x,p] S1[p] S2[x], B[b,p,y] S2[y], C[z,y,d] S1[z], A[x,z,c]
+    scale_leg(c, D, 2, s.S1.p());
+    scale_leg(c, D, 1, s.S2.p());
+    scale_leg(c, B, 2, s.S2.p());
+    scale_leg(c, C, 0, s.S1.p());
+    DT X = contract(c, D, {La, Lx, Lp}, B, {Lb, Lp, Ly}, {La, Lb, Lx, Ly});
+    DT Y = contract(c, C, {Lz, Ly, Ld}, A, {Lx, Lz, Lc}, {Lx, Ly, Lc, Ld});
+    A = DT(); B = DT(); C = DT(); D = DT();
+    s.T = contract(c, X, {La, Lb, Lx, Ly}, Y, {Lx, Ly, Lc, Ld}, {La, Lb, Lc, Ld});
+    s.S1 = std::move(S1n);
+    s.S2 = std::move(S2n);
+}
+
+// eigh_trunc!(project_hermitian!(MM)) of a (rows x rows) Gram tensor -> U[r1, r2, k]
+static DT eig_proj(Scheme& s, const DT& MM, int chi, TsvdOut& out) {
+    Ctx& c = *s.ctx;
+    int64_t n = MM.d[0] * MM.d[1];
+    int k = (int)std::min<int64_t>(chi, n);
+    DT U = make_dt(c.pool.get(), {MM.d[0], MM.d[1], (int64_t)k});
+    Buf lam(c.pool.get(), (size_t)k * sizeof(double));
+    out = teigh(c, MM.p(), n, k, U.p(), lam.d());
+    return U;
+}
+
+// choose between the two projectors: keep U unless eps > eps' (hotrg.jl:112-114)
+static DT choose_proj(Scheme& s, DT&& U, TsvdOut& r, DT&& U2, TsvdOut& r2) {
+    s.last_eps.push_back(r.err);
+    s.last_eps.push_back(r2.err);
+    if (r.err > r2.err) {
+        s.record(r2);
+        return std::move(U2);
+    }
+    s.record(r);
+    return std::move(U);
+}
+
+// _get_hotrg_xproj (src/schemes/hotrg.jl:82-116) with A1 = A2 = T
+static DT hotrg_xproj(Scheme& s, const DT& T, int chi) {
+    Ctx& c = *s.ctx;
+    TsvdOut r1, r2;
+    DT U1, U2;
+    {
+        // MM[-1 -2;-3 -4] = A2[-1 5;1 2] A1[-2 3;5 4] conj(A2[-3 6;1 2]) conj(A1[-4 3;6 4])
+        DT X = contract(c, T, {La, Le, Li, Lj}, T, {Lc, Lf, Li, Lj}, {La, Le, Lc, Lf}, false);
+        DT Y = contract(c, T, {Lb, Lk, Le, Ll}, T, {Ld, Lk, Lf, Ll}, {Lb, Le, Ld, Lf}, false);
+        DT MM = contract(c, X, {La, Le, Lc, Lf}, Y, {Lb, Le, Ld, Lf}, {La, Lb, Lc, Ld}, false);
+        U1 = eig_proj(s, MM, chi, r1);
+    }
+    {
+        // MM = conj(A2[2 5;1 -1]) conj(A1[4 3;5 -2]) A2[2 6;1 -3] A1[4 3;6 -4]
+        DT X = contract(c, T, {Lj, Le, Li, La}, T, {Lj, Lf, Li, Lc}, {Le, La, Lf, Lc}, false);
+        DT Y = contract(c, T, {Ll, Lk, Le, Lb}, T, {Ll, Lk, Lf, Ld}, {Le, Lb, Lf, Ld}, false);
+        DT MM = contract(c, X, {Le, La, Lf, Lc}, Y, {Le, Lb, Lf, Ld}, {La, Lb, Lc, Ld}, false);
+        U2 = eig_proj(s, MM, chi, r2);
+    }
+    return choose_proj(s, std::move(U1), r1, std::move(U2), r2);
+}
+
+// _get_hotrg_yproj (src/schemes/hotrg.jl:118-152)
+static DT hotrg_yproj(Scheme& s, const DT& T, int chi) {
+    Ctx& c = *s.ctx;
+    TsvdOut r1, r2;
+    DT U1, U2;
+    {
+        // MM = A1[1 -1;2 5] A2[5 -2;4 3] conj(A1[1 -3;2 6]) conj(A2[6 -4;4 3])
+        DT X = contract(c, T, {Li, La, Lj, Lp}, T, {Li, Lc, Lj, Lr}, {La, Lp, Lc, Lr}, false);
+        DT Y = contract(c, T, {Lp, Lb, Ll, Lk}, T, {Lr, Ld, Ll, Lk}, {Lp, Lb, Lr, Ld}, false);
+        DT MM = contract(c, X, {La, Lp, Lc, Lr}, Y, {Lp, Lb, Lr, Ld}, {La, Lb, Lc, Ld}, false);
+        U1 = eig_proj(s, MM, chi, r1);
+    }
+    {
+        // MM = conj(A1[1 2;-1 5]) conj(A2[5 4;-2 3]) A1[1 2;-3 6] A2[6 4;-4 3]
+        DT X = contract(c, T, {Li, Lj, La, Lp}, T, {Li, Lj, Lc, Lr}, {La, Lp, Lc, Lr}, false);
+        DT Y = contract(c, T, {Lp, Ll, Lb, Lk}, T, {Lr, Ll, Ld, Lk}, {Lp, Lb, Lr, Ld}, false);
+        DT MM = contract(c, X, {La, Lp, Lc, Lr}, Y, {Lp, Lb, Lr, Ld}, {La, Lb, Lc, Ld}, false);
+        U2 = eig_proj(s, MM, chi, r2);
+    }
+    return choose_proj(s, std::move(U1), r1, std::move(U2), r2);
+}
+
+// _step_hotrg_y (src/schemes/hotrg.jl:42-60), A1 = A2 = T (dims dL, dD, dU, dR):
+//   T'[a,b,g,d] = Ux[i,j,a] Ux[k,l,d] A2[i,e,g,k] A1[j,b,e,l]
+// as W2[b,l,e,i,a] = A1p[j,(b,l,e)] Uxp[j,(i,a)];  V[b,l,k,g,a] = W2[(b,l),(e,i)] A2p[(e,i),(k,g)] per a;
+//    O[b,d,g,a] = V[b,(l,k)] Uxq[(l,k),d] per (g,a);  T' = O permuted (a,b,g,d).
+static void hotrg_step_y(Scheme& s, const DT& Ux) {
+    Ctx& c = *s.ctx;
+    const DT& T = s.T;
+    const int64_t dL = T.d[0], dD = T.d[1], dU = T.d[2], dR = T.d[3], kx = Ux.d[2];
+    TNR_REQUIRE(Ux.d[0] == dL && Ux.d[1] == dL && dL == dR && dD == dU, TNR_ERR_INVALID_ARG, "HOTRG y-step dims");
+    DT A1p = permuted(c, T, {0, 1, 3, 2});          // [j,b,l,e]
+    DT Uxp = permuted(c, Ux, {1, 0, 2});            // [j,i,a]
+    const int64_t mW = dD * dR * dU, nW = dL * kx;
+    DT W2 = make_dt(c.pool.get(), {dD, dR, dU, dL, kx});
+    gemm_bulk(c, true, false, mW, nW, dL, 1.0, A1p.p(), dL, 0, Uxp.p(), dL, 0, 0.0, W2.p(), mW, 0);
+    A1p = DT(); Uxp = DT();
+    DT A2p = permuted(c, T, {1, 0, 3, 2});          // [e,i,k,g]
+    DT V = make_dt(c.pool.get(), {dD, dR, dR, dU, kx});
+    {
+        Batch2 bt;
+        bt.n1 = (int)kx;
+        bt.sA1 = dD * dR * dU * dL;
+        bt.sB1 = 0;
+        bt.sC1 = dD * dR * dR * dU;
+        gemm_bulk(c, false, false, dD * dR, dR * dU, dU * dL, 1.0, W2.p(), dD * dR, A2p.p(), dU * dL, 0.0, V.p(),
+                  dD * dR, bt);
+    }
+    W2 = DT(); A2p = DT();
+    DT Uxq = permuted(c, Ux, {1, 0, 2});            // [l,k,d]
+    DT O = make_dt(c.pool.get(), {dD, kx, dU, kx});
+    {
+        Batch2 bt;
+        bt.n1 = (int)(dU * kx);
+        bt.sA1 = dD * dR * dR;
+        bt.sC1 = dD * kx;
+        gemm_bulk(c, false, false, dD, kx, dR * dR, 1.0, V.p(), dD, Uxq.p(), dR * dR, 0.0, O.p(), dD, bt);
+    }
+    V = DT();
+    s.T = permuted(c, O, {3, 0, 2, 1});
+}
+
+// _step_hotrg_x (src/schemes/hotrg.jl:62-80):
+//   T'[a,b,c,d] = A1[a,i,k,e] A2[e,j,l,d] Uy[i,j,b] Uy[k,l,c]
+// as W[a,k,e,j,b] = A1p[(a,k,e),i] Uy[i,(j,b)];  V[a,k,l,d,b] = W[(a,k),(e,j)] A2[(e,j),(l,d)] per b;
+//    T'[a,b,c,d] = V[a,(k,l)] Uy[(k,l),c] per (d,b), written in place (ldc = dL*ky).
+static void hotrg_step_x(Scheme& s, const DT& Uy) {
+    Ctx& c = *s.ctx;
+    const DT& T = s.T;
+    const int64_t dL = T.d[0], dD = T.d[1], dU = T.d[2], dR = T.d[3], ky = Uy.d[2];
+    TNR_REQUIRE(Uy.d[0] == dD && Uy.d[1] == dD && dL == dR && dD == dU, TNR_ERR_INVALID_ARG, "HOTRG x-step dims");
+    DT A1p = permuted(c, T, {0, 2, 3, 1});          // [a,k,e,i]
+    const int64_t mW = dL * dU * dR;
+    DT W = make_dt(c.pool.get(), {dL, dU, dR, dD, ky});
+    gemm_bulk(c, false, false, mW, dD * ky, dD, 1.0, A1p.p(), mW, 0, Uy.p(), dD, 0, 0.0, W.p(), mW, 0);
+    A1p = DT();
+    DT V = make_dt(c.pool.get(), {dL, dU, dU, dR, ky});
+    {
+        Batch2 bt;
+        bt.n1 = (int)ky;
+        bt.sA1 = dL * dU * dR * dD;
+        bt.sC1 = dL * dU * dU * dR;
+        gemm_bulk(c, false, false, dL * dU, dU * dR, dR * dD, 1.0, W.p(), dL * dU, T.p(), dR * dD, 0.0, V.p(),
+                  dL * dU, bt);
+    }
+    W = DT();
+    DT Tn = make_dt(c.pool.get(), {dL, ky, ky, dR});
+    {
+        Batch2 bt;
+        bt.n1 = (int)dR;                 // d
+        bt.sA1 = dL * dU * dU;
+        bt.sC1 = dL * ky * ky;
+        bt.n2 = (int)ky;                 // b
+        bt.sA2 = dL * dU * dU * dR;
+        bt.sC2 = dL;
+        gemm_bulk(c, false, false, dL, ky, dU * dU, 1.0, V.p(), dL, Uy.p(), dU * dU, 0.0, Tn.p(), dL * ky, bt);
+    }
+    s.T = std::move(Tn);
+}
+
+// step!(::HOTRG) (src/schemes/hotrg.jl:154-160)
+static void step_hotrg(Scheme& s, int chi) {
+    DT Ux = hotrg_xproj(s, s.T, chi);
+    hotrg_step_y(s, Ux);
+    DT Uy = hotrg_yproj(s, s.T, chi);
+    hotrg_step_x(s, Uy);
+}
+
+// ---------------------------------------------------------------------------
+// HOTRG_3D (src/schemes/hotrg3d.jl); legs (1..6) = (D, U', N, E, S', W'), bosonic
+// ---------------------------------------------------------------------------
+// _get_MMdag_3d / _get_MdagM_3d (hotrg3d.jl:48-84); xleg = 5 (W) or 3 (E), 0-based
+static DT gram3d(Scheme& s, const DT& T, bool mdagm) {
+    Ctx& c = *s.ctx;
+    // labels of the six legs of A2 / A1 copies
+    // MMdag: A2[z w Y X y x] A2[v w Y X y u] -> P[x,z,v,u];  A1[p z Y X y r] A1[p v Y X y s] -> N[z,r,v,s]
+    // MdagM: A2[z w Y x y X] A2[v w Y u y X] -> P[x,z,v,u];  A1[p z Y r y X] A1[p v Y s y X] -> N[z,r,v,s]
+    const int Y = Lh, X = Lg, y = Ly, w = Lw;
+    std::vector<int> a2 = mdagm ? std::vector<int>{Lz, w, Y, Lx, y, X} : std::vector<int>{Lz, w, Y, X, y, Lx};
+    std::vector<int> a2c = mdagm ? std::vector<int>{Lv, w, Y, Lu, y, X} : std::vector<int>{Lv, w, Y, X, y, Lu};
+    DT P = contract(c, T, a2, T, a2c, {Lx, Lz, Lv, Lu}, false);
+    std::vector<int> a1 = mdagm ? std::vector<int>{Lp, Lz, Y, Lr, y, X} : std::vector<int>{Lp, Lz, Y, X, y, Lr};
+    std::vector<int> a1c = mdagm ? std::vector<int>{Lp, Lv, Y, Ls, y, X} : std::vector<int>{Lp, Lv, Y, X, y, Ls};
+    DT N = contract(c, T, a1, T, a1c, {Lz, Lr, Lv, Ls}, false);
+    return contract(c, P, {Lx, Lz, Lv, Lu}, N, {Lz, Lr, Lv, Ls}, {Lr, Lx, Ls, Lu}, false);
+}
+
+// _get_hotrg3d_xproj (hotrg3d.jl:86-98)
+static DT hotrg3d_xproj(Scheme& s, const DT& T, int chi) {
+    TsvdOut r1, r2;
+    DT U1, U2;
+    {
+        DT MM = gram3d(s, T, false);
+        U1 = eig_proj(s, MM, chi, r1);
+    }
+    {
+        DT MM = gram3d(s, T, true);
+        U2 = eig_proj(s, MM, chi, r2);
+    }
+    return choose_proj(s, std::move(U1), r1, std::move(U2), r2);
+}
+
+// _step_hotrg3d (hotrg3d.jl:108-117):
+//   T[a,b,c,d,e,f] = Ux[x1,x2,f] Ux[x1',x2',d] Uy[y1,y2,e] Uy[y1',y2',c] A1[a,z,y1',x1',y1,x1] A2[z,b,y2',x2',y2,x2]
+// contracted leg by leg (largest intermediate chi^8), sliced over the open leg a.
+static void hotrg3d_contract(Scheme& s, const DT& Ux, const DT& Uy, int64_t max_entries) {
+    Ctx& c = *s.ctx;
+    const DT& T = s.T;
+    // A1 with the open leg a moved last so slices are contiguous: A1s[z,P,Q,y,x,a]
+    DT A1s = permuted(c, T, {1, 2, 3, 4, 5, 0});
+    const int64_t da = T.d[0];
+    int64_t per_a = 1;
+    for (int i = 1; i < 6; ++i) per_a *= T.d[i];
+    // largest intermediate per unit of a: the N and E legs of A1 replaced by (S, c) and (R, d)
+    int64_t inter = (per_a / (T.d[2] * T.d[3])) * Ux.d[1] * Ux.d[2] * Uy.d[1] * Uy.d[2];
+    int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(da, max_entries / std::max<int64_t>(inter, 1)));
+    const int P_ = Lp, Q_ = Lq, R_ = Lr, S_ = Ls;
+    // output collected as [b,c,d,e,f,a]
+    std::vector<int64_t> od = {T.d[1], Uy.d[2], Ux.d[2], Uy.d[2], Ux.d[2], da};
+    DT Out = make_dt(c.pool.get(), od);
+    const int64_t slab = od[0] * od[1] * od[2] * od[3] * od[4];
+    for (int64_t a0 = 0; a0 < da; a0 += chunk) {
+        int64_t na = std::min(chunk, da - a0);
+        std::vector<int64_t> ds = {T.d[1], T.d[2], T.d[3], T.d[4], T.d[5], na};
+        const double* A1p = A1s.p() + a0 * per_a;
+        // X[z,P,y,x,a,R,d] = A1[z,P,Q,y,x,a] Ux[Q,R,d]
+        DT X = contract(c, A1p, ds, {Lz, P_, Q_, Ly, Lx, La}, Ux.p(), Ux.dims(), {Q_, R_, Ld},
+                        {Lz, P_, Ly, Lx, La, R_, Ld});
+        // Y = X Uy[P,S,c]
+        DT Yt = contract(c, X, {Lz, P_, Ly, Lx, La, R_, Ld}, Uy, {P_, S_, Lc}, {Lz, Ly, Lx, La, R_, Ld, S_, Lc});
+        X = DT();
+        // Z = Y A2[z,b,S,R,u,v]
+        DT Z = contract(c, Yt, {Lz, Ly, Lx, La, R_, Ld, S_, Lc}, T, {Lz, Lb, S_, R_, Lu, Lv},
+                        {Ly, Lx, La, Ld, Lc, Lb, Lu, Lv});
+        Yt = DT();
+        // W = Z conj(Ux[x,v,f])
+        DT W = contract(c, Z, {Ly, Lx, La, Ld, Lc, Lb, Lu, Lv}, Ux, {Lx, Lv, Lf}, {Ly, La, Ld, Lc, Lb, Lu, Lf});
+        Z = DT();
+        // out = W conj(Uy[y,u,e]) -> [b,c,d,e,f,a]
+        DT O = contract(c, W, {Ly, La, Ld, Lc, Lb, Lu, Lf}, Uy, {Ly, Lu, Le}, {Lb, Lc, Ld, Le, Lf, La});
+        copy_f64(c, Out.p() + a0 * slab, O.p(), slab * na);
+    }
+    s.T = permuted(c, Out, {5, 0, 1, 2, 3, 4});
+}
+
+// step!(::HOTRG_3D) (hotrg3d.jl:120-135)
+static void step_hotrg3d(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    for (int sub = 0; sub < 3; ++sub) {
+        DT Ux = hotrg3d_xproj(s, s.T, chi);
+        DT Ty = permuted(c, s.T, {0, 1, 3, 2, 5, 4});   // _get_hotrg3d_yproj: perm ((1,2),(4,3,6,5))
+        DT Uy = hotrg3d_xproj(s, Ty, chi);
+        Ty = DT();
+        hotrg3d_contract(s, Ux, Uy, s.max_slice_entries);
+        s.T = permuted(c, s.T, {5, 3, 1, 2, 0, 4});      // permute(T, ((6,4),(2,3,1,5)))
+    }
+}
+
+void Scheme::step(int chi) {
+    TNR_REQUIRE(chi >= 1, TNR_ERR_INVALID_ARG, "truncrank(chi) needs chi >= 1");
+    last_vals.clear();
+    last_counts.clear();
+    last_eps.clear();
+    switch (kind) {
+        case TNR_TRG: step_trg(*this, chi); break;
+        case TNR_BTRG: step_btrg(*this, chi); break;
+        case TNR_HOTRG: step_hotrg(*this, chi); break;
+        case TNR_HOTRG_3D: step_hotrg3d(*this, chi); break;
+        default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
+    }
+    ++steps;
+}
+
+// finalize! (src/utility/finalize.jl:4-14,62-66): norm into *d_norm, T /= norm
+void Scheme::finalize_async(double* d_norm) {
+    Ctx& c = *ctx;
+    switch (kind) {
+        case TNR_TRG:
+        case TNR_HOTRG: trace2d(c, T.p(), T.d, d_norm); break;
+        case TNR_BTRG: trace_btrg(c, T.p(), T.d, S1.p(), S2.p(), d_norm); break;
+        case TNR_HOTRG_3D: trace3d(c, T.p(), T.d, d_norm); break;
+        default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
+    }
+    scale_inplace(c, T.p(), T.size(), d_norm);
+}
+
+double Scheme::finalize() {
+    finalize_async(ctx->d_scalar + 8);
+    std::vector<double> n = dvec_to_host(*ctx, ctx->d_scalar + 8, 1);
+    return n[0];
+}
+
+std::vector<double> Scheme::run(int chi, int maxiter, bool finalize_beginning) {
+    Ctx& c = *ctx;
+    const int nsteps = std::max(maxiter, 1);       // the loop body runs before the first check
+    const int nn = nsteps + (finalize_beginning ? 1 : 0);
+    Buf norms(c.pool.get(), (size_t)nn * sizeof(double));
+    int at = 0;
+    if (finalize_beginning) finalize_async(norms.d() + at++);
+    for (int i = 0; i < nsteps; ++i) {
+        step(chi);
+        finalize_async(norms.d() + at++);
+    }
+    check_finite(c, norms.d(), nn);
+    std::vector<double> h = dvec_to_host(c, norms.d(), nn);
+    int st = c.read_status_and_clear();
+    TNR_REQUIRE(!(st & ST_NONFINITE), TNR_ERR_NONFINITE, "run!: non-finite norm");
+    return h;
+}
+
+}  // namespace tnr

@@ -1,0 +1,307 @@
+// Truncated SVD / symmetric eigendecomposition on the device
+// (replaces MatrixAlgebraKit's svd_trunc / eigh_trunc! with truncrank(k)).
+//
+// GB300 runs FP64 at ~2 DFMA/clk/SM, so FP64 work that lives on one SM (Jacobi
+// sweeps, Cholesky) is avoided on the iteration path:
+//  * randomized subspace iteration with r = min(3k, 128) columns; every iteration
+//    aligns the basis with the current Ritz vectors (FP32 Jacobi on the r x r
+//    Gram) and orthonormalises with column-scaled CholeskyQR (FP32 Cholesky,
+//    GEMMs in FP64 or split precision);
+//  * the number of iterations comes from the estimated gap (sigma_r / sigma_k)^2
+//    per iteration, so the kept subspace reaches the target angle;
+//  * one final Rayleigh-Ritz in FP64: polar correction of the basis (GEMMs only),
+//    FP32 Jacobi to align, FP64 Jacobi cleanup of the nearly diagonal remainder,
+//    singular values as column norms (one-sided, accurate for graded spectra).
+//  * min(m, n) <= 128: the same final step on the whole matrix (exact).
+#include "common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+namespace tnr {
+
+constexpr int RDIRECT = 128;
+constexpr int RMAX = 128;
+constexpr int MAXIT = 40;
+
+static void check_status(Ctx& c, const char* where) {
+    int st = c.read_status_and_clear();
+    if (st & ST_NONFINITE) throw Error(TNR_ERR_NONFINITE, std::string(where) + ": non-finite values");
+    if (st & ST_JACOBI_NOCONV) throw Error(TNR_ERR_NOT_CONVERGED, std::string(where) + ": Jacobi sweep cap reached");
+}
+
+static std::vector<double> to_host(Ctx& c, const double* d, int n) {
+    std::vector<double> h(n);
+    if (n) TNR_CUDA(cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    return h;
+}
+
+// Q (m x r) <- orthonormal (to FP32 level) basis of span(Y); Y is overwritten.
+// Column-scaled CholeskyQR with an FP32 Cholesky; the first pass is shifted.
+static void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q, int passes) {
+    Buf G(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf ds(c.pool.get(), (size_t)r * sizeof(double));
+    double* src = Y;
+    for (int pass = 0; pass < passes; ++pass) {
+        double shift = pass == 0 ? 1e-6 * std::max(1, r / 16) : 1e-7;
+        for (int attempt = 0;; ++attempt) {
+            gemm_f64(c, true, false, r, r, m, 1.0, src, m, 0, src, m, 0, 0.0, G.d(), r, 0);
+            gram_unit_diag(c, G.d(), r, ds.d());
+            chol_inv_f32(c, G.d(), r, shift);
+            int st = c.read_status_and_clear();
+            if (!(st & ST_CHOL_BREAKDOWN)) break;
+            TNR_REQUIRE(attempt < 5, TNR_ERR_NOT_CONVERGED, "orth: Cholesky breakdown");
+            shift *= 30.0;
+        }
+        col_scale(c, G.d(), r, r, r, ds.d(), 0);         // Linv D
+        double* dst = (src == Q) ? Y : Q;
+        gemm_f64(c, false, true, m, r, r, 1.0, src, m, 0, G.d(), r, 0, 0.0, dst, m, 0);
+        src = dst;
+    }
+    if (src != Q) copy_f64(c, Q, src, m * (int64_t)r);
+}
+
+// Q <- Q (I - E/2 + 3E^2/8), E = Q^T Q - I: cubic correction to FP64 orthonormality (GEMMs only)
+static void polar(Ctx& c, double* Q, int64_t m, int r) {
+    Buf E(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf E2(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf T(c.pool.get(), (size_t)m * r * sizeof(double));
+    for (int it = 0; it < 2; ++it) {
+        gemm_f64(c, true, false, r, r, m, 1.0, Q, m, 0, Q, m, 0, 0.0, E.d(), r, 0);
+        add_identity(c, E.d(), r, -1.0);
+        gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, 0, E.d(), r, 0, 0.0, E2.d(), r, 0);
+        polar_coeff(c, E.d(), E2.d(), E.d(), r);
+        gemm_f64(c, false, false, m, r, r, 1.0, Q, m, 0, E.d(), r, 0, 0.0, T.d(), m, 0);
+        copy_f64(c, Q, T.d(), m * (int64_t)r);
+    }
+}
+
+// Exact SVD of the tall X = op(M) (m x p, p <= 128): X V = Ux diag(s), Ux unit columns.
+// trans=false: X = M (ld m); trans=true: X = M^T with M stored p x m (ld p).
+static void final_svd(Ctx& c, const double* M, bool trans, int64_t m, int p, double* Ux, double* s, double* V) {
+    Buf G(c.pool.get(), (size_t)p * p * sizeof(double));
+    Buf W1(c.pool.get(), (size_t)p * p * sizeof(double));
+    Buf W2(c.pool.get(), (size_t)p * p * sizeof(double));
+    Buf lam(c.pool.get(), (size_t)p * sizeof(double));
+    const int64_t ldm = trans ? p : m;
+    // pass 1: align with the eigenvectors of X^T X (FP32 Jacobi), W1 made orthogonal in FP64
+    gemm_f64(c, !trans, trans, p, p, m, 1.0, M, ldm, 0, M, ldm, 0, 0.0, G.d(), p, 0);
+    jacobi_eigh_f32(c, G.d(), p, p, W1.d(), lam.d());
+    polar(c, W1.d(), p, p);
+    // pass 2: X W1 has nearly orthogonal columns; FP64 Jacobi cleans up the rest
+    gemm_f64(c, trans, false, m, p, p, 1.0, M, ldm, 0, W1.d(), p, 0, 0.0, Ux, m, 0);
+    gemm_f64(c, true, false, p, p, m, 1.0, Ux, m, 0, Ux, m, 0, 0.0, G.d(), p, 0);
+    jacobi_eigh(c, G.d(), p, p, W2.d(), lam.d());
+    gemm_f64(c, false, false, p, p, p, 1.0, W1.d(), p, 0, W2.d(), p, 0, 0.0, V, p, 0);
+    gemm_f64(c, trans, false, m, p, p, 1.0, M, ldm, 0, V, p, 0, 0.0, Ux, m, 0);
+    col_norms(c, Ux, m, p, m, s);
+    col_scale(c, Ux, m, p, m, s, 2);
+    check_status(c, "final_svd");
+}
+
+// symmetric H (p x p): eigenvectors W (FP64-orthogonal) and eigenvalues, |lambda| descending
+static void final_eigh(Ctx& c, const double* H, int p, double* W, double* lam) {
+    Buf W1(c.pool.get(), (size_t)p * p * sizeof(double));
+    Buf W2(c.pool.get(), (size_t)p * p * sizeof(double));
+    Buf G(c.pool.get(), (size_t)p * p * sizeof(double));
+    Buf T(c.pool.get(), (size_t)p * p * sizeof(double));
+    jacobi_eigh_f32(c, H, p, p, W1.d(), lam);
+    polar(c, W1.d(), p, p);
+    gemm_f64(c, false, false, p, p, p, 1.0, H, p, 0, W1.d(), p, 0, 0.0, T.d(), p, 0);
+    gemm_f64(c, true, false, p, p, p, 1.0, W1.d(), p, 0, T.d(), p, 0, 0.0, G.d(), p, 0);
+    jacobi_eigh(c, G.d(), p, p, W2.d(), lam);
+    gemm_f64(c, false, false, p, p, p, 1.0, W1.d(), p, 0, W2.d(), p, 0, 0.0, W, p, 0);
+    check_status(c, "final_eigh");
+}
+
+static void transpose2d(Ctx& c, const double* in, int64_t m, int64_t n, double* out) {
+    int64_t d[2] = {m, n};
+    int perm[2] = {1, 0};
+    permute(c, in, d, 2, perm, out);
+}
+
+// iterations needed so the kept subspace reaches the target angle: one iteration
+// contracts the error by rho = (v[r-1] / v[k-1])^power, v = FP64 estimates of |values|
+// (column norms of the aligned basis) sorted descending
+static int iterations_needed(std::vector<double> v, int k, int r, int power, double target) {
+    std::sort(v.begin(), v.end(), [](double a, double b) { return std::fabs(a) > std::fabs(b); });
+    double vk = std::fabs(v[k - 1]), vr = std::fabs(v[r - 1]), v1 = std::fabs(v[0]);
+    if (!(v1 > 0)) return 2;
+    if (vk <= 1e-13 * v1) return 2;                  // kept tail is numerically zero
+    vr = std::max(vr, 1e-15 * v1);
+    double rho = std::pow(vr / vk, (double)power);
+    if (rho >= 0.999) return MAXIT;
+    int n = (int)std::ceil(std::log(target) / std::log(rho)) + 1;
+    return std::max(2, std::min(MAXIT, n));
+}
+
+static bool debug_on() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = getenv("TNR_DEBUG");
+        on = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return on == 1;
+}
+
+static double target_angle(Ctx& c) { return c.precision == TNR_PREC_F64 ? 1e-13 : 1e-9; }
+
+TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt) {
+    TsvdOut out;
+    const int64_t p = std::min(m, n);
+    k = (int)std::min<int64_t>(k, p);
+    out.k = k;
+    if (k <= 0) return out;
+    if (p <= RDIRECT) {
+        const int pp = (int)p;
+        const bool wide = m < n;
+        const int64_t rows = wide ? n : m;               // X = M (tall) or M^T
+        Buf Ux(c.pool.get(), (size_t)rows * pp * sizeof(double));
+        Buf V(c.pool.get(), (size_t)pp * pp * sizeof(double));
+        Buf sv(c.pool.get(), (size_t)pp * sizeof(double));
+        final_svd(c, M, wide, rows, pp, Ux.d(), sv.d(), V.d());
+        if (!wide) {
+            copy_f64(c, U, Ux.d(), m * (int64_t)k);
+            transpose2d(c, V.d(), pp, k, Vt);
+        } else {
+            copy_f64(c, U, V.d(), m * (int64_t)k);
+            transpose2d(c, Ux.d(), n, k, Vt);
+        }
+        copy_f64(c, s, sv.d(), k);
+        std::vector<double> vals = to_host(c, sv.d(), pp);
+        double tot = 0, kept = 0;
+        for (int i = 0; i < pp; ++i) { tot += vals[i] * vals[i]; if (i < k) kept += vals[i] * vals[i]; }
+        out.fro2 = tot;
+        out.err = std::sqrt(std::max(tot - kept, 0.0));
+        out.vals.assign(vals.begin(), vals.begin() + k);
+        return out;
+    }
+    int r = (int)std::min<int64_t>({p, (int64_t)RMAX, (int64_t)((3 * k + 7) / 8 * 8)});
+    r = std::max(r, std::min((int)p, k + 8));
+    Buf Om(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf Y(c.pool.get(), (size_t)m * r * sizeof(double));
+    Buf Uq(c.pool.get(), (size_t)m * r * sizeof(double));
+    Buf Z(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf Vq(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf G(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf W(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf lam(c.pool.get(), (size_t)r * sizeof(double));
+    fill_normal(c, Om.d(), n * (int64_t)r, c.seed + 0x1000193ull * (++c.call_counter));
+    gemm_bulk(c, false, false, m, r, n, 1.0, M, m, 0, Om.d(), n, 0, 0.0, Y.d(), m, 0);
+    orth_scaled(c, Y.d(), m, r, Uq.d(), 2);
+    int need = MAXIT, it = 0;
+    for (; it < need; ++it) {
+        // Z = M^T U, aligned with the Ritz vectors of Z^T Z (FP32), then orthonormalised
+        gemm_bulk(c, true, false, n, r, m, 1.0, M, m, 0, Uq.d(), m, 0, 0.0, Z.d(), n, 0);
+        gemm_f64(c, true, false, r, r, n, 1.0, Z.d(), n, 0, Z.d(), n, 0, 0.0, G.d(), r, 0);
+        jacobi_eigh_f32(c, G.d(), r, r, W.d(), lam.d());
+        gemm_f64(c, false, false, n, r, r, 1.0, Z.d(), n, 0, W.d(), r, 0, 0.0, Vq.d(), n, 0);
+        copy_f64(c, Z.d(), Vq.d(), n * (int64_t)r);
+        if (it == 0 || it == 2) col_norms(c, Z.d(), n, r, n, lam.d());   // ~ sigma_i (FP64)
+        orth_scaled(c, Z.d(), n, r, Vq.d(), it == 0 ? 2 : 1);
+        gemm_bulk(c, false, false, m, r, n, 1.0, M, m, 0, Vq.d(), n, 0, 0.0, Y.d(), m, 0);
+        orth_scaled(c, Y.d(), m, r, Uq.d(), it == 0 ? 2 : 1);
+        if (it == 0 || it == 2) {
+            std::vector<double> est = to_host(c, lam.d(), r);
+            need = std::max(it + 1, iterations_needed(est, k, r, 2, target_angle(c)));
+            check_status(c, "tsvd");
+        }
+    }
+    out.iters = it;
+    c.last_iters = it;
+    if (debug_on()) fprintf(stderr, "[tnr] tsvd m=%lld n=%lld k=%d r=%d iters=%d\n", (long long)m, (long long)n, k, r, it);
+    // final Rayleigh-Ritz in FP64: M ~ U (U^T M) = U B, B^T = M^T U
+    polar(c, Uq.d(), m, r);
+    Buf Ub(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf Vb(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf sb(c.pool.get(), (size_t)r * sizeof(double));
+    gemm_f64(c, true, false, n, r, m, 1.0, M, m, 0, Uq.d(), m, 0, 0.0, Z.d(), n, 0);
+    final_svd(c, Z.d(), false, n, r, Ub.d(), sb.d(), Vb.d());      // B^T = Ub s Vb^T -> M ~ (U Vb) s Ub^T
+    gemm_f64(c, false, false, m, k, r, 1.0, Uq.d(), m, 0, Vb.d(), r, 0, 0.0, U, m, 0);
+    copy_f64(c, s, sb.d(), k);
+    transpose2d(c, Ub.d(), n, k, Vt);
+    std::vector<double> cur = to_host(c, sb.d(), r);
+    sum_squares(c, M, m * n, c.d_scalar);
+    std::vector<double> f = to_host(c, c.d_scalar, 1);
+    out.fro2 = f[0];
+    double kept = 0, ritz_tail = 0;
+    for (int i = 0; i < r; ++i) { if (i < k) kept += cur[i] * cur[i]; else ritz_tail += cur[i] * cur[i]; }
+    out.err = std::sqrt(ritz_tail + std::max(out.fro2 - kept - ritz_tail, 0.0));
+    out.vals.assign(cur.begin(), cur.begin() + k);
+    return out;
+}
+
+TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk) {
+    TsvdOut out;
+    k = (int)std::min<int64_t>(k, n);
+    out.k = k;
+    if (k <= 0) return out;
+    sum_squares(c, M, n * n, c.d_scalar);
+    if (n <= RDIRECT) {
+        const int nn = (int)n;
+        Buf W(c.pool.get(), (size_t)nn * nn * sizeof(double));
+        Buf l(c.pool.get(), (size_t)nn * sizeof(double));
+        Buf Hs(c.pool.get(), (size_t)nn * nn * sizeof(double));
+        copy_f64(c, Hs.d(), M, n * n);
+        final_eigh(c, Hs.d(), nn, W.d(), l.d());
+        copy_f64(c, U, W.d(), n * (int64_t)k);
+        copy_f64(c, lamk, l.d(), k);
+        std::vector<double> all = to_host(c, l.d(), nn);
+        double disc = 0, tot = 0;
+        for (int i = 0; i < nn; ++i) { tot += all[i] * all[i]; if (i >= k) disc += all[i] * all[i]; }
+        out.err = std::sqrt(disc);
+        out.fro2 = tot;
+        out.vals.assign(all.begin(), all.begin() + k);
+        return out;
+    }
+    int r = (int)std::min<int64_t>({n, (int64_t)RMAX, (int64_t)((3 * k + 7) / 8 * 8)});
+    r = std::max(r, std::min((int)n, k + 8));
+    Buf Om(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf Y(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf Q(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf T(c.pool.get(), (size_t)n * r * sizeof(double));
+    Buf H(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf W(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf l(c.pool.get(), (size_t)r * sizeof(double));
+    fill_normal(c, Om.d(), n * (int64_t)r, c.seed + 0x1000193ull * (++c.call_counter));
+    gemm_bulk(c, false, false, n, r, n, 1.0, M, n, 0, Om.d(), n, 0, 0.0, Y.d(), n, 0);
+    orth_scaled(c, Y.d(), n, r, Q.d(), 2);
+    int need = MAXIT, it = 0;
+    for (; it < need; ++it) {
+        gemm_bulk(c, false, false, n, r, n, 1.0, M, n, 0, Q.d(), n, 0, 0.0, Y.d(), n, 0);
+        gemm_f64(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
+        jacobi_eigh_f32(c, H.d(), r, r, W.d(), l.d());
+        gemm_f64(c, false, false, n, r, r, 1.0, Y.d(), n, 0, W.d(), r, 0, 0.0, T.d(), n, 0);
+        if (it == 0 || it == 2) col_norms(c, T.d(), n, r, n, l.d());     // ~ |lambda_i| (FP64)
+        orth_scaled(c, T.d(), n, r, Q.d(), it == 0 ? 2 : 1);
+        if (it == 0 || it == 2) {
+            std::vector<double> est = to_host(c, l.d(), r);
+            need = std::max(it + 1, iterations_needed(est, k, r, 1, target_angle(c)));
+            check_status(c, "teigh");
+        }
+    }
+    out.iters = it;
+    c.last_iters = it;
+    if (debug_on()) fprintf(stderr, "[tnr] teigh n=%lld k=%d r=%d iters=%d\n", (long long)n, k, r, it);
+    // final Rayleigh-Ritz in FP64
+    polar(c, Q.d(), n, r);
+    gemm_f64(c, false, false, n, r, n, 1.0, M, n, 0, Q.d(), n, 0, 0.0, Y.d(), n, 0);
+    gemm_f64(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
+    final_eigh(c, H.d(), r, W.d(), l.d());
+    gemm_f64(c, false, false, n, k, r, 1.0, Q.d(), n, 0, W.d(), r, 0, 0.0, U, n, 0);
+    copy_f64(c, lamk, l.d(), k);
+    std::vector<double> cur = to_host(c, l.d(), r);
+    std::vector<double> f = to_host(c, c.d_scalar, 1);
+    out.fro2 = f[0];
+    double kept = 0, ritz_tail = 0;
+    for (int i = 0; i < r; ++i) { if (i < k) kept += cur[i] * cur[i]; else ritz_tail += cur[i] * cur[i]; }
+    out.err = std::sqrt(ritz_tail + std::max(out.fro2 - kept - ritz_tail, 0.0));
+    out.vals.assign(cur.begin(), cur.begin() + k);
+    return out;
+}
+
+}  // namespace tnr

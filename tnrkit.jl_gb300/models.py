@@ -1,0 +1,123 @@
+"""Initial partition-function tensors of the models the coarse-graining path runs on.
+
+Host-side constructors (NumPy, FP64) that build the dense arrays TensorKit stores
+for the reference's models; the arrays are indexed ``T[i1, i2, i3, i4]`` (leg order
+left, down, up, right) and, for 3D, ``T[D, U, N, E, S, W]``.  Z_N-symmetric models
+also carry the charge of every basis index so the engine can check conservation.
+
+Reference: src/models/ising.jl, src/models/potts.jl, src/models/clock.jl.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+ising_βc = ising_beta_c = math.log(1.0 + math.sqrt(2.0)) / 2.0                      # ising.jl:1
+f_onsager = -2.1096511446082074596677792835110847808254932754354                # ising.jl:2
+ising_βc_3D = ising_beta_c_3D = 1.0 / 4.51152469                                # ising.jl:8
+
+
+def potts_βc(q):
+    """potts.jl:204"""
+    return math.log(1.0 + math.sqrt(q))
+
+
+potts_beta_c = potts_βc
+
+
+@dataclass
+class SymTensor:
+    """Dense array plus the Z_N charge of each basis index of each leg (N = 1: Trivial)."""
+
+    array: np.ndarray
+    charges: list | None = None
+    N: int = 1
+
+    @property
+    def shape(self):
+        return self.array.shape
+
+
+def _charges(d, nlegs, N):
+    return None if N == 1 else [np.arange(d, dtype=np.int32) % N for _ in range(nlegs)]
+
+
+def classical_ising(symmetry="Z2", beta=ising_βc, h=0.0):
+    """``classical_ising(S, β; h)`` (ising.jl:10-15,39-67).  Trivial and Z2 share the array at h = 0."""
+    if symmetry not in ("Z2", "Trivial"):
+        raise ValueError("symmetry must be 'Trivial' or 'Z2'")
+    if symmetry == "Z2" and h != 0.0:
+        raise ValueError("External magnetic field is not compatible with Z2 symmetry")
+    x, y = math.cosh(beta), math.sinh(beta)
+    w = np.array([math.sqrt(x), math.sqrt(y)])
+    par = np.add.outer(np.add.outer(np.arange(2), np.arange(2)), np.add.outer(np.arange(2), np.arange(2))) % 2
+    init = np.where(par == 0, math.cosh(h * beta), math.sinh(h * beta))
+    a = 2.0 * init * w[:, None, None, None] * w[None, :, None, None] * w[None, None, :, None] * w[None, None, None, :]
+    N = 2 if symmetry == "Z2" else 1
+    return SymTensor(np.ascontiguousarray(a), _charges(2, 4, N), N)
+
+
+def classical_ising_3D(symmetry="Z2", beta=ising_βc_3D, J=1.0):
+    """``classical_ising_3D(Z2Irrep, β; J)`` (ising.jl:149-165): legs D, U', N, E, S', W'."""
+    x, y = math.cosh(beta * J), math.sinh(beta * J)
+    W = np.array([[math.sqrt(x), math.sqrt(y)], [math.sqrt(x), -math.sqrt(y)]])
+    t = np.einsum('ai,aj,ak,al,am,an->ijklmn', W, W, W, W, W, W)
+    a = np.ascontiguousarray(np.transpose(t, (0, 3, 4, 5, 1, 2)))   # permute(t, ((1,4),(5,6,2,3)))
+    if symmetry == "Z2":
+        return SymTensor(a, _charges(2, 6, 2), 2)
+    if symmetry == "Trivial":
+        # ising.jl:130-148: same model in the spin basis
+        K = beta * J
+        tm = np.array([[math.exp(K), math.exp(-K)], [math.exp(-K), math.exp(K)]])
+        ev, v = np.linalg.eigh(tm)
+        q = v @ np.diag(np.sqrt(ev)) @ v.T
+        O = np.zeros((2,) * 6)
+        O[(0,) * 6] = O[(1,) * 6] = 1.0
+        b = np.einsum('abcdef,ia,jb,kc,ld,me,nf->ijklmn', O, q, q, q, q, q, q)
+        return SymTensor(np.ascontiguousarray(b), None, 1)
+    raise ValueError("symmetry must be 'Trivial' or 'Z2'")
+
+
+def _zn_fourier(A, q):
+    w = np.exp(2j * np.pi / q)
+    P = np.array([[w ** (k * c) for c in range(q)] for k in range(q)]) / math.sqrt(q)
+    U = np.einsum('ijkl,ia,jb,kc,ld->abcd', A.astype(complex), P.conj(), P.conj(), P, P)
+    a = np.real(U)
+    ch = np.arange(q)
+    tot = (ch[:, None, None, None] + ch[None, :, None, None] - ch[None, None, :, None] - ch[None, None, None, :]) % q
+    return np.ascontiguousarray(np.where(tot == 0, a, 0.0))
+
+
+def classical_potts(q=3, beta=None, symmetry="ZN"):
+    """``classical_potts(S, q, β)`` (potts.jl:187-195,228-246)."""
+    beta = potts_βc(q) if beta is None else beta
+    i = np.arange(q)
+    d = (i[:, None] == i[None, :]).astype(float)
+    E = -(d[:, :, None, None] + d[None, :, None, :] + d[None, None, :, :] + d.T[:, None, :, None])
+    A = np.exp(-beta * E)
+    if symmetry == "Trivial":
+        return SymTensor(np.ascontiguousarray(A), None, 1)
+    return SymTensor(_zn_fourier(A, q), _charges(q, 4, q), q)
+
+
+def classical_clock(q=6, beta=1.0, symmetry="ZN"):
+    """``classical_clock(S, q, β)`` (clock.jl:1-12,316-339), Trivial and Z_q."""
+    i = np.arange(q)
+    cl = -np.cos(2 * np.pi / q * (i[:, None] - i[None, :]))
+    E = cl[:, :, None, None] + cl[None, :, None, :] + cl.T[None, None, :, :] + cl.T[:, None, :, None]
+    A = np.exp(-beta * E)
+    if symmetry == "Trivial":
+        return SymTensor(np.ascontiguousarray(A), None, 1)
+    return SymTensor(_zn_fourier(A, q), _charges(q, 4, q), q)
+
+
+def random_hotrg_tensor(chi, seed, decay=6.0):
+    """Seeded dense 4-leg tensor for the single-step HOTRG workload: N(0,1) entries times
+    exp(-k/decay) per leg index k, normalised to Frobenius norm 1 (numpy PCG64)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = rng.standard_normal((chi,) * 4)
+    s = np.exp(-np.arange(chi) / decay)
+    a = a * s[:, None, None, None] * s[None, :, None, None] * s[None, None, :, None] * s[None, None, None, :]
+    return SymTensor(a / np.linalg.norm(a), None, 1)
