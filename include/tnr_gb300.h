@@ -142,6 +142,7 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter,
 #define TNR_PROF_CHOL      3  /* Cholesky + inverse; work = r^3                     */
 #define TNR_PROF_PERMUTE   4  /* leg permutes; work = bytes read + written          */
 #define TNR_PROF_SPLIT     5  /* FP64 -> 3xBF16 operand split; work = bytes         */
+#define TNR_PROF_JACOBI32  6  /* FP32 Jacobi (basis alignment); work = r^3          */
 int tnr_profile_enable(int on);
 int tnr_profile_reset(void);
 int tnr_profile_read(int cls, uint64_t* launches, double* total_ms, double* work);

@@ -68,7 +68,8 @@ enum ProfClass : int {
     PROF_CHOL = 3,        // Cholesky + inverse, work = r^3
     PROF_PERMUTE = 4,     // leg permutes, work = bytes moved
     PROF_SPLIT = 5,       // FP64 -> BF16 split conversion, work = bytes moved
-    PROF_NCLASS = 6
+    PROF_JACOBI32 = 6,    // FP32 Jacobi (alignment), work = r^3
+    PROF_NCLASS = 7
 };
 extern std::atomic<bool> g_prof_on;
 int prof_start(cudaStream_t s);
@@ -207,6 +208,9 @@ void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, dou
 void chol_inv_f32(Ctx& c, double* G, int r, double shift);
 void add_identity(Ctx& c, double* X, int r, double alpha);
 void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r);
+void decouple_rotation(Ctx& c, const double* G, int r, int kb, double* P);
+void diag_copy(Ctx& c, const double* G, int r, int kb, double* lam);
+void diag_to_host(Ctx& c, const double* G, int r, double* host);
 void fill_normal(Ctx& c, double* x, int64_t n, uint64_t seed);
 void col_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);
 void row_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);

@@ -12,14 +12,19 @@ namespace tnr {
 
 constexpr int JMAX = 160;           // largest matrix held in shared memory
 constexpr int JTHREADS = 512;
-constexpr int JMAX_SWEEPS = 40;
+constexpr int JMAX_SWEEPS = 60;
 
 template <class T>
 __device__ __forceinline__ T& SG(T* G, int ld, int i, int j) { return G[i + j * ld]; }
 
+// Rotation thresholds: rotate (p, q) iff |g_pq| > max(rel * sqrt|g_pp g_qq|, floor * |G|_F).
+// FP64 cleans up matrices already aligned by the FP32 pass: rel = 1e-12 leaves
+// orthogonality errors of 1e-12; the floor 1e-22 keeps graded values down to 1e-11 of the
+// largest singular value resolved while rounding noise (~1e-32) is left alone.
+// FP32 (alignment only) cannot resolve entries below ~1e-7 |G|: floor 1e-9.
 template <class T> struct JTol;
-template <> struct JTol<double> { static constexpr double rel = 1e-15; };
-template <> struct JTol<float> { static constexpr double rel = 2e-7; };
+template <> struct JTol<double> { static constexpr double rel = 1e-12, floor = 1e-22; };
+template <> struct JTol<float> { static constexpr double rel = 2e-7, floor = 1e-9; };
 
 // Parallel (round-robin ordering) two-sided Jacobi in shared memory, arithmetic type T.
 // Input G is FP64 (symmetrised on load); W (FP64, r x r) and lam (FP64) are sorted by |lambda|.
@@ -56,7 +61,7 @@ k_jacobi(const double* __restrict__ Gin, int64_t ldg, int r, double* __restrict_
         if (tid == 0) fro = sqrt(acc);
     }
     __syncthreads();
-    const T abs_floor = (T)1e-30 * fro;
+    const T abs_floor = (T)JTol<T>::floor * fro;
     const T reltol = (T)JTol<T>::rel;
     int sweep = 0;
     bool converged = (r <= 1);
@@ -154,7 +159,7 @@ static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W
     int rec = prof_start(c.stream);
     k_jacobi<T><<<1, nt, smem, c.stream>>>(G, ldg, r, W, lam, ww.as<T>(), c.d_status);
     check_launch("jacobi");
-    prof_stop(rec, c.stream, PROF_JACOBI, (double)r * r * r);
+    prof_stop(rec, c.stream, sizeof(T) == 8 ? PROF_JACOBI : PROF_JACOBI32, (double)r * r * r);
 }
 
 void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {

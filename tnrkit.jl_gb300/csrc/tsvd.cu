@@ -135,7 +135,9 @@ static int iterations_needed(std::vector<double> v, int k, int r, int power, dou
     vr = std::max(vr, 1e-15 * v1);
     double rho = std::pow(vr / vk, (double)power);
     if (rho >= 0.999) return MAXIT;
-    int n = (int)std::ceil(std::log(target) / std::log(rho)) + 1;
+    // +2: the column-norm estimates of the smallest values are upper bounds, and vk is an
+    // estimate too; two spare iterations keep the kept subspace at the target angle
+    int n = (int)std::ceil(std::log(target) / std::log(rho)) + 2;
     return std::max(2, std::min(MAXIT, n));
 }
 
