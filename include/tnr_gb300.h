@@ -158,6 +158,27 @@ int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t 
                    const double* B, int64_t ldb, int64_t strideB,
                    double* C, int64_t ldc, int64_t strideC, int batch);
 
+/* ---- allocation-free split GEMM ------------------------------------------ */
+/* No counterpart in the reference.  C = alpha * op(A) op(B) + beta * C on device
+ * pointers (column-major FP64), computed by the split 3xBF16 tensor-core kernel
+ * without allocating: its BF16 plane scratch is a 16 MiB file-scope device array
+ * that every GPU loading the library holds until exit.  For callers that cannot
+ * call cudaMalloc (code running inside another allocator's arena, such as a
+ * CUDA.jl pool or a server that reserves all free HBM, and latency-critical paths
+ * where cudaMalloc's implicit device synchronisation stalls other streams).
+ *   - limits: m >= 64, n >= 16, k >= 16 and 6 * (m + n) * ceil8(k) bytes <= 16 MiB;
+ *     larger operands are rejected with TNR_ERR_INVALID_ARG and a message in err;
+ *   - the first call on a device resolves the scratch's device address with that
+ *     device current; make that first call before any stream capture;
+ *   - every call shares the one scratch array: calls that overlap on the GPU
+ *     (different streams, different host threads) race; serialise them;
+ *   - runs on `stream` (NULL = legacy default stream) and returns after
+ *     synchronising it; calls no cudaMalloc, cudaFree or allocating routine. */
+int tnr_gemm_split_noalloc(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                           const double* A, int64_t lda, const double* B, int64_t ldb,
+                           double beta, double* C, int64_t ldc, void* stream,
+                           char* err, size_t err_cap);
+
 /* ---- library info ------------------------------------------------------- */
 int tnr_device_info(int* sm_count, int* cc_major, int* cc_minor, size_t* hbm_bytes);
 const char* tnr_version(void);

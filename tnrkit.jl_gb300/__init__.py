@@ -35,7 +35,8 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_free_energy", "tnr_get_tensor", "tnr_singular_values", "tnr_truncation_errors", "tnr_btrg_bonds",
            "tnr_device_bytes", "tnr_destroy", "tnr_last_error", "tnr_status_string", "tnr_timer_start",
            "tnr_timer_stop", "tnr_run_batch", "tnr_device_info", "tnr_version", "tnr_kernel_launches",
-           "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm"]
+           "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm",
+           "tnr_gemm_split_noalloc"]
 
 
 class TNRError(RuntimeError):
@@ -88,6 +89,8 @@ def lib():
         "tnr_profile_read": (I, [I, C.POINTER(C.c_uint64), pd, pd]),
         "tnr_debug_gemm": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, pd, C.c_int64, C.c_int64, pd, C.c_int64,
                                C.c_int64, pd, C.c_int64, C.c_int64, I]),
+        "tnr_gemm_split_noalloc": (I, [I, I, C.c_int64, C.c_int64, C.c_int64, D, P, C.c_int64, P, C.c_int64, D, P,
+                                       C.c_int64, P, C.c_char_p, Z]),
         "tnr_device_info": (I, [C.POINTER(I), C.POINTER(I), C.POINTER(I), pz]),
         "tnr_version": (C.c_char_p, []),
         "tnr_kernel_launches": (C.c_uint64, []),

@@ -20,7 +20,9 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
+#include <string>
 
 namespace tnr {
 
@@ -381,4 +383,124 @@ bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, do
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free entry point: the same split kernel with its BF16 plane scratch in a
+// file-scope device array instead of the pool.  For callers that cannot call cudaMalloc:
+// code running inside another allocator's arena (a Julia CUDA.jl pool, or a serving
+// process that reserves all free HBM up front) and latency-critical paths where
+// cudaMalloc's implicit device synchronisation would stall every other stream.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(16) << 20;   // 16 MiB of BF16 planes, held until exit
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+static __device__ int g_noalloc_status;
+
+struct NoAllocDevice {
+    unsigned char* scratch = nullptr;
+    int* status = nullptr;
+};
+constexpr int NOALLOC_MAX_DEVICES = 64;
+NoAllocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_mu;
+
+// First call on a device: resolve the device addresses of the file-scope arrays with that
+// device current (a host-side use of the array name is not a device address).
+const NoAllocDevice* noalloc_device(int dev) {
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    NoAllocDevice& d = g_noalloc_dev[dev];
+    if (!d.scratch) {
+        void* p = nullptr;
+        void* q = nullptr;
+        TNR_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        TNR_CUDA(cudaGetSymbolAddress(&q, g_noalloc_status));
+        d.scratch = static_cast<unsigned char*>(p);
+        d.status = static_cast<int*>(q);
+    }
+    return &d;
+}
+
+}  // namespace
+
 }  // namespace tnr
+
+using tnr::Error;
+
+extern "C" int tnr_gemm_split_noalloc(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                                      const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                                      double* C, int64_t ldc, void* stream, char* err, size_t err_cap) {
+    using namespace tnr;
+    auto report = [&](int code, const std::string& msg) {
+        if (err && err_cap) {
+            size_t len = std::min(err_cap - 1, msg.size());
+            std::memcpy(err, msg.data(), len);
+            err[len] = 0;
+        }
+        return code;
+    };
+    if (!A || !B || !C) return report(TNR_ERR_INVALID_ARG, "NULL operand pointer");
+    if (m < 64 || n < 16 || k < 16)
+        return report(TNR_ERR_UNSUPPORTED, "split kernel shape limits: m >= 64, n >= 16, k >= 16");
+    if (lda < (ta ? k : m) || ldb < (tb ? n : k) || ldc < m) return report(TNR_ERR_INVALID_ARG, "leading dimension too small");
+    if ((n + BN - 1) / BN > 65535) return report(TNR_ERR_UNSUPPORTED, "n too large for the grid");
+    const int64_t Kp = (k + 7) / 8 * 8;
+    const size_t bytesA = (size_t)3 * m * Kp * 2, bytesB = (size_t)3 * n * Kp * 2;
+    const size_t offB = (bytesA + 255) / 256 * 256;
+    if (offB + bytesB > NOALLOC_SCRATCH_BYTES)
+        return report(TNR_ERR_INVALID_ARG, "operands need " + std::to_string(offB + bytesB) +
+                                               " bytes of BF16 planes; the allocation-free scratch holds " +
+                                               std::to_string(NOALLOC_SCRATCH_BYTES) + " (6*(m+n)*ceil8(k) bytes)");
+    try {
+        int dev = 0;
+        TNR_CUDA(cudaGetDevice(&dev));
+        TNR_REQUIRE(dev >= 0 && dev < NOALLOC_MAX_DEVICES, TNR_ERR_UNSUPPORTED, "device index out of range");
+        const NoAllocDevice* d = noalloc_device(dev);
+        TNR_REQUIRE(encode_fn(), TNR_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        static std::once_flag once;
+        std::call_once(once, [] {
+            cudaFuncSetAttribute(k_gemm_split_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        });
+        // the status word keeps the previous call's value: clear it
+        TNR_CUDA(cudaMemsetAsync(d->status, 0, sizeof(int), st));
+        __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(d->scratch);
+        __nv_bfloat16* pb = reinterpret_cast<__nv_bfloat16*>(d->scratch + offB);
+        SplitArgs sa{A, m, k, Kp, ta ? lda : 1, ta ? 1 : lda, 0, 0, 1, 1, pa};
+        SplitArgs sb{B, n, k, Kp, tb ? 1 : ldb, tb ? ldb : 1, 0, 0, 1, 1, pb};
+        for (const SplitArgs* s : {&sa, &sb}) {
+            int64_t ntiles = ((s->rows + 31) / 32) * ((Kp + 31) / 32);
+            int g = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 16);
+            k_split_planes<<<g, dim3(32, 8), 0, st>>>(*s);
+            check_launch("split_planes (allocation-free)");
+        }
+        CUtensorMap mA, mB;
+        make_map(&mA, pa, m, Kp, 1, BM);
+        make_map(&mB, pb, n, Kp, 1, BN);
+        TcArgs args;
+        args.m = m;
+        args.n = n;
+        args.nkb = (int)((Kp + BK - 1) / BK);
+        args.alpha = alpha;
+        args.beta = beta;
+        args.C = C;
+        args.ldc = ldc;
+        args.n1 = 1;
+        args.sC1 = 0;
+        args.sC2 = 0;
+        args.a_batched = 0;
+        args.b_batched = 0;
+        args.status = d->status;
+        dim3 grid((unsigned)((m + BM - 1) / BM), (unsigned)((n + BN - 1) / BN), 1);
+        k_gemm_split_tc<<<grid, NTHREADS, SMEM_BYTES, st>>>(mA, mB, args);
+        check_launch("gemm_split_tc (allocation-free)");
+        int h = 0;
+        TNR_CUDA(cudaMemcpyAsync(&h, d->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TNR_CUDA(cudaStreamSynchronize(st));
+        TNR_REQUIRE(h == 0, TNR_ERR_CUDA, "tensor-core pipeline wait timed out (status " + std::to_string(h) + ")");
+    } catch (const Error& e) {
+        return report(e.code, e.what());
+    } catch (const std::exception& e) {
+        return report(TNR_ERR_CUDA, e.what());
+    }
+    return report(TNR_OK, "");
+}
