@@ -44,6 +44,10 @@ def parse():
                    help="instances of the batch also solved on the plain FP64 path (solves/s and |df/f|)")
     p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="beta_sweep", choices=["beta_sweep", "hotrg_step", "serving", "hotrg3d"],
+                   help="beta_sweep is the headline metric; the others measure the remaining configurations")
+    p.add_argument("--chis", default=None, help="comma-separated chi list for hotrg_step / hotrg3d")
+    p.add_argument("--requests", type=int, default=32, help="serving: number of requests in the arrival trace")
     return p.parse_args()
 
 
@@ -330,9 +334,110 @@ def run_ours(args, d):
     return out, chis
 
 
+def run_hotrg_step(args, tnr):
+    """One HOTRG step (+ finalize) on the seeded chi^4 test tensor, plain FP64 vs split."""
+    chis = [int(c) for c in (args.chis or "32,48,64").split(",")]
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    out = []
+    for chi in chis:
+        T = tnr.random_hotrg_tensor(chi, 1)
+        row = {"chi": chi, "flops_contraction": 8.0 * chi ** 7 + 28.0 * chi ** 6}
+        norms = {}
+        for name, prec in (("f64", tnr.PREC_F64), ("split", tnr.PREC_SPLIT)):
+            times = []
+            for rep in range(1 + max(args.steps, 1)):
+                s = tnr.HOTRG(T, precision=prec)
+                with tnr.Timer(s) as tm:
+                    tnr.step(s, tnr.truncrank(chi))
+                    n = tnr.finalize(s)
+                if rep > 0:
+                    times.append(tm.ms)
+                norms[name] = n
+                s.close()
+            row[name + "_ms"] = statistics.median(times)
+            row[name + "_tflops"] = row["flops_contraction"] / (row[name + "_ms"] * 1e-3) / 1e12
+        row["split_rel_norm_err"] = abs(norms["split"] / norms["f64"] - 1)
+        if chi <= 32 and not args.no_cpu_baseline:
+            import tnr_oracle as o
+            so = o.HOTRG(o.random_hotrg_tensor(chi, 1))
+            t0 = time.perf_counter()
+            o.step(so, chi)
+            no = o.finalize(so)
+            row["cpu_oracle_ms"] = 1000 * (time.perf_counter() - t0)
+            row["f64_rel_norm_err_vs_oracle"] = abs(norms["f64"] / no - 1)
+        out.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+    return {"workload": "hotrg_step: one HOTRG step + finalize on the seeded chi^4 tensor (N(0,1) x exp(-k/6) per "
+                        "leg, Frobenius 1, PCG64 seed 1)", "rows": out}
+
+
+def run_serving(args, tnr):
+    """Poisson arrivals (mean 200/s) of mixed run! requests through the serving loop."""
+    rng = np.random.Generator(np.random.PCG64(args.seed))
+    n = args.requests
+    gaps = rng.exponential(1.0 / 200.0, n)
+    arrivals = np.cumsum(gaps)
+    reqs = []
+    for i in range(n):
+        model = rng.integers(0, 3)
+        beta = float(rng.uniform(0.2, 1.2))
+        scheme = "HOTRG" if rng.integers(0, 2) == 0 else "BTRG"
+        chi = int(rng.integers(16, 65))
+        maxiter = int(rng.integers(20, 41))
+        T = (tnr.classical_ising("Z2", beta) if model == 0 else
+             tnr.classical_potts(3, beta) if model == 1 else tnr.classical_clock(6, beta))
+        reqs.append((T, scheme, chi, maxiter, beta, ("ising_z2", "potts_z3", "clock_z6")[model]))
+    prec = tnr.PREC_SPLIT if args.precision == "split" else tnr.PREC_F64
+    srv = tnr.Server(hbm_budget_bytes=200 << 30, max_active=48, precision=prec)
+    t0 = time.perf_counter()
+    ids = []
+    for (T, scheme, chi, maxiter, beta, name), at in zip(reqs, arrivals):
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        ids.append(srv.submit(T, scheme, chi, maxiter))
+    lats, queues, fs = [], [], []
+    for rid, (T, scheme, chi, maxiter, beta, name) in zip(ids, reqs):
+        norms, lat, q = srv.result(rid)
+        lats.append(lat)
+        queues.append(q)
+        fs.append(tnr.free_energy(norms, beta, 4.0 if scheme == "HOTRG" else 2.0))
+    wall = time.perf_counter() - t0
+    srv.close()
+    return {"workload": "serving: %d Poisson(200/s) run! requests, models {Ising Z2, Potts Z3, clock Z6}, "
+                        "beta~U[0.2,1.2], HOTRG|BTRG, chi~U{16..64}, maxiter~U[20,40], seed %d" % (n, args.seed),
+            "solves_per_s": n / wall, "wall_s": wall, "p50_ms": float(np.percentile(lats, 50)),
+            "p99_ms": float(np.percentile(lats, 99)), "p50_queue_ms": float(np.percentile(queues, 50)),
+            "precision": args.precision, "admission": "HBM footprint, budget 200 GiB, 48 slots"}
+
+
+def run_hotrg3d(args, tnr):
+    chis = [int(c) for c in (args.chis or "16").split(",")]
+    rows = []
+    for chi in chis:
+        T = tnr.classical_ising_3D("Z2", 0.2216)
+        s = tnr.HOTRG_3D(T, precision=tnr.PREC_SPLIT if args.precision == "split" else tnr.PREC_F64)
+        with tnr.Timer(s) as tm:
+            data = tnr.run(s, tnr.truncrank(chi), tnr.maxiter(args.maxiter))
+        rows.append({"chi": chi, "iterations": args.maxiter, "ms": tm.ms,
+                     "f": tnr.free_energy(data, 0.2216, 8.0), "precision": args.precision})
+        print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+        s.close()
+    return {"workload": "hotrg3d: 3D Ising Z2 at beta=0.2216, HOTRG_3D", "rows": rows}
+
+
 def main():
     args = parse()
     d = Dist()
+    if args.workload != "beta_sweep":
+        sys.path.insert(0, ROOT)
+        import __graft_entry__ as ge
+        ge.build()
+        tnr = ge.package()
+        fn = {"hotrg_step": run_hotrg_step, "serving": run_serving, "hotrg3d": run_hotrg3d}[args.workload]
+        if d.rank == 0:
+            print(json.dumps(fn(args, tnr)), flush=True)
+        return
     if args.impl == "reference":
         if d.rank != 0:
             return

@@ -135,6 +135,28 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter,
                   int finalize_beginning, double* norms_out, size_t stride,
                   size_t* n_out, double* device_ms_out, double* latency_ms_out);
 
+/* ---- serving loop: run!() requests admitted by HBM footprint ------------- */
+/* No reference counterpart (the reference runs one run!() per call,
+ * tnrscheme.jl:33).  A server owns max_active host workers; a request is admitted
+ * when a worker is free and its estimated footprint (tnr_footprint_bytes: chi^4
+ * tensors for TRG/BTRG, two chi^5 intermediates for HOTRG, chi^6 tensors plus a
+ * sliced chi^8 intermediate for HOTRG_3D) fits the unused part of the budget.
+ * Admitted requests keep their tensor resident and iterate concurrently, one
+ * CUDA stream each; requests that arrive meanwhile wait in FIFO order and are
+ * admitted as slots and memory free up.  A request that can never fit is refused
+ * at submission with TNR_ERR_ADMISSION. */
+typedef struct tnr_server_s* tnr_server;
+int tnr_server_create(tnr_server* out, size_t hbm_budget_bytes, int max_active, int precision);
+int tnr_server_submit(tnr_server s, int kind, int nlegs, const int64_t* dims, const double* data,
+                      int chi, int maxiter, double btrg_k, uint64_t* id_out);
+/* wait != 0 blocks until request `id` finishes.  Returns the request's status;
+ * latency_ms = submission to completion, queue_ms = submission to admission. */
+int tnr_server_poll(tnr_server s, uint64_t id, int wait, int* done, double* norms, size_t cap,
+                    size_t* n_out, double* latency_ms, double* queue_ms);
+int tnr_server_stats(tnr_server s, int* active, int* queued, size_t* bytes_in_use);
+int tnr_server_destroy(tnr_server s);
+size_t tnr_footprint_bytes(int kind, int chi, int nlegs, const int64_t* dims);
+
 /* ---- profiling: CUDA events around every launch of a kernel class -------- */
 #define TNR_PROF_GEMM_BULK 0  /* bulk contraction GEMMs; work = flops               */
 #define TNR_PROF_GEMM_F64  1  /* FP64 GEMMs inside the decompositions; work = flops */

@@ -24,7 +24,7 @@ from .models import (SymTensor, classical_clock, classical_ising, classical_isin
                      random_hotrg_tensor)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libtnr_gb300.so")
+LIB_PATH = os.environ.get("TNR_GB300_LIB") or os.path.join(HERE, "libtnr_gb300.so")
 
 TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D = 1, 2, 3, 4
 PREC_F64, PREC_SPLIT = 0, 1
@@ -36,7 +36,8 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_device_bytes", "tnr_destroy", "tnr_last_error", "tnr_status_string", "tnr_timer_start",
            "tnr_timer_stop", "tnr_run_batch", "tnr_device_info", "tnr_version", "tnr_kernel_launches",
            "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm",
-           "tnr_gemm_split_noalloc"]
+           "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_poll",
+           "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes"]
 
 
 class TNRError(RuntimeError):
@@ -91,6 +92,12 @@ def lib():
                                C.c_int64, pd, C.c_int64, C.c_int64, I]),
         "tnr_gemm_split_noalloc": (I, [I, I, C.c_int64, C.c_int64, C.c_int64, D, P, C.c_int64, P, C.c_int64, D, P,
                                        C.c_int64, P, C.c_char_p, Z]),
+        "tnr_server_create": (I, [C.POINTER(P), Z, I, I]),
+        "tnr_server_submit": (I, [P, I, I, pi64, pd, I, I, D, C.POINTER(C.c_uint64)]),
+        "tnr_server_poll": (I, [P, C.c_uint64, I, C.POINTER(I), pd, Z, pz, pd, pd]),
+        "tnr_server_stats": (I, [P, C.POINTER(I), C.POINTER(I), pz]),
+        "tnr_server_destroy": (I, [P]),
+        "tnr_footprint_bytes": (Z, [I, I, I, pi64]),
         "tnr_device_info": (I, [C.POINTER(I), C.POINTER(I), C.POINTER(I), pz]),
         "tnr_version": (C.c_char_p, []),
         "tnr_kernel_launches": (C.c_uint64, []),
@@ -340,6 +347,66 @@ def profile_read():
         _check(lib().tnr_profile_read(cls, C.byref(n), C.byref(ms), C.byref(w)))
         out[name] = (n.value, ms.value, w.value)
     return out
+
+
+class Server:
+    """Serving loop: submit run! requests, admitted by HBM footprint, solved concurrently.
+
+    ``submit(T, scheme, chi, maxiter)`` returns a request id; ``result(id)`` blocks and
+    returns (norms, latency_ms, queue_ms)."""
+
+    KINDS = {"TRG": TNR_TRG, "BTRG": TNR_BTRG, "HOTRG": TNR_HOTRG, "HOTRG_3D": TNR_HOTRG_3D}
+
+    def __init__(self, hbm_budget_bytes, max_active=32, precision=PREC_F64):
+        h = C.c_void_p()
+        _check(lib().tnr_server_create(C.byref(h), int(hbm_budget_bytes), int(max_active), int(precision)))
+        self._h = h
+        self.maxiter = {}
+
+    def submit(self, T, scheme, chi, maxiter, k=-0.5):
+        a = np.asfortranarray(_as_sym(T).array, dtype=np.float64)
+        kind = self.KINDS[scheme if isinstance(scheme, str) else scheme.__name__]
+        dims = (C.c_int64 * a.ndim)(*a.shape)
+        rid = C.c_uint64()
+        st = lib().tnr_server_submit(self._h, kind, a.ndim, dims, a.ctypes.data_as(C.POINTER(C.c_double)), int(chi),
+                                     int(maxiter), float(k), C.byref(rid))
+        _check(st)
+        self.maxiter[rid.value] = maxiter
+        return rid.value
+
+    def result(self, rid, wait=True):
+        cap = max(self.maxiter[rid], 1) + 1
+        out = np.empty(cap)
+        done, n, lat, q = C.c_int(), C.c_size_t(), C.c_double(), C.c_double()
+        st = lib().tnr_server_poll(self._h, rid, 1 if wait else 0, C.byref(done),
+                                   out.ctypes.data_as(C.POINTER(C.c_double)), cap, C.byref(n), C.byref(lat),
+                                   C.byref(q))
+        _check(st)
+        if not done.value:
+            return None
+        return list(out[:n.value]), lat.value, q.value
+
+    def stats(self):
+        a, qd, b = C.c_int(), C.c_int(), C.c_size_t()
+        _check(lib().tnr_server_stats(self._h, C.byref(a), C.byref(qd), C.byref(b)))
+        return {"active": a.value, "queued": qd.value, "bytes_in_use": b.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tnr_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def footprint_bytes(scheme, chi, dims):
+    kind = Server.KINDS[scheme if isinstance(scheme, str) else scheme.__name__]
+    d = (C.c_int64 * len(dims))(*dims)
+    return int(lib().tnr_footprint_bytes(kind, int(chi), len(dims), d))
 
 
 def free_energy(data, beta, scalefactor=2.0, initial_size=1.0):

@@ -102,8 +102,24 @@ static size_t round_block(size_t b) {
     return (b + g - 1) / g * g;
 }
 
+// Stream-ordered allocations: cudaMallocAsync / cudaFreeAsync never synchronise the device,
+// so many handles on many streams allocate without stalling each other.  The device's
+// default pool keeps freed memory cached (release threshold raised once per process).
+static void keep_pool_memory() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaMemPool_t mp;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&mp, dev) == cudaSuccess) {
+            uint64_t thr = ~0ull;
+            cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        cudaGetLastError();
+    });
+}
+
 Pool::~Pool() {
-    for (auto& kv : size_of_) cudaFree(kv.first);
+    for (auto& kv : size_of_) cudaFreeAsync(kv.first, stream_);
 }
 
 void* Pool::get(size_t bytes) {
@@ -115,11 +131,12 @@ void* Pool::get(size_t bytes) {
         return p;
     }
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, b);
+    keep_pool_memory();
+    cudaError_t e = cudaMallocAsync(&p, b, stream_);
     if (e != cudaSuccess) {
         cudaGetLastError();
         trim();                                // give cached blocks back, then retry once
-        e = cudaMalloc(&p, b);
+        e = cudaMallocAsync(&p, b, stream_);
         if (e != cudaSuccess) {
             cudaGetLastError();
             throw Error(TNR_ERR_OOM, "device allocation of " + std::to_string(b) + " bytes failed");
@@ -144,9 +161,10 @@ void Pool::trim() {
             held_ -= it->second;
             size_of_.erase(it);
         }
-        cudaFree(kv.second);
+        cudaFreeAsync(kv.second, stream_);
     }
     free_.clear();
+    cudaStreamSynchronize(stream_);
 }
 
 DT make_dt(Pool* pool, const std::vector<int64_t>& dims) {
@@ -170,9 +188,10 @@ Ctx::Ctx(cudaStream_t s, int prec, uint64_t seed_) : precision(prec) {
         own_stream = true;
     }
     pool.reset(new Pool(stream));
-    TNR_CUDA(cudaMalloc(&d_status, 64));
+    keep_pool_memory();
+    TNR_CUDA(cudaMallocAsync((void**)&d_status, 64, stream));
     TNR_CUDA(cudaMemsetAsync(d_status, 0, 64, stream));
-    TNR_CUDA(cudaMalloc(&d_scalar, 4096 * sizeof(double)));
+    TNR_CUDA(cudaMallocAsync((void**)&d_scalar, 4096 * sizeof(double), stream));
     TNR_CUDA(cudaEventCreate(&ev0));
     TNR_CUDA(cudaEventCreate(&ev1));
 }
@@ -180,8 +199,9 @@ Ctx::Ctx(cudaStream_t s, int prec, uint64_t seed_) : precision(prec) {
 Ctx::~Ctx() {
     if (stream) cudaStreamSynchronize(stream);
     pool.reset();
-    if (d_status) cudaFree(d_status);
-    if (d_scalar) cudaFree(d_scalar);
+    if (d_status) cudaFreeAsync(d_status, stream);
+    if (d_scalar) cudaFreeAsync(d_scalar, stream);
+    if (stream) cudaStreamSynchronize(stream);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (own_stream && stream) cudaStreamDestroy(stream);

@@ -341,7 +341,7 @@ bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, do
                    int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
     const int batch = bt.n1 * bt.n2;
     // tiny products stay on the FP64 path (the early coarse-graining steps carry the largest weights)
-    if (m < 64 || n < 16 || k < 16 || (double)m * n * k * batch < (double)(1 << 22)) return false;
+    if (m < 64 || n < 16 || k < 16 || (double)m * n * k * batch < (double)(1 << 26)) return false;
     if (batch > 65535 || (m + BM - 1) / BM > 2147483647 || (n + BN - 1) / BN > 65535) return false;
     if (!encode_fn()) return false;
     static std::once_flag once;

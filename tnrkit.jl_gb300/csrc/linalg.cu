@@ -12,7 +12,8 @@ namespace tnr {
 
 constexpr int JMAX = 160;           // largest matrix held in shared memory
 constexpr int JTHREADS = 512;
-constexpr int JMAX_SWEEPS = 60;
+constexpr int JMAX_SWEEPS = 60;          // FP64 cleanup
+constexpr int JMAX_SWEEPS_F32 = 16;      // FP32 alignment (converged or cycling on noise by then)
 
 template <class T>
 __device__ __forceinline__ T& SG(T* G, int ld, int i, int j) { return G[i + j * ld]; }
@@ -21,10 +22,21 @@ __device__ __forceinline__ T& SG(T* G, int ld, int i, int j) { return G[i + j * 
 // FP64 cleans up matrices already aligned by the FP32 pass: rel = 1e-12 leaves
 // orthogonality errors of 1e-12; the floor 1e-22 keeps graded values down to 1e-11 of the
 // largest singular value resolved while rounding noise (~1e-32) is left alone.
-// FP32 (alignment only) cannot resolve entries below ~1e-7 |G|: floor 1e-9.
+// FP32 (alignment only) cannot resolve entries below ~1e-7 |G|: below the floor 1e-9 |G|
+// rotations would only stir rounding noise, so they are skipped (the FP64 stage resolves
+// those directions).
+#ifndef TNR_JACOBI64_REL
+#define TNR_JACOBI64_REL 1e-12
+#endif
+#ifndef TNR_JACOBI64_FLOOR
+#define TNR_JACOBI64_FLOOR 1e-22
+#endif
+#ifndef TNR_JACOBI32_FLOOR
+#define TNR_JACOBI32_FLOOR 1e-9
+#endif
 template <class T> struct JTol;
-template <> struct JTol<double> { static constexpr double rel = 1e-12, floor = 1e-22; };
-template <> struct JTol<float> { static constexpr double rel = 2e-7, floor = 1e-9; };
+template <> struct JTol<double> { static constexpr double rel = TNR_JACOBI64_REL, floor = TNR_JACOBI64_FLOOR; };
+template <> struct JTol<float> { static constexpr double rel = 2e-7, floor = TNR_JACOBI32_FLOOR; };
 
 // Parallel (round-robin ordering) two-sided Jacobi in shared memory, arithmetic type T.
 // Input G is FP64 (symmetrised on load); W (FP64, r x r) and lam (FP64) are sorted by |lambda|.
@@ -39,6 +51,9 @@ k_jacobi(const double* __restrict__ Gin, int64_t ldg, int r, double* __restrict_
     T* sn = cs + (JMAX / 2 + 1);
     int* pp = (int*)(sn + (JMAX / 2 + 1));
     int* qq = pp + (JMAX / 2 + 1);
+    // FP32: the eigenvector matrix lives in shared memory too (two r x r FP32 arrays fit);
+    // FP64 keeps it in global memory (L1/L2 resident)
+    if (sizeof(T) == 4) Ww = reinterpret_cast<T*>(qq + (JMAX / 2 + 1));
     __shared__ int rot_count;
     __shared__ T fro;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -65,7 +80,8 @@ k_jacobi(const double* __restrict__ Gin, int64_t ldg, int r, double* __restrict_
     const T reltol = (T)JTol<T>::rel;
     int sweep = 0;
     bool converged = (r <= 1);
-    for (; sweep < JMAX_SWEEPS && !converged; ++sweep) {
+    const int max_sweeps = sizeof(T) == 4 ? JMAX_SWEEPS_F32 : JMAX_SWEEPS;
+    for (; sweep < max_sweeps && !converged; ++sweep) {
         if (tid == 0) rot_count = 0;
         __syncthreads();
         for (int t = 0; t < n; ++t) {
@@ -129,7 +145,24 @@ k_jacobi(const double* __restrict__ Gin, int64_t ldg, int r, double* __restrict_
         converged = (rot_count == 0);
         __syncthreads();
     }
-    if (!converged && tid == 0) atomicOr(status, ST_JACOBI_NOCONV);
+    // The FP32 pass only aligns a basis for the FP64 stage: no convergence requirement.
+    // FP64: after the cap, only a remaining off-diagonal above 1e-9 of its diagonal scale
+    // (not rounding noise in a numerically zero block) is reported.
+    if (!converged && sizeof(T) == 8) {
+        __shared__ int bad;
+        if (tid == 0) bad = 0;
+        __syncthreads();
+        for (int e = tid; e < r * r; e += nt) {
+            int i = e % r, j = e / r;
+            if (i < j) {
+                T g = SG(G, ld, i, j);
+                if (fabs(g) > (T)1e-9 * sqrt(fabs(SG(G, ld, i, i) * SG(G, ld, j, j))) && fabs(g) > (T)1e-16 * fro)
+                    bad = 1;
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && bad) atomicOr(status, ST_JACOBI_NOCONV);
+    }
     // sort by |lambda| descending (stable by index)
     for (int i = tid; i < r; i += nt) {
         T li = SG(G, ld, i, i);
@@ -148,10 +181,11 @@ template <class T>
 static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {
     TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "jacobi_eigh: r out of range");
     const size_t aux = 2 * (JMAX / 2 + 1) * (sizeof(T) + sizeof(int));
-    size_t smem = (size_t)(r + 1) * r * sizeof(T) + aux;
+    const bool w_in_smem = sizeof(T) == 4;      // FP32: eigenvectors in shared memory as well
+    size_t smem = (size_t)(r + 1) * r * sizeof(T) + aux + (w_in_smem ? (size_t)r * r * sizeof(T) : 0);
     static std::once_flag once;
-    std::call_once(once, [aux] {
-        size_t maxs = (size_t)(JMAX + 1) * JMAX * sizeof(T) + aux;
+    std::call_once(once, [aux, w_in_smem] {
+        size_t maxs = (size_t)(JMAX + 1) * JMAX * sizeof(T) + aux + (w_in_smem ? (size_t)JMAX * JMAX * sizeof(T) : 0);
         cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxs);
     });
     Buf ww(c.pool.get(), (size_t)r * r * sizeof(T));

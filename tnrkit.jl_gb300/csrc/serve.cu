@@ -1,0 +1,241 @@
+// Serving loop: run!() requests admitted by their HBM footprint, kept resident on the
+// device while they iterate, with the steps of every admitted request in flight at once
+// (one CUDA stream per request, a pool of host workers).  A request that arrives while
+// others run is admitted as soon as a slot and enough of the HBM budget free up.
+#include "schemes.cuh"
+
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+
+using namespace tnr;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    uint64_t id = 0;
+    int kind = 0, chi = 0, maxiter = 0;
+    std::vector<int64_t> dims;
+    std::vector<double> data;
+    double btrg_k = -0.5;
+    size_t footprint = 0;
+    Clock::time_point t_submit, t_start, t_done;
+    int status = TNR_OK;
+    std::string err;
+    std::vector<double> norms;
+    bool done = false;
+};
+
+// Device bytes a request needs at bond dimension chi (tensor, intermediates, workspace),
+// from the contraction plans: TRG/BTRG hold chi^4-sized tensors, HOTRG two chi^5
+// intermediates, HOTRG_3D chi^6 tensors plus one sliced chi^8 intermediate of at most
+// 2^31 entries.
+size_t footprint_bytes(int kind, int chi, const std::vector<int64_t>& dims) {
+    double c = chi;
+    double d0 = 1;
+    for (auto d : dims) d0 = std::max<double>(d0, (double)d);
+    c = std::max(c, d0);
+    double entries;
+    switch (kind) {
+        case TNR_TRG:
+        case TNR_BTRG: entries = 12.0 * c * c * c * c + 4.0 * 128 * c * c; break;
+        case TNR_HOTRG: entries = 2.2 * c * c * c * c * c + 12.0 * c * c * c * c; break;
+        default: {
+            double c6 = c * c * c * c * c * c;
+            entries = 10.0 * c6 + 3.0 * std::min(c6 * c * c, 2147483648.0);
+        }
+    }
+    const double bytes = entries * 8.0 + double(size_t(64) << 20);
+    return bytes >= 9.0e18 ? size_t(9000000000000000000ull) : (size_t)bytes;   // saturate, never wrap
+}
+
+}  // namespace
+
+struct tnr_server_s {
+    size_t budget = 0, in_use = 0;
+    int max_active = 1, active = 0, precision = TNR_PREC_F64;
+    uint64_t next_id = 1;
+    bool stopping = false;
+    std::mutex mu;
+    std::condition_variable cv, cv_done;
+    std::deque<Request*> queue;
+    std::map<uint64_t, Request*> all;
+    std::vector<std::thread> workers;
+    int dev = 0;
+
+    void worker() {
+        cudaSetDevice(dev);
+        for (;;) {
+            Request* r = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                // admit the oldest queued request that fits the free budget (first fit)
+                cv.wait(lk, [&] {
+                    if (stopping) return true;
+                    if (active >= max_active) return false;
+                    for (Request* q : queue)
+                        if (q->footprint <= budget - in_use) return true;
+                    return false;
+                });
+                if (stopping && queue.empty()) return;
+                if (stopping) {
+                    // drain: fail what never got admitted
+                    for (Request* q : queue) {
+                        q->status = TNR_ERR_ADMISSION;
+                        q->err = "server stopped";
+                        q->done = true;
+                    }
+                    queue.clear();
+                    cv_done.notify_all();
+                    return;
+                }
+                for (auto it = queue.begin(); it != queue.end(); ++it)
+                    if ((*it)->footprint <= budget - in_use) {
+                        r = *it;
+                        queue.erase(it);
+                        break;
+                    }
+                in_use += r->footprint;
+                ++active;
+            }
+            r->t_start = Clock::now();
+            tnr_handle h = nullptr;
+            tnr_options o;
+            tnr_default_options(&o);
+            o.precision = precision;
+            o.btrg_k = r->btrg_k;
+            int st = tnr_create(&h, r->kind, (int)r->dims.size(), r->dims.data(), r->data.data(), &o);
+            if (st == TNR_OK) {
+                const size_t cap = (size_t)std::max(r->maxiter, 1) + 1;
+                r->norms.resize(cap);
+                size_t n = 0;
+                st = tnr_run(h, r->chi, r->maxiter, 1, r->norms.data(), cap, &n);
+                r->norms.resize(n);
+            }
+            if (st != TNR_OK) {
+                char buf[512];
+                tnr_last_error(h, buf, sizeof buf);
+                r->err = buf;
+            }
+            if (h) tnr_destroy(h);
+            r->status = st;
+            r->t_done = Clock::now();
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                in_use -= r->footprint;
+                --active;
+                r->done = true;
+            }
+            cv.notify_all();
+            cv_done.notify_all();
+        }
+    }
+};
+
+extern "C" {
+
+int tnr_server_create(tnr_server* out, size_t hbm_budget_bytes, int max_active, int precision) {
+    if (!out || max_active < 1 || hbm_budget_bytes == 0) return TNR_ERR_INVALID_ARG;
+    if (precision != TNR_PREC_F64 && precision != TNR_PREC_SPLIT) return TNR_ERR_INVALID_ARG;
+    tnr_server s = new (std::nothrow) tnr_server_s();
+    if (!s) return TNR_ERR_OOM;
+    s->budget = hbm_budget_bytes;
+    s->max_active = max_active;
+    s->precision = precision;
+    cudaGetDevice(&s->dev);
+    for (int i = 0; i < max_active; ++i) s->workers.emplace_back([s] { s->worker(); });
+    *out = s;
+    return TNR_OK;
+}
+
+int tnr_server_submit(tnr_server s, int kind, int nlegs, const int64_t* dims, const double* data, int chi,
+                      int maxiter, double btrg_k, uint64_t* id_out) {
+    if (!s || !dims || !data || !id_out || chi < 1) return TNR_ERR_INVALID_ARG;
+    if (kind < TNR_TRG || kind > TNR_HOTRG_3D) return TNR_ERR_INVALID_ARG;
+    if (nlegs != (kind == TNR_HOTRG_3D ? 6 : 4)) return TNR_ERR_INVALID_ARG;
+    Request* r = new (std::nothrow) Request();
+    if (!r) return TNR_ERR_OOM;
+    r->kind = kind;
+    r->chi = chi;
+    r->maxiter = maxiter;
+    r->btrg_k = btrg_k;
+    r->dims.assign(dims, dims + nlegs);
+    int64_t total = 1;
+    for (int l = 0; l < nlegs; ++l) {
+        if (dims[l] < 1) {
+            delete r;
+            return TNR_ERR_INVALID_ARG;
+        }
+        total *= dims[l];
+    }
+    r->data.assign(data, data + total);
+    r->footprint = footprint_bytes(kind, chi, r->dims);
+    r->t_submit = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (r->footprint > s->budget) {
+        // can never fit: refused at submission (admission control)
+        delete r;
+        return TNR_ERR_ADMISSION;
+    }
+    r->id = s->next_id++;
+    s->all[r->id] = r;
+    s->queue.push_back(r);
+    *id_out = r->id;
+    s->cv.notify_all();
+    return TNR_OK;
+}
+
+int tnr_server_poll(tnr_server s, uint64_t id, int wait, int* done, double* norms, size_t cap, size_t* n_out,
+                    double* latency_ms, double* queue_ms) {
+    if (!s || !done) return TNR_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return TNR_ERR_INVALID_ARG;
+    Request* r = it->second;
+    if (wait) s->cv_done.wait(lk, [&] { return r->done; });
+    *done = r->done ? 1 : 0;
+    if (!r->done) return TNR_OK;
+    if (n_out) *n_out = r->norms.size();
+    if (norms) {
+        if (cap < r->norms.size()) return TNR_ERR_INVALID_ARG;
+        std::memcpy(norms, r->norms.data(), r->norms.size() * sizeof(double));
+    }
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    if (queue_ms) *queue_ms = std::chrono::duration<double, std::milli>(r->t_start - r->t_submit).count();
+    return r->status;
+}
+
+int tnr_server_stats(tnr_server s, int* active, int* queued, size_t* bytes_in_use) {
+    if (!s) return TNR_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (active) *active = s->active;
+    if (queued) *queued = (int)s->queue.size();
+    if (bytes_in_use) *bytes_in_use = s->in_use;
+    return TNR_OK;
+}
+
+int tnr_server_destroy(tnr_server s) {
+    if (!s) return TNR_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+    }
+    s->cv.notify_all();
+    for (auto& t : s->workers) t.join();
+    for (auto& kv : s->all) delete kv.second;
+    delete s;
+    return TNR_OK;
+}
+
+size_t tnr_footprint_bytes(int kind, int chi, int nlegs, const int64_t* dims) {
+    std::vector<int64_t> d(dims, dims + nlegs);
+    return footprint_bytes(kind, chi, d);
+}
+
+}  // extern "C"

@@ -150,7 +150,10 @@ static bool debug_on() {
     return on == 1;
 }
 
-static double target_angle(Ctx& c) { return c.precision == TNR_PREC_F64 ? 1e-13 : 1e-9; }
+#ifndef TNR_TARGET_F64
+#define TNR_TARGET_F64 1e-15
+#endif
+static double target_angle(Ctx& c) { return c.precision == TNR_PREC_F64 ? TNR_TARGET_F64 : 1e-9; }
 
 TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt) {
     TsvdOut out;
