@@ -180,6 +180,14 @@ int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t 
                    const double* B, int64_t ldb, int64_t strideB,
                    double* C, int64_t ldc, int64_t strideC, int batch);
 
+/* Device time of one batched GEMM of that shape on seeded N(0,1) device operands
+ * (contiguous column-major, strides m*k, k*n, m*n): *ms_out = the CUDA-event time
+ * of `reps` back-to-back calls / reps, after one untimed call.  For the split
+ * precision the time includes the FP64 -> BF16 plane pass.  No reference
+ * counterpart (kernel measurements). */
+int tnr_gemm_time(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k, int batch, int reps,
+                  double* ms_out);
+
 /* ---- allocation-free split GEMM ------------------------------------------ */
 /* No counterpart in the reference.  C = alpha * op(A) op(B) + beta * C on device
  * pointers (column-major FP64), computed by the split 3xBF16 tensor-core kernel

@@ -189,3 +189,44 @@ def test_split_gemm_tc(tnr, m, n, k, ta, tb, batch):
     assert err < 6e-8 * np.sqrt(k), err
     f64 = tnr.debug_gemm(A, B, ta, tb, tnr.PREC_F64)
     assert np.linalg.norm(f64 - ref) / np.linalg.norm(ref) < 1e-14
+
+
+@pytest.mark.parametrize("cls,chi", [("BTRG", 24), ("TRG", 16)])
+@pytest.mark.parametrize("precision", ["f64", "split"])
+def test_lockstep_group_equals_single(tnr, cls, chi, precision):
+    """Equal-chi instances in one run_batch step in lockstep (one batched launch per kernel);
+    each must match its own single run.  FP64: every norm to 1e-11 (the group iterates as
+    long as its slowest member needs).  Split precision: the free energy to 1e-7, its
+    accuracy contract; its norms only to FP32 level, since the products of the truncated
+    SVD carry errors of ~1e-7 sigma_1 and the late, small singular directions move with
+    the random start.  The betas are well conditioned: the oracle's norms move by at most
+    2e-13 under a 1e-14 relative perturbation of the input tensor (at beta = 0.33 they move
+    by 3e-7: a near-tie sits at the cut, where two runs with different random starts may
+    keep different vectors)."""
+    prec = tnr.PREC_F64 if precision == "f64" else tnr.PREC_SPLIT
+    betas = [0.40, 0.42, 0.44, 0.46, 0.47]
+    group = [getattr(tnr, cls)(tnr.classical_ising("Trivial", b), precision=prec) for b in betas]
+    out = tnr.run_batch(group, [chi] * len(betas), [12] * len(betas))
+    for b, d, g in zip(betas, out, group):
+        s = getattr(tnr, cls)(tnr.classical_ising("Trivial", b), precision=prec)
+        ref = tnr.run(s, tnr.truncrank(chi), tnr.maxiter(12))
+        if precision == "f64":
+            np.testing.assert_allclose(d, ref, rtol=1e-11)
+        else:
+            assert tnr.free_energy(d, b) == pytest.approx(tnr.free_energy(ref, b), rel=1e-7)
+            np.testing.assert_allclose(d, ref, rtol=1e-3)
+        # the member is left in its final state, like after run!
+        assert g.T.shape == s.T.shape
+
+
+@pytest.mark.parametrize("cls,chi,beta", [("BTRG", 24, 0.53), ("BTRG", 24, 0.57), ("TRG", 16, 0.53),
+                                          ("TRG", 24, 0.6)])
+def test_ordered_phase_f64(tnr, oracle, cls, chi, beta):
+    """Ordered phase (beta > beta_c): the kept spectrum falls to ~1e-12 sigma_1, so the
+    subspace iteration must stay backward stable in FP64 for the small directions
+    (shifted CholeskyQR3); 12 steps against the oracle at 1e-10."""
+    s = getattr(tnr, cls)(tnr.classical_ising("Trivial", beta))
+    got = tnr.run(s, tnr.truncrank(chi), tnr.maxiter(12))
+    ref = oracle.run(getattr(oracle, cls)(oracle.classical_ising(beta, "Trivial")), oracle.truncrank(chi),
+                     oracle.maxiter(12))
+    np.testing.assert_allclose(got, ref, rtol=1e-10)

@@ -35,7 +35,7 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_free_energy", "tnr_get_tensor", "tnr_singular_values", "tnr_truncation_errors", "tnr_btrg_bonds",
            "tnr_device_bytes", "tnr_destroy", "tnr_last_error", "tnr_status_string", "tnr_timer_start",
            "tnr_timer_stop", "tnr_run_batch", "tnr_device_info", "tnr_version", "tnr_kernel_launches",
-           "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm",
+           "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm", "tnr_gemm_time",
            "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_poll",
            "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes"]
 
@@ -90,6 +90,7 @@ def lib():
         "tnr_profile_read": (I, [I, C.POINTER(C.c_uint64), pd, pd]),
         "tnr_debug_gemm": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, pd, C.c_int64, C.c_int64, pd, C.c_int64,
                                C.c_int64, pd, C.c_int64, C.c_int64, I]),
+        "tnr_gemm_time": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, I, I, pd]),
         "tnr_gemm_split_noalloc": (I, [I, I, C.c_int64, C.c_int64, C.c_int64, D, P, C.c_int64, P, C.c_int64, D, P,
                                        C.c_int64, P, C.c_char_p, Z]),
         "tnr_server_create": (I, [C.POINTER(P), Z, I, I]),
@@ -436,6 +437,13 @@ def debug_gemm(A, B, ta=False, tb=False, precision=PREC_SPLIT):
     _check(st)
     out = np.transpose(Cf, (0, 2, 1))
     return out if A.ndim == 3 else out[0]
+
+
+def gemm_time(m, n, k, batch=1, ta=False, tb=False, precision=PREC_SPLIT, reps=5):
+    """Average device milliseconds of one batched GEMM of this shape on seeded device operands."""
+    ms = C.c_double()
+    _check(lib().tnr_gemm_time(precision, int(ta), int(tb), m, n, k, batch, reps, C.byref(ms)))
+    return ms.value
 
 
 def device_info():

@@ -2,9 +2,11 @@
 // exceptions and returns a status code; nothing aborts the process.
 #include "schemes.cuh"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <thread>
 
@@ -304,21 +306,57 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
         size_t need = (size_t)std::max(maxiter[i], 1) + (finalize_beginning ? 1 : 0);
         if (need > stride) return fail(nullptr, TNR_ERR_INVALID_ARG, "stride too small for run!");
     }
+    // lockstep groups: fresh TRG/BTRG schemes with equal kind, precision, k, dims, chi, maxiter
+    struct Task {
+        std::vector<int> idx;
+        std::unique_ptr<Ctx> ctx;   // group context (null: run the single handle on its own)
+    };
+    std::vector<Task> tasks;
+    {
+        std::map<std::string, int> key_to_task;
+        for (int i = 0; i < n; ++i) {
+            Scheme& sc = hs[i]->s;
+            bool groupable = (sc.kind == TNR_TRG || sc.kind == TNR_BTRG) && sc.steps == 0;
+            std::string key;
+            if (groupable) {
+                key = std::to_string(sc.kind) + "/" + std::to_string(sc.ctx->precision) + "/" +
+                      std::to_string(sc.btrg_k) + "/" + std::to_string(chi[i]) + "/" + std::to_string(maxiter[i]);
+                for (int l = 0; l < sc.T.rank; ++l) key += "/" + std::to_string(sc.T.d[l]);
+            }
+            auto it = groupable ? key_to_task.find(key) : key_to_task.end();
+            if (it == key_to_task.end()) {
+                tasks.push_back(Task());
+                tasks.back().idx.push_back(i);
+                if (groupable) key_to_task[key] = (int)tasks.size() - 1;
+            } else {
+                tasks[it->second].idx.push_back(i);
+            }
+        }
+    }
+    int st0 = guarded(nullptr, [&] {
+        for (auto& t : tasks)
+            if (t.idx.size() > 1)
+                t.ctx.reset(new Ctx(nullptr, hs[t.idx[0]]->s.ctx->precision, hs[t.idx[0]]->s.ctx->seed));
+    });
+    if (st0 != TNR_OK) return st0;
+    // largest groups first
+    std::stable_sort(tasks.begin(), tasks.end(), [](const Task& a, const Task& b) { return a.idx.size() > b.idx.size(); });
+    auto task_stream = [&](const Task& t) { return t.ctx ? t.ctx->stream : hs[t.idx[0]]->s.ctx->stream; };
     cudaStream_t ts = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<cudaEvent_t> done;
-    int st0 = guarded(nullptr, [&] {
+    st0 = guarded(nullptr, [&] {
         if (device_ms_out) {
             TNR_CUDA(cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking));
             TNR_CUDA(cudaEventCreate(&e0));
             TNR_CUDA(cudaEventCreate(&e1));
             TNR_CUDA(cudaEventRecord(e0, ts));
-            for (int i = 0; i < n; ++i) TNR_CUDA(cudaStreamWaitEvent(hs[i]->s.ctx->stream, e0, 0));
+            for (auto& t : tasks) TNR_CUDA(cudaStreamWaitEvent(task_stream(t), e0, 0));
         }
     });
     if (st0 != TNR_OK) return st0;
-    // one host worker per concurrent instance; each handle runs on its own stream
-    const int workers = std::min(n, 32);
+    // one host worker per concurrent task; a task is a lockstep group or a single handle
+    const int workers = std::min((int)tasks.size(), 32);
     std::vector<int> status(n, TNR_OK);
     std::atomic<int> next{0};
     int dev = 0;
@@ -327,13 +365,33 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
     auto work = [&] {
         cudaSetDevice(dev);
         for (;;) {
-            int i = next.fetch_add(1);
-            if (i >= n) break;
-            status[i] = tnr_run(hs[i], chi[i], maxiter[i], finalize_beginning, norms_out + (size_t)i * stride, stride,
-                                n_out + i);
+            int ti = next.fetch_add(1);
+            if (ti >= (int)tasks.size()) break;
+            Task& t = tasks[ti];
+            if (!t.ctx) {
+                int i = t.idx[0];
+                status[i] = tnr_run(hs[i], chi[i], maxiter[i], finalize_beginning, norms_out + (size_t)i * stride,
+                                    stride, n_out + i);
+            } else {
+                std::vector<Scheme*> mem;
+                for (int i : t.idx) mem.push_back(&hs[i]->s);
+                std::vector<std::vector<double>> nv;
+                int i0 = t.idx[0];
+                int st = guarded(hs[i0], [&] { run_group(*t.ctx, mem, chi[i0], maxiter[i0], finalize_beginning != 0, nv); });
+                for (size_t j = 0; j < t.idx.size(); ++j) {
+                    int i = t.idx[j];
+                    status[i] = st;
+                    if (st == TNR_OK) {
+                        std::memcpy(norms_out + (size_t)i * stride, nv[j].data(), nv[j].size() * sizeof(double));
+                        n_out[i] = nv[j].size();
+                    } else {
+                        hs[i]->s.err = hs[i0]->s.err;
+                    }
+                }
+            }
+            const double lat = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             if (latency_ms_out)
-                latency_ms_out[i] =
-                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+                for (int i : t.idx) latency_ms_out[i] = lat;
         }
     };
     std::vector<std::thread> th;
@@ -341,10 +399,10 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
     for (auto& t : th) t.join();
     int st1 = guarded(nullptr, [&] {
         if (device_ms_out) {
-            for (int i = 0; i < n; ++i) {
+            for (auto& t : tasks) {
                 cudaEvent_t e;
                 TNR_CUDA(cudaEventCreate(&e));
-                TNR_CUDA(cudaEventRecord(e, hs[i]->s.ctx->stream));
+                TNR_CUDA(cudaEventRecord(e, task_stream(t)));
                 TNR_CUDA(cudaStreamWaitEvent(ts, e, 0));
                 done.push_back(e);
             }
@@ -409,6 +467,49 @@ int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t 
         TNR_CUDA(cudaMemcpyAsync(C, dC.d(), eC * 8, cudaMemcpyDeviceToHost, c.stream));
         int st = c.read_status_and_clear();
         TNR_REQUIRE(st == 0, TNR_ERR_CUDA, "kernel status word " + std::to_string(st));
+    });
+}
+
+int tnr_gemm_time(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k, int batch, int reps,
+                  double* ms_out) {
+    if (m < 1 || n < 1 || k < 1 || batch < 1 || reps < 1 || !ms_out)
+        return fail(nullptr, TNR_ERR_INVALID_ARG, "bad gemm_time arguments");
+    if (precision != TNR_PREC_F64 && precision != TNR_PREC_SPLIT)
+        return fail(nullptr, TNR_ERR_INVALID_ARG, "unknown precision");
+    return guarded(nullptr, [&] {
+        require_device();
+        Ctx c(nullptr, precision, 0);
+        const int64_t sA = m * k, sB = k * n, sC = m * n;
+        Buf dA(c.pool.get(), (size_t)sA * batch * 8), dB(c.pool.get(), (size_t)sB * batch * 8),
+            dC(c.pool.get(), (size_t)sC * batch * 8);
+        fill_normal(c, dA.d(), sA * batch, 1);
+        fill_normal(c, dB.d(), sB * batch, 2);
+        Batch2 bt;
+        bt.n1 = batch; bt.sA1 = sA; bt.sB1 = sB; bt.sC1 = sC;
+        const int64_t lda = ta ? k : m, ldb = tb ? n : k;
+        auto once = [&] {
+            if (precision == TNR_PREC_SPLIT) {
+                bool ran = gemm_split_tc(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), m, bt);
+                TNR_REQUIRE(ran, TNR_ERR_UNSUPPORTED, "split kernel declined this shape");
+            } else {
+                gemm_f64(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), m, bt);
+            }
+        };
+        once();   // warm-up (tensor maps, function attributes)
+        cudaEvent_t e0, e1;
+        TNR_CUDA(cudaEventCreate(&e0));
+        TNR_CUDA(cudaEventCreate(&e1));
+        TNR_CUDA(cudaEventRecord(e0, c.stream));
+        for (int i = 0; i < reps; ++i) once();
+        TNR_CUDA(cudaEventRecord(e1, c.stream));
+        TNR_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        TNR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        int st = c.read_status_and_clear();
+        TNR_REQUIRE(st == 0, TNR_ERR_CUDA, "kernel status word " + std::to_string(st));
+        *ms_out = (double)ms / reps;
     });
 }
 

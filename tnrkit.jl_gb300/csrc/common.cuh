@@ -1,6 +1,7 @@
 // Shared declarations of the GB300 coarse-graining engine (internal).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstddef>
@@ -199,15 +200,51 @@ bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, do
                    const double* A, int64_t lda, const double* B, int64_t ldb,
                    double beta, double* C, int64_t ldc, const Batch2& bt);
 
+// BF16 planes of one FP64 A operand, split once and reused by every product with it
+// (the matrix of a truncated SVD meets many thin right-hand sides); inactive unless the
+// context runs the split precision and the products qualify for the tcgen05 kernel.
+struct SplitA {
+    bool active = false;
+    bool batched = false;
+    int nb = 0;
+    int64_t m = 0, k = 0, Kp = 0;
+    Buf planes;
+    CUtensorMap map;
+};
+// prepare op(A) (m x k; batch from bt.n1/bt.sA1) for products with about n_hint columns
+void split_a_prepare(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int64_t m, int64_t k,
+                     int64_t n_hint, const Batch2& bt);
+// gemm_bulk with a prepared A (falls back to gemm_bulk when P is inactive)
+void gemm_bulk_a(Ctx& c, const SplitA& P, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
+                 const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                 const Batch2& bt);
+bool gemm_split_tc_a(Ctx& c, const SplitA& P, bool tb, int64_t n, const double* B, int64_t ldb, double alpha,
+                     double beta, double* C, int64_t ldc, const Batch2& bt);
+bool split_a_build(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int64_t m, int64_t k,
+                   const Batch2& bt);
+
 // symmetric eigendecomposition of an r x r matrix (r <= 128), eigenvalues sorted by |lambda| desc
-void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam);
+// batch > 1: `batch` matrices strideG apart; W (r x r) and lam (r) outputs packed per matrix
+void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch = 1,
+                 int64_t strideG = 0);
 // G <- Cholesky factor inverse: on exit Linv (lower) with (G + shift I) = L L^T; returns via status
-void chol_inv(Ctx& c, double* G, int r, double shift);
+void chol_inv(Ctx& c, double* G, int r, double shift, int batch = 1);
 // FP32 versions (one SM runs FP32 at 64x its FP64 rate): results returned in FP64 buffers
-void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam);
-void chol_inv_f32(Ctx& c, double* G, int r, double shift);
-void add_identity(Ctx& c, double* X, int r, double alpha);
-void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r);
+void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch = 1,
+                     int64_t strideG = 0);
+void chol_inv_f32(Ctx& c, double* G, int r, double shift, int batch = 1);
+void add_identity(Ctx& c, double* X, int r, double alpha, int batch = 1);
+void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r, int batch = 1);
+// X (k x n_total, ld k) rows scaled per batch: X[i, j] *= f(s[(j / n_per) * k + i])
+void row_scale_batched(Ctx& c, double* X, int64_t k, int64_t n_total, const double* s, int mode, int64_t n_per);
+// T (per = elements per instance, batch instances): T[e] *= v[b * dim + (e % per / stride) % dim]
+void scale_leg_batched(Ctx& c, double* T, int64_t per, int batch, int64_t stride, int64_t dim, const double* v);
+// out[b] (k x n) = transpose of the leading k columns of in[b] (n x p, ld n)
+void transpose_lead(Ctx& c, const double* in, int64_t n, int64_t p, int k, int batch, double* out);
+// trace norms of a batch: out[b] = |trace(T_b)|; then T_b /= out[b]
+void trace2d_batched(Ctx& c, const double* T, const int64_t* d, int batch, const double* S1, const double* S2,
+                     double* out);
+void scale_batched(Ctx& c, double* T, int64_t per, int batch, const double* norms);
 void decouple_rotation(Ctx& c, const double* G, int r, int kb, double* P);
 void diag_copy(Ctx& c, const double* G, int r, int kb, double* lam);
 void diag_to_host(Ctx& c, const double* G, int r, double* host);
@@ -215,7 +252,7 @@ void fill_normal(Ctx& c, double* x, int64_t n, uint64_t seed);
 void col_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);
 void row_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);
 void col_norms(Ctx& c, const double* X, int64_t m, int64_t n, int64_t ldx, double* out);
-void gram_unit_diag(Ctx& c, double* G, int r, double* dscale);
+void gram_unit_diag(Ctx& c, double* G, int r, double* dscale, int batch = 1);
 void sum_squares(Ctx& c, const double* x, int64_t n, double* out);
 void scale_inplace(Ctx& c, double* x, int64_t n, const double* inv_scale_ptr);
 void fill_identity(Ctx& c, double* x, int64_t m, int64_t n);
@@ -244,14 +281,19 @@ struct TsvdOut {
 TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt);
 // symmetric M (n x n): U (n x k) eigenvectors of the k largest |eigenvalues|, lam (k)
 TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lam);
+// B stacked m x n matrices (stride m*n), decomposed in lockstep: U [B][m x k], s [B][k], Vt [B][k x n]
+std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U, double* s,
+                                  double* Vt);
 
 // ---------------------------------------------------------------------------
 // generic pairwise contraction (permute + GEMM + permute)
 // ---------------------------------------------------------------------------
 // labels are small ints; out_labels gives the output leg order
+// batch > 1: A, B and the result carry `batch` instances (an implicit trailing leg); the
+// dims / labels name the per-instance legs and the result's dims end with `batch`
 DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::vector<int>& lA,
             const double* B, const std::vector<int64_t>& dB, const std::vector<int>& lB,
-            const std::vector<int>& lOut, bool bulk = true);
+            const std::vector<int>& lOut, bool bulk = true, int batch = 1);
 inline DT contract(Ctx& c, const DT& A, const std::vector<int>& lA, const DT& B,
                    const std::vector<int>& lB, const std::vector<int>& lOut, bool bulk = true) {
     return contract(c, A.p(), A.dims(), lA, B.p(), B.dims(), lB, lOut, bulk);

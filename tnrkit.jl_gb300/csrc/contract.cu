@@ -33,7 +33,8 @@ std::vector<int> concat(const std::vector<int>& a, const std::vector<int>& b) {
 
 DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::vector<int>& lA,
             const double* B, const std::vector<int64_t>& dB, const std::vector<int>& lB,
-            const std::vector<int>& lOut, bool bulk) {
+            const std::vector<int>& lOut, bool bulk, int batch) {
+    TNR_REQUIRE(batch >= 1, TNR_ERR_INVALID_ARG, "contract: batch < 1");
     TNR_REQUIRE(dA.size() == lA.size() && dB.size() == lB.size(), TNR_ERR_INVALID_ARG, "contract: rank/labels");
     std::vector<int> K, FA, FB;
     for (int x : lA) {
@@ -92,36 +93,51 @@ DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::
     Buf bufA, bufB;
     const double* pa = A;
     const double* pb = B;
+    // a batch is a trailing leg that every operand and the output carry unchanged
+    auto permute_b = [&](const double* in, const std::vector<int64_t>& d, std::vector<int> perm, double* out) {
+        std::vector<int64_t> dd(d);
+        if (batch > 1) {
+            perm.push_back((int)d.size());
+            dd.push_back(batch);
+        }
+        permute(c, in, dd.data(), (int)dd.size(), perm.data(), out);
+    };
     if (best.permA) {
         std::vector<int> target = concat(best.FA, best.K);
         std::vector<int> perm(target.size());
         for (size_t i = 0; i < target.size(); ++i) perm[i] = idx_of(lA, target[i]);
-        bufA = Buf(pool, (size_t)sizeA * sizeof(double));
-        permute(c, A, dA.data(), (int)dA.size(), perm.data(), bufA.d());
+        bufA = Buf(pool, (size_t)sizeA * batch * sizeof(double));
+        permute_b(A, dA, perm, bufA.d());
         pa = bufA.d();
     }
     if (best.permB) {
         std::vector<int> target = concat(best.K, best.FB);
         std::vector<int> perm(target.size());
         for (size_t i = 0; i < target.size(); ++i) perm[i] = idx_of(lB, target[i]);
-        bufB = Buf(pool, (size_t)sizeB * sizeof(double));
-        permute(c, B, dB.data(), (int)dB.size(), perm.data(), bufB.d());
+        bufB = Buf(pool, (size_t)sizeB * batch * sizeof(double));
+        permute_b(B, dB, perm, bufB.d());
         pb = bufB.d();
     }
     // result in natural order
     std::vector<int> nat = best.swap ? concat(best.FB, best.FA) : concat(best.FA, best.FB);
     std::vector<int64_t> natd;
     for (int x : nat) natd.push_back(dim_of(x));
+    if (batch > 1) natd.push_back(batch);
     DT Cn = make_dt(pool, natd);
     const int64_t lda = best.ta ? kk : m;   // A matrix: [FA|K] (m x kk) or [K|FA] (kk x m)
     const int64_t ldb = best.tb ? n : kk;   // B matrix: [K|FB] (kk x n) or [FB|K] (n x kk)
-    auto run = [&](bool ta, bool tb, int64_t M_, int64_t N_, const double* X, int64_t ldx, const double* Yp,
-                   int64_t ldy) {
-        if (bulk) gemm_bulk(c, ta, tb, M_, N_, kk, 1.0, X, ldx, 0, Yp, ldy, 0, 0.0, Cn.p(), M_, 0);
-        else gemm_f64(c, ta, tb, M_, N_, kk, 1.0, X, ldx, 0, Yp, ldy, 0, 0.0, Cn.p(), M_, 0);
+    auto run = [&](bool ta, bool tb, int64_t M_, int64_t N_, const double* X, int64_t ldx, int64_t sX,
+                   const double* Yp, int64_t ldy, int64_t sY) {
+        Batch2 bt;
+        bt.n1 = batch;
+        bt.sA1 = sX;
+        bt.sB1 = sY;
+        bt.sC1 = M_ * N_;
+        if (bulk) gemm_bulk(c, ta, tb, M_, N_, kk, 1.0, X, ldx, Yp, ldy, 0.0, Cn.p(), M_, bt);
+        else gemm_f64(c, ta, tb, M_, N_, kk, 1.0, X, ldx, Yp, ldy, 0.0, Cn.p(), M_, bt);
     };
-    if (!best.swap) run(best.ta, best.tb, m, n, pa, lda, pb, ldb);
-    else run(!best.tb, !best.ta, n, m, pb, ldb, pa, lda);   // C^T = op(B)^T op(A)^T
+    if (!best.swap) run(best.ta, best.tb, m, n, pa, lda, sizeA, pb, ldb, sizeB);
+    else run(!best.tb, !best.ta, n, m, pb, ldb, sizeB, pa, lda, sizeA);   // C^T = op(B)^T op(A)^T
     bufA.release();
     bufB.release();
     if (!best.permOut) {
@@ -130,6 +146,7 @@ DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::
     }
     std::vector<int> perm(lOut.size());
     for (size_t i = 0; i < lOut.size(); ++i) perm[i] = idx_of(nat, lOut[i]);
+    if (batch > 1) perm.push_back((int)lOut.size());
     return permuted(c, Cn, perm);
 }
 

@@ -404,6 +404,8 @@ void col_norms(Ctx& c, const double* X, int64_t m, int64_t n, int64_t ldx, doubl
 // G <- D^{-1} G D^{-1} with D = sqrt(diag(G)); dscale <- 1/sqrt(diag) (0 for a zero column)
 __global__ void k_gram_unit_diag(double* G, int r, double* dscale) {
     __shared__ double inv[256];
+    G += (int64_t)blockIdx.x * r * r;     // one CTA per matrix of a batch
+    dscale += (int64_t)blockIdx.x * r;
     for (int i = threadIdx.x; i < r; i += blockDim.x) {
         double v = G[i + (int64_t)i * r];
         inv[i] = v > 0.0 ? rsqrt(v) : 0.0;
@@ -417,9 +419,9 @@ __global__ void k_gram_unit_diag(double* G, int r, double* dscale) {
         G[e] = v;
     }
 }
-void gram_unit_diag(Ctx& c, double* G, int r, double* dscale) {
+void gram_unit_diag(Ctx& c, double* G, int r, double* dscale, int batch) {
     TNR_REQUIRE(r <= 256, TNR_ERR_UNSUPPORTED, "gram_unit_diag r > 256");
-    k_gram_unit_diag<<<1, 256, 0, c.stream>>>(G, r, dscale);
+    k_gram_unit_diag<<<batch, 256, 0, c.stream>>>(G, r, dscale);
     check_launch("gram_unit_diag");
 }
 
@@ -485,22 +487,24 @@ void fill_identity(Ctx& c, double* x, int64_t m, int64_t n) {
 // X += alpha * I (r x r)
 __global__ void k_add_identity(double* X, int r, double alpha) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    X += (int64_t)blockIdx.y * r * r;
     if (i < r) X[i + (int64_t)i * r] += alpha;
 }
-void add_identity(Ctx& c, double* X, int r, double alpha) {
-    k_add_identity<<<(r + 127) / 128, 128, 0, c.stream>>>(X, r, alpha);
+void add_identity(Ctx& c, double* X, int r, double alpha, int batch) {
+    k_add_identity<<<dim3((r + 127) / 128, batch), 128, 0, c.stream>>>(X, r, alpha);
     check_launch("add_identity");
 }
 
 // C = I - E/2 + 3/8 E^2 (C may alias E)
-__global__ void k_polar_coeff(const double* E, const double* E2, double* C, int r) {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < r * r; e += gridDim.x * blockDim.x) {
-        int i = e % r, j = e / r;
+__global__ void k_polar_coeff(const double* E, const double* E2, double* C, int r, int64_t total) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = e % r, j = (e / r) % r;
         C[e] = (i == j ? 1.0 : 0.0) - 0.5 * E[e] + 0.375 * E2[e];
     }
 }
-void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r) {
-    k_polar_coeff<<<(r * r + 255) / 256, 256, 0, c.stream>>>(E, E2, C, r);
+void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r, int batch) {
+    const int64_t total = (int64_t)r * r * batch;
+    k_polar_coeff<<<grid_for(total, 256), 256, 0, c.stream>>>(E, E2, C, r, total);
     check_launch("polar_coeff");
 }
 
@@ -544,6 +548,89 @@ void diag_to_host(Ctx& c, const double* G, int r, double* host) {
     TNR_CUDA(cudaMemcpy2DAsync(host, sizeof(double), G, (size_t)(r + 1) * sizeof(double), sizeof(double), r,
                                cudaMemcpyDeviceToHost, c.stream));
     c.sync();
+}
+
+__global__ void k_row_scale_batched(double* X, int64_t k, int64_t n_total, const double* s, int mode, int64_t n_per) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * n_total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = e % k, j = e / k;
+        X[e] *= scale_of(s[(j / n_per) * k + i], mode);
+    }
+}
+void row_scale_batched(Ctx& c, double* X, int64_t k, int64_t n_total, const double* s, int mode, int64_t n_per) {
+    if (k * n_total == 0) return;
+    k_row_scale_batched<<<grid_for(k * n_total, 256), 256, 0, c.stream>>>(X, k, n_total, s, mode, n_per);
+    check_launch("row_scale_batched");
+}
+
+__global__ void k_scale_leg_batched(double* T, int64_t per, int64_t total, int64_t stride, int64_t dim,
+                                    const double* v) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+        T[e] *= v[(e / per) * dim + ((e % per) / stride) % dim];
+}
+void scale_leg_batched(Ctx& c, double* T, int64_t per, int batch, int64_t stride, int64_t dim, const double* v) {
+    const int64_t total = per * batch;
+    if (!total) return;
+    k_scale_leg_batched<<<grid_for(total, 256), 256, 0, c.stream>>>(T, per, total, stride, dim, v);
+    check_launch("scale_leg_batched");
+}
+
+__global__ void k_transpose_lead(const double* in, int64_t n, int64_t p, int k, int64_t total, double* out) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        // out[b][i + k * j] = in[b][j + n * i],  i < k, j < n
+        int64_t b = e / (k * n), rem = e % (k * n);
+        int64_t i = rem % k, j = rem / k;
+        out[e] = in[b * n * p + j + n * i];
+    }
+}
+void transpose_lead(Ctx& c, const double* in, int64_t n, int64_t p, int k, int batch, double* out) {
+    const int64_t total = (int64_t)k * n * batch;
+    if (!total) return;
+    k_transpose_lead<<<grid_for(total, 256), 256, 0, c.stream>>>(in, n, p, k, total, out);
+    check_launch("transpose_lead");
+}
+
+// |sum_{a,b} T_b[a,b,b,a] w1[b] w2[a]| per instance (one CTA per instance)
+__global__ void k_trace2d_batched(const double* T, int64_t d1, int64_t d2, int64_t d3, int64_t per,
+                                  const double* S1, const double* S2, double* out) {
+    __shared__ double sh[32];
+    const int b = blockIdx.x;
+    T += (int64_t)b * per;
+    if (S1) S1 += (int64_t)b * d2;
+    if (S2) S2 += (int64_t)b * d1;
+    double acc = 0.0;
+    for (int64_t e = threadIdx.x; e < d1 * d2; e += blockDim.x) {
+        int64_t a = e % d1, bb = e / d1;
+        double v = T[a + d1 * (bb + d2 * (bb + d3 * a))];
+        if (S1) v *= S1[bb];
+        if (S2) v *= S2[a];
+        acc += v;
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) out[b] = fabs(acc);
+    }
+}
+void trace2d_batched(Ctx& c, const double* T, const int64_t* d, int batch, const double* S1, const double* S2,
+                     double* out) {
+    TNR_REQUIRE(d[0] == d[3] && d[1] == d[2], TNR_ERR_INVALID_ARG, "trace T[1 2;2 1] needs d1==d4, d2==d3");
+    k_trace2d_batched<<<batch, 256, 0, c.stream>>>(T, d[0], d[1], d[2], d[0] * d[1] * d[2] * d[3], S1, S2, out);
+    check_launch("trace2d_batched");
+}
+
+__global__ void k_scale_batched(double* T, int64_t per, int64_t total, const double* norms) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+        T[e] /= fabs(norms[e / per]);
+}
+void scale_batched(Ctx& c, double* T, int64_t per, int batch, const double* norms) {
+    const int64_t total = per * batch;
+    if (!total) return;
+    k_scale_batched<<<grid_for(total, 256), 256, 0, c.stream>>>(T, per, total, norms);
+    check_launch("scale_batched");
 }
 
 void copy_f64(Ctx& c, double* dst, const double* src, int64_t n) {

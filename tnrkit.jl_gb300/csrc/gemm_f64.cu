@@ -143,13 +143,34 @@ void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double 
     gemm_f64(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
 }
 
+#ifndef TNR_SPLIT_MIN_MNK
+#define TNR_SPLIT_MIN_MNK 4194304.0   // m n k of one instance below which a bulk product stays FP64
+#endif
+
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
-    if (c.precision == TNR_PREC_SPLIT && gemm_split_tc(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt))
+    // products of small instances stay on the FP64 path: the early coarse-graining steps,
+    // whose norms carry the largest weights in the free energy, are all small
+    if (c.precision == TNR_PREC_SPLIT && (double)m * n * k >= TNR_SPLIT_MIN_MNK &&
+        gemm_split_tc(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt))
         return;
     c.bulk_call = true;
     gemm_f64(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
     c.bulk_call = false;
+}
+
+void split_a_prepare(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int64_t m, int64_t k,
+                     int64_t n_hint, const Batch2& bt) {
+    P.active = false;
+    if (c.precision != TNR_PREC_SPLIT || (double)m * n_hint * k < TNR_SPLIT_MIN_MNK || n_hint < 16) return;
+    split_a_build(c, P, ta, A, lda, m, k, bt);
+}
+
+void gemm_bulk_a(Ctx& c, const SplitA& P, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
+                 const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                 const Batch2& bt) {
+    if (P.active && P.m == m && P.k == k && gemm_split_tc_a(c, P, tb, n, B, ldb, alpha, beta, C, ldc, bt)) return;
+    gemm_bulk(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
 }
 
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,

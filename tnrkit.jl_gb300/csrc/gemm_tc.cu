@@ -128,6 +128,18 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// FP32 -> FP64 with integer operations only (FP64 arithmetic is scarce on this part):
+// exponent rebias and mantissa shift; FP32 subnormals (below 2^-126) become signed zero,
+// infinities and NaNs keep their class.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu, mant = u & 0x7FFFFFu, sign = u & 0x80000000u;
+    const uint32_t e64 = e == 255u ? 2047u : e + 896u;
+    const uint32_t hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
+    const uint32_t lo = e == 0u ? 0u : (mant << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 struct TcArgs {
     int64_t m, n;
     int nkb;            // K blocks of 64
@@ -217,6 +229,7 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     const int b1 = b % a.n1, b2 = b / a.n1;
     double* C = a.C + b1 * a.sC1 + b2 * a.sC2;
     const int64_t row = (int64_t)tile_m * BM + warp * 32 + lane;
+    const bool plain = a.alpha == 1.0 && a.beta == 0.0;   // C = op(A) op(B): no FP64 arithmetic
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
         float v[16];
@@ -227,8 +240,11 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
                 const int64_t col = (int64_t)tile_n * BN + c0 + j;
                 if (col < a.n) {
                     double* p = C + row + col * a.ldc;
-                    double r = a.alpha * (double)v[j];
-                    if (a.beta != 0.0) r = fma(a.beta, *p, r);
+                    double r = f32_to_f64(v[j]);
+                    if (!plain) {
+                        r *= a.alpha;
+                        if (a.beta != 0.0) r = fma(a.beta, *p, r);
+                    }
                     *p = ok ? r : 0.0;
                 }
             }
@@ -250,6 +266,39 @@ struct SplitArgs {
     int n1, nb;
     __nv_bfloat16* dst;
 };
+
+// x (FP64) -> three BF16 planes with integer and FP32 operations only (FP64 arithmetic is
+// scarce on this part).  xh = x truncated to 24 significant bits (bit fields), xl = the
+// next 23 bits of x as an FP32 value; p0 = rn(xh), p1 = rn(xh - p0), p2 = rn(xh - p0 - p1
+// + xl) with both differences exact in FP32.  |x| below 2^-126 gives zero planes; |x| at
+// or above 2^128 gives infinities, NaN gives NaN.
+__device__ __forceinline__ void split3(double x, __nv_bfloat16& p0, __nv_bfloat16& p1, __nv_bfloat16& p2) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi = (uint32_t)(bits >> 32), lo = (uint32_t)bits;
+    const uint32_t sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FF);   // biased FP64 exponent
+    float xh, xl = 0.0f;
+    if (e < 897) {                              // below the FP32 normal range (or zero)
+        xh = __uint_as_float(sign);
+    } else if (e > 1150) {                      // beyond the FP32 range: inf, or NaN
+        const bool nan = e == 2047 && (((hi & 0xFFFFFu) | lo) != 0u);
+        xh = __uint_as_float(sign | 0x7F800000u | (nan ? 0x00400000u : 0u));
+    } else {
+        xh = __uint_as_float(sign | ((uint32_t)(e - 896) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+        const int es = e - 1023 - 23 + 127;     // FP32 biased exponent of 2^(E - 23)
+        if (es >= 1) {
+            const uint32_t r23 = (lo & 0x1FFFFFFFu) >> 6;   // next 23 bits of the significand
+            const float fr = __uint_as_float(0x4B000000u | r23) - 8388608.0f;   // exact integer
+            xl = (fr * 1.1920928955078125e-07f) * __uint_as_float((uint32_t)es << 23);   // r23 2^-23 2^(E-23)
+            if (sign) xl = -xl;
+        }
+    }
+    p0 = __float2bfloat16_rn(xh);
+    const float r1 = xh - __bfloat162float(p0);
+    p1 = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(p1);
+    p2 = __float2bfloat16_rn(r2 + xl);
+}
 
 __global__ void k_split_planes(SplitArgs a) {
     __shared__ double tile[32][33];
@@ -274,12 +323,8 @@ __global__ void k_split_planes(SplitArgs a) {
         for (int y = threadIdx.y; y < 32; y += blockDim.y) {
             const int64_t i = i0 + y, k = k0 + threadIdx.x;
             if (i < a.rows && k < a.Kp) {
-                const double x = tile[y][threadIdx.x];
-                const __nv_bfloat16 p0 = __double2bfloat16(x);
-                const double r1 = x - (double)__bfloat162float(p0);
-                const __nv_bfloat16 p1 = __double2bfloat16(r1);
-                const double r2 = r1 - (double)__bfloat162float(p1);
-                const __nv_bfloat16 p2 = __double2bfloat16(r2);
+                __nv_bfloat16 p0, p1, p2;
+                split3(tile[y][threadIdx.x], p0, p1, p2);
                 const int64_t plane = a.rows * a.Kp;
                 __nv_bfloat16* D = a.dst + bi * 3 * plane + i * a.Kp + k;
                 D[0] = p0;
@@ -337,30 +382,25 @@ void split_operand(Ctx& c, const double* src, int64_t rows, int64_t K, int64_t K
 
 }  // namespace
 
-bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
-                   int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
-    const int batch = bt.n1 * bt.n2;
-    // tiny products stay on the FP64 path (the early coarse-graining steps carry the largest weights)
-    if (m < 64 || n < 16 || k < 16 || (double)m * n * k * batch < (double)(1 << 26)) return false;
-    if (batch > 65535 || (m + BM - 1) / BM > 2147483647 || (n + BN - 1) / BN > 65535) return false;
+namespace {
+
+bool tc_ready() {
     if (!encode_fn()) return false;
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(k_gemm_split_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     });
-    const int64_t Kp = (k + 7) / 8 * 8;
-    const bool a_b = (bt.sA1 != 0 || bt.sA2 != 0) && batch > 1;
-    const bool b_b = (bt.sB1 != 0 || bt.sB2 != 0) && batch > 1;
-    const int nbA = a_b ? batch : 1, nbB = b_b ? batch : 1;
-    Buf pa(c.pool.get(), (size_t)nbA * 3 * m * Kp * 2), pb(c.pool.get(), (size_t)nbB * 3 * n * Kp * 2);
-    // op(A)(i, kk): ta ? A[kk + i*lda] : A[i + kk*lda];  op(B)(kk, j) as rows j: tb ? B[j + kk*ldb] : B[kk + j*ldb]
-    split_operand(c, A, m, k, Kp, ta ? lda : 1, ta ? 1 : lda, a_b ? bt.sA1 : 0, a_b ? bt.sA2 : 0, a_b ? bt.n1 : 1, nbA,
-                  pa.as<__nv_bfloat16>());
-    split_operand(c, B, n, k, Kp, tb ? 1 : ldb, tb ? ldb : 1, b_b ? bt.sB1 : 0, b_b ? bt.sB2 : 0, b_b ? bt.n1 : 1, nbB,
-                  pb.as<__nv_bfloat16>());
-    CUtensorMap mA, mB;
-    make_map(&mA, pa.as<void>(), m, Kp, nbA, BM);
-    make_map(&mB, pb.as<void>(), n, Kp, nbB, BN);
+    return true;
+}
+
+bool tc_shape_ok(int64_t m, int64_t n, int64_t k, int batch) {
+    if (m < 64 || n < 16 || k < 16) return false;
+    return batch <= 65535 && (m + BM - 1) / BM <= 2147483647 && (n + BN - 1) / BN <= 65535;
+}
+
+void launch_tc(Ctx& c, const CUtensorMap& mA, const CUtensorMap& mB, int64_t m, int64_t n, int64_t k, int64_t Kp,
+               double alpha, double beta, double* C, int64_t ldc, const Batch2& bt, bool a_b, bool b_b) {
+    const int batch = bt.n1 * bt.n2;
     TcArgs args;
     args.m = m;
     args.n = n;
@@ -380,6 +420,60 @@ bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, do
     k_gemm_split_tc<<<grid, NTHREADS, SMEM_BYTES, c.stream>>>(mA, mB, args);
     check_launch("gemm_split_tc");
     prof_stop(rec, c.stream, PROF_GEMM_BULK, 2.0 * m * n * k * batch);
+}
+
+// op(B) (k x n) as n rows of K-major planes; returns whether B is batched
+bool split_b(Ctx& c, bool tb, int64_t n, int64_t k, int64_t Kp, const double* B, int64_t ldb, const Batch2& bt,
+             Buf& pb, CUtensorMap& mB) {
+    const int batch = bt.n1 * bt.n2;
+    const bool b_b = (bt.sB1 != 0 || bt.sB2 != 0) && batch > 1;
+    const int nbB = b_b ? batch : 1;
+    pb = Buf(c.pool.get(), (size_t)nbB * 3 * n * Kp * 2);
+    // op(B)(kk, j) as rows j: tb ? B[j + kk*ldb] : B[kk + j*ldb]
+    split_operand(c, B, n, k, Kp, tb ? 1 : ldb, tb ? ldb : 1, b_b ? bt.sB1 : 0, b_b ? bt.sB2 : 0, b_b ? bt.n1 : 1, nbB,
+                  pb.as<__nv_bfloat16>());
+    make_map(&mB, pb.as<void>(), n, Kp, nbB, BN);
+    return b_b;
+}
+
+}  // namespace
+
+bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                   int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
+    const int batch = bt.n1 * bt.n2;
+    if (!tc_shape_ok(m, n, k, batch) || !tc_ready()) return false;
+    SplitA P;
+    if (!split_a_build(c, P, ta, A, lda, m, k, bt)) return false;
+    return gemm_split_tc_a(c, P, tb, n, B, ldb, alpha, beta, C, ldc, bt);
+}
+
+// planes of op(A) (m x k): op(A)(i, kk) = ta ? A[kk + i*lda] : A[i + kk*lda]
+bool split_a_build(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int64_t m, int64_t k,
+                   const Batch2& bt) {
+    const int batch = bt.n1 * bt.n2;
+    if (m < 64 || k < 16 || batch > 65535 || !tc_ready()) return false;
+    P.m = m;
+    P.k = k;
+    P.Kp = (k + 7) / 8 * 8;
+    P.batched = (bt.sA1 != 0 || bt.sA2 != 0) && batch > 1;
+    P.nb = P.batched ? batch : 1;
+    P.planes = Buf(c.pool.get(), (size_t)P.nb * 3 * m * P.Kp * 2);
+    split_operand(c, A, m, k, P.Kp, ta ? lda : 1, ta ? 1 : lda, P.batched ? bt.sA1 : 0, P.batched ? bt.sA2 : 0,
+                  P.batched ? bt.n1 : 1, P.nb, P.planes.as<__nv_bfloat16>());
+    make_map(&P.map, P.planes.as<void>(), m, P.Kp, P.nb, BM);
+    P.active = true;
+    return true;
+}
+
+bool gemm_split_tc_a(Ctx& c, const SplitA& P, bool tb, int64_t n, const double* B, int64_t ldb, double alpha,
+                     double beta, double* C, int64_t ldc, const Batch2& bt) {
+    const int batch = bt.n1 * bt.n2;
+    if (!P.active || !tc_shape_ok(P.m, n, P.k, batch)) return false;
+    if (P.batched && P.nb != batch) return false;
+    Buf pb;
+    CUtensorMap mB;
+    const bool b_b = split_b(c, tb, n, P.k, P.Kp, B, ldb, bt, pb, mB);
+    launch_tc(c, P.map, mB, P.m, n, P.k, P.Kp, alpha, beta, C, ldc, bt, P.batched, b_b);
     return true;
 }
 

@@ -42,8 +42,13 @@ template <> struct JTol<float> { static constexpr double rel = 2e-7, floor = TNR
 // Input G is FP64 (symmetrised on load); W (FP64, r x r) and lam (FP64) are sorted by |lambda|.
 template <class T>
 __global__ void __launch_bounds__(JTHREADS)
-k_jacobi(const double* __restrict__ Gin, int64_t ldg, int r, double* __restrict__ Wout,
+k_jacobi(const double* __restrict__ Gin, int64_t ldg, int64_t strideG, int r, double* __restrict__ Wout,
          double* __restrict__ lam, T* __restrict__ Ww, int* status) {
+    // one CTA per matrix of a batch
+    Gin += (int64_t)blockIdx.x * strideG;
+    Wout += (int64_t)blockIdx.x * r * r;
+    lam += (int64_t)blockIdx.x * r;
+    if (sizeof(T) == 8) Ww += (int64_t)blockIdx.x * r * r;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ld = r + 1;
     T* G = reinterpret_cast<T*>(smem_raw);  // r x r, leading dim r+1
@@ -178,7 +183,8 @@ k_jacobi(const double* __restrict__ Gin, int64_t ldg, int r, double* __restrict_
 }
 
 template <class T>
-static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {
+static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch,
+                          int64_t strideG) {
     TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "jacobi_eigh: r out of range");
     const size_t aux = 2 * (JMAX / 2 + 1) * (sizeof(T) + sizeof(int));
     const bool w_in_smem = sizeof(T) == 4;      // FP32: eigenvectors in shared memory as well
@@ -188,26 +194,28 @@ static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W
         size_t maxs = (size_t)(JMAX + 1) * JMAX * sizeof(T) + aux + (w_in_smem ? (size_t)JMAX * JMAX * sizeof(T) : 0);
         cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxs);
     });
-    Buf ww(c.pool.get(), (size_t)r * r * sizeof(T));
+    Buf ww(c.pool.get(), w_in_smem ? sizeof(T) : (size_t)batch * r * r * sizeof(T));
     int nt = r <= 32 ? 128 : (r <= 64 ? 256 : JTHREADS);
     int rec = prof_start(c.stream);
-    k_jacobi<T><<<1, nt, smem, c.stream>>>(G, ldg, r, W, lam, ww.as<T>(), c.d_status);
+    k_jacobi<T><<<batch, nt, smem, c.stream>>>(G, ldg, strideG, r, W, lam, ww.as<T>(), c.d_status);
     check_launch("jacobi");
-    prof_stop(rec, c.stream, sizeof(T) == 8 ? PROF_JACOBI : PROF_JACOBI32, (double)r * r * r);
+    prof_stop(rec, c.stream, sizeof(T) == 8 ? PROF_JACOBI : PROF_JACOBI32, (double)r * r * r * batch);
 }
 
-void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {
-    launch_jacobi<double>(c, G, ldg, r, W, lam);
+void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch, int64_t strideG) {
+    launch_jacobi<double>(c, G, ldg, r, W, lam, batch, strideG);
 }
 
-void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam) {
-    launch_jacobi<float>(c, G, ldg, r, W, lam);
+void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch,
+                     int64_t strideG) {
+    launch_jacobi<float>(c, G, ldg, r, W, lam, batch, strideG);
 }
 
 // Cholesky of (G + shift I) = L L^T in shared memory, then L^{-1} (lower) written over G.
 template <class T>
 __global__ void __launch_bounds__(512)
 k_chol_inv(double* G, int r, double shift, int* status) {
+    G += (int64_t)blockIdx.x * r * r;     // one CTA per matrix of a batch
     extern __shared__ __align__(16) unsigned char smem_c[];
     T* S = reinterpret_cast<T*>(smem_c);
     const int ld = r + 1;
@@ -236,45 +244,48 @@ k_chol_inv(double* G, int r, double shift, int* status) {
         }
         __syncthreads();
     }
-    // inverse of the lower-triangular L: column j of L^{-1} by forward substitution,
-    // one warp per column (lanes split the inner products), result kept in S's upper part
-    T* X = S + (size_t)ld * r;   // r x r scratch (column-major, ld r+1)
+    // inverse of the lower-triangular L: column j of X = L^{-1} by forward substitution, one
+    // warp per column (lanes split the inner products).  X shares S's storage: X[i,j], i > j,
+    // sits at the transposed position S[j + i*ld] (strict upper triangle, free once L is
+    // done) and X[j,j] = 1/L[j,j] in the spare row S[r + j*ld]; L stays in the lower triangle.
     const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
     for (int j = warp; j < r; j += nw) {
-        for (int i = 0; i < r; ++i) {
-            if (i < j) { if (lane == 0) X[i + j * ld] = T(0); continue; }
+        if (lane == 0) S[r + j * ld] = T(1) / S[j + j * ld];
+        __syncwarp();
+        for (int i = j + 1; i < r; ++i) {
             T acc = T(0);
-            for (int kk = j + lane; kk < i; kk += 32) acc += S[i + kk * ld] * X[kk + j * ld];
+            for (int kk = j + lane; kk < i; kk += 32)
+                acc += S[i + kk * ld] * (kk == j ? S[r + j * ld] : S[j + kk * ld]);
             for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) X[i + j * ld] = ((i == j ? T(1) : T(0)) - acc) / S[i + i * ld];
+            if (lane == 0) S[j + i * ld] = -acc / S[i + i * ld];
             __syncwarp();
         }
     }
     __syncthreads();
     for (int e = tid; e < r * r; e += nt) {
         int i = e % r, j = e / r;
-        G[e] = (double)X[i + j * ld];
+        G[e] = i > j ? (double)S[j + i * ld] : (i == j ? (double)S[r + j * ld] : 0.0);
     }
     if (tid == 0 && bad) atomicOr(status, ST_CHOL_BREAKDOWN);
 }
 
 template <class T>
-static void launch_chol(Ctx& c, double* G, int r, double shift) {
+static void launch_chol(Ctx& c, double* G, int r, double shift, int batch) {
     TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "chol_inv: r out of range");
-    size_t smem = 2 * (size_t)(r + 1) * r * sizeof(T);
+    size_t smem = (size_t)(r + 1) * r * sizeof(T);
     TNR_REQUIRE(smem <= 227 * 1024, TNR_ERR_UNSUPPORTED, "chol_inv: matrix too large for shared memory");
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(k_chol_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::min<size_t>(2 * (JMAX + 1) * JMAX * sizeof(T), 227 * 1024));
+                             (int)std::min<size_t>((size_t)(JMAX + 1) * JMAX * sizeof(T), 227 * 1024));
     });
     int rec = prof_start(c.stream);
-    k_chol_inv<T><<<1, 512, smem, c.stream>>>(G, r, shift, c.d_status);
+    k_chol_inv<T><<<batch, 512, smem, c.stream>>>(G, r, shift, c.d_status);
     check_launch("chol_inv");
-    prof_stop(rec, c.stream, PROF_CHOL, (double)r * r * r);
+    prof_stop(rec, c.stream, PROF_CHOL, (double)r * r * r * batch);
 }
 
-void chol_inv(Ctx& c, double* G, int r, double shift) { launch_chol<double>(c, G, r, shift); }
-void chol_inv_f32(Ctx& c, double* G, int r, double shift) { launch_chol<float>(c, G, r, shift); }
+void chol_inv(Ctx& c, double* G, int r, double shift, int batch) { launch_chol<double>(c, G, r, shift, batch); }
+void chol_inv_f32(Ctx& c, double* G, int r, double shift, int batch) { launch_chol<float>(c, G, r, shift, batch); }
 
 }  // namespace tnr

@@ -25,4 +25,9 @@ struct Scheme {
     void record(const TsvdOut& r);
 };
 
+// run!() of fresh TRG/BTRG schemes with equal kind, dims and k in lockstep on `c`;
+// norms[b] receives member b's norms and every member is left in its final state
+void run_group(Ctx& c, const std::vector<Scheme*>& members, int chi, int maxiter, bool finalize_beginning,
+               std::vector<std::vector<double>>& norms);
+
 }  // namespace tnr

@@ -3,10 +3,13 @@
 //
 // GB300 runs FP64 at ~2 DFMA/clk/SM, so FP64 work that lives on one SM (Jacobi
 // sweeps, Cholesky) is avoided on the iteration path:
-//  * randomized subspace iteration with r = min(3k, 128) columns; every iteration
-//    aligns the basis with the current Ritz vectors (FP32 Jacobi on the r x r
-//    Gram) and orthonormalises with column-scaled CholeskyQR (FP32 Cholesky,
-//    GEMMs in FP64 or split precision);
+//  * randomized subspace iteration with r = min(3k, 128) columns;
+//    FP64 precision orthonormalises with shifted CholeskyQR3 (FP64 Gram, FP64
+//    Cholesky of the column-scaled Gram, one shifted and two plain passes): backward
+//    stable, so singular directions far below sigma_1 (the steep spectra of ordered
+//    phases) keep FP64 accuracy.  The split precision, whose products carry FP32-level
+//    errors anyway, aligns the basis with the current Ritz vectors (FP32 Jacobi on the
+//    r x r Gram) and orthonormalises with one or two FP32 column-scaled CholeskyQR passes;
 //  * the number of iterations comes from the estimated gap (sigma_r / sigma_k)^2
 //    per iteration, so the kept subspace reaches the target angle;
 //  * one final Rayleigh-Ritz in FP64: polar correction of the basis (GEMMs only),
@@ -40,26 +43,32 @@ static std::vector<double> to_host(Ctx& c, const double* d, int n) {
     return h;
 }
 
-// Q (m x r) <- orthonormal (to FP32 level) basis of span(Y); Y is overwritten.
-// Column-scaled CholeskyQR with an FP32 Cholesky; the first pass is shifted.
+// Q (m x r) <- orthonormal basis of span(Y); Y is overwritten.  Column-scaled CholeskyQR:
+// FP64 precision runs three passes with the FP64 Cholesky, the first shifted by
+// 11 (m r + r (r + 1)) eps (shifted CholeskyQR3, stable for any column grading); the
+// split precision runs `passes` passes with the FP32 Cholesky, the first shifted.
 static void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q, int passes) {
+    const bool f64 = c.precision == TNR_PREC_F64;
+    if (f64) passes = 3;
     Buf G(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf ds(c.pool.get(), (size_t)r * sizeof(double));
     double* src = Y;
     for (int pass = 0; pass < passes; ++pass) {
-        double shift = pass == 0 ? 1e-6 * std::max(1, r / 16) : 1e-7;
+        double shift = f64 ? (pass == 0 ? 11.0 * ((double)m * r + (double)r * (r + 1)) * 2.220446049250313e-16 : 0.0)
+                           : (pass == 0 ? 1e-6 * std::max(1, r / 16) : 1e-7);
         for (int attempt = 0;; ++attempt) {
-            gemm_f64(c, true, false, r, r, m, 1.0, src, m, 0, src, m, 0, 0.0, G.d(), r, 0);
+            gemm_bulk(c, true, false, r, r, m, 1.0, src, m, 0, src, m, 0, 0.0, G.d(), r, 0);
             gram_unit_diag(c, G.d(), r, ds.d());
-            chol_inv_f32(c, G.d(), r, shift);
+            if (f64) chol_inv(c, G.d(), r, shift);
+            else chol_inv_f32(c, G.d(), r, shift);
             int st = c.read_status_and_clear();
             if (!(st & ST_CHOL_BREAKDOWN)) break;
             TNR_REQUIRE(attempt < 5, TNR_ERR_NOT_CONVERGED, "orth: Cholesky breakdown");
-            shift *= 30.0;
+            shift = std::max(shift * 30.0, 1e-14);
         }
         col_scale(c, G.d(), r, r, r, ds.d(), 0);         // Linv D
         double* dst = (src == Q) ? Y : Q;
-        gemm_f64(c, false, true, m, r, r, 1.0, src, m, 0, G.d(), r, 0, 0.0, dst, m, 0);
+        gemm_bulk(c, false, true, m, r, r, 1.0, src, m, 0, G.d(), r, 0, 0.0, dst, m, 0);
         src = dst;
     }
     if (src != Q) copy_f64(c, Q, src, m * (int64_t)r);
@@ -196,19 +205,29 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
     Buf W(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf lam(c.pool.get(), (size_t)r * sizeof(double));
     fill_normal(c, Om.d(), n * (int64_t)r, c.seed + 0x1000193ull * (++c.call_counter));
-    gemm_bulk(c, false, false, m, r, n, 1.0, M, m, 0, Om.d(), n, 0, 0.0, Y.d(), m, 0);
+    // the split precision splits M into BF16 planes once for every product of the iteration
+    const Batch2 one;
+    SplitA PM, PMt;
+    split_a_prepare(c, PM, false, M, m, m, n, r, one);
+    split_a_prepare(c, PMt, true, M, m, n, m, r, one);
+    gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Om.d(), n, 0.0, Y.d(), m, one);
     orth_scaled(c, Y.d(), m, r, Uq.d(), 2);
     int need = MAXIT, it = 0;
+    const bool f64 = c.precision == TNR_PREC_F64;
     for (; it < need; ++it) {
-        // Z = M^T U, aligned with the Ritz vectors of Z^T Z (FP32), then orthonormalised
-        gemm_bulk(c, true, false, n, r, m, 1.0, M, m, 0, Uq.d(), m, 0, 0.0, Z.d(), n, 0);
-        gemm_f64(c, true, false, r, r, n, 1.0, Z.d(), n, 0, Z.d(), n, 0, 0.0, G.d(), r, 0);
-        jacobi_eigh_f32(c, G.d(), r, r, W.d(), lam.d());
-        gemm_f64(c, false, false, n, r, r, 1.0, Z.d(), n, 0, W.d(), r, 0, 0.0, Vq.d(), n, 0);
-        copy_f64(c, Z.d(), Vq.d(), n * (int64_t)r);
-        if (it == 0 || it == 2) col_norms(c, Z.d(), n, r, n, lam.d());   // ~ sigma_i (FP64)
+        // Z = M^T U; its columns aligned with the Ritz vectors of Z^T Z (FP32) give the
+        // sigma estimates, and in split precision the aligned basis is orthonormalised
+        gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, one);
+        const bool estimate = it == 0 || it == 2;
+        if (!f64 || estimate) {
+            gemm_bulk(c, true, false, r, r, n, 1.0, Z.d(), n, 0, Z.d(), n, 0, 0.0, G.d(), r, 0);
+            jacobi_eigh_f32(c, G.d(), r, r, W.d(), lam.d());
+            gemm_bulk(c, false, false, n, r, r, 1.0, Z.d(), n, 0, W.d(), r, 0, 0.0, Vq.d(), n, 0);
+            if (estimate) col_norms(c, Vq.d(), n, r, n, lam.d());   // ~ sigma_i (FP64)
+            if (!f64) copy_f64(c, Z.d(), Vq.d(), n * (int64_t)r);
+        }
         orth_scaled(c, Z.d(), n, r, Vq.d(), it == 0 ? 2 : 1);
-        gemm_bulk(c, false, false, m, r, n, 1.0, M, m, 0, Vq.d(), n, 0, 0.0, Y.d(), m, 0);
+        gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Vq.d(), n, 0.0, Y.d(), m, one);
         orth_scaled(c, Y.d(), m, r, Uq.d(), it == 0 ? 2 : 1);
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, lam.d(), r);
@@ -273,16 +292,24 @@ TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk
     Buf W(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf l(c.pool.get(), (size_t)r * sizeof(double));
     fill_normal(c, Om.d(), n * (int64_t)r, c.seed + 0x1000193ull * (++c.call_counter));
-    gemm_bulk(c, false, false, n, r, n, 1.0, M, n, 0, Om.d(), n, 0, 0.0, Y.d(), n, 0);
+    // M is symmetric: M Q = M^T Q, whose planes are K-contiguous; split once for every product
+    const Batch2 one;
+    SplitA PMt;
+    split_a_prepare(c, PMt, true, M, n, n, n, r, one);
+    gemm_bulk_a(c, PMt, true, false, n, r, n, 1.0, M, n, Om.d(), n, 0.0, Y.d(), n, one);
     orth_scaled(c, Y.d(), n, r, Q.d(), 2);
     int need = MAXIT, it = 0;
+    const bool f64 = c.precision == TNR_PREC_F64;
     for (; it < need; ++it) {
-        gemm_bulk(c, false, false, n, r, n, 1.0, M, n, 0, Q.d(), n, 0, 0.0, Y.d(), n, 0);
-        gemm_f64(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
-        jacobi_eigh_f32(c, H.d(), r, r, W.d(), l.d());
-        gemm_f64(c, false, false, n, r, r, 1.0, Y.d(), n, 0, W.d(), r, 0, 0.0, T.d(), n, 0);
-        if (it == 0 || it == 2) col_norms(c, T.d(), n, r, n, l.d());     // ~ |lambda_i| (FP64)
-        orth_scaled(c, T.d(), n, r, Q.d(), it == 0 ? 2 : 1);
+        gemm_bulk_a(c, PMt, true, false, n, r, n, 1.0, M, n, Q.d(), n, 0.0, Y.d(), n, one);
+        const bool estimate = it == 0 || it == 2;
+        if (!f64 || estimate) {
+            gemm_bulk(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
+            jacobi_eigh_f32(c, H.d(), r, r, W.d(), l.d());
+            gemm_bulk(c, false, false, n, r, r, 1.0, Y.d(), n, 0, W.d(), r, 0, 0.0, T.d(), n, 0);
+            if (estimate) col_norms(c, T.d(), n, r, n, l.d());     // ~ |lambda_i| (FP64)
+        }
+        orth_scaled(c, f64 ? Y.d() : T.d(), n, r, Q.d(), it == 0 ? 2 : 1);
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, l.d(), r);
             need = std::max(it + 1, iterations_needed(est, k, r, 1, target_angle(c)));
