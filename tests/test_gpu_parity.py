@@ -230,3 +230,24 @@ def test_ordered_phase_f64(tnr, oracle, cls, chi, beta):
     ref = oracle.run(getattr(oracle, cls)(oracle.classical_ising(beta, "Trivial")), oracle.truncrank(chi),
                      oracle.maxiter(12))
     np.testing.assert_allclose(got, ref, rtol=1e-10)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_split_group_fixed_point_flows(tnr, seed):
+    """A lockstep group of ten chi = 32 BTRG instances over 30 steps, in which beta = 0.584
+    flows to the ordered and beta = 0.378 to the disordered fixed point: their matrices
+    become numerically rank 1-2 while the group keeps iterating for the others, so most
+    basis columns are noise.  The split path must orthonormalise those columns stably
+    (shifted CholeskyQR3): every member's free energy within 2e-7 of the FP64 group's
+    (an unstable orthonormalisation diverged here, |df/f| = 0.3)."""
+    betas = [0.548, 0.402, 0.458, 0.404, 0.584, 0.378, 0.465, 0.441, 0.503, 0.398]
+
+    def run(prec, sd):
+        out = tnr.run_batch([tnr.BTRG(tnr.classical_ising("Trivial", b), precision=prec, seed=sd) for b in betas],
+                            [32] * len(betas), [30] * len(betas))
+        return [tnr.free_energy(o, b) for o, b in zip(out, betas)]
+
+    ref = run(tnr.PREC_F64, 0)
+    got = run(tnr.PREC_SPLIT, seed)
+    for b, g, r in zip(betas, got, ref):
+        assert abs(g / r - 1) < 2e-7, (b, g, r)

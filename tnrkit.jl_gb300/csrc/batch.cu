@@ -134,9 +134,13 @@ void run_group(Ctx& c, const std::vector<Scheme*>& mem, int chi, int maxiter, bo
     Buf dn(c.pool.get(), (size_t)nn * B * sizeof(double));
     int at = 0;
     if (finalize_beginning) finalize_b(c, s, dn.d() + (at++) * B);
+    const int64_t step0 = mem[0]->steps;
     for (int i = 0; i < nsteps; ++i) {
-        if (s.kind == TNR_TRG) step_trg_b(c, s, chi);
-        else step_btrg_b(c, s, chi);
+        {
+            PrecisionScope scope(c, step0 + i < split_fp64_steps(s.kind));
+            if (s.kind == TNR_TRG) step_trg_b(c, s, chi);
+            else step_btrg_b(c, s, chi);
+        }
         finalize_b(c, s, dn.d() + (at++) * B);
     }
     check_finite(c, dn.d(), (int64_t)nn * B);

@@ -367,11 +367,15 @@ static void step_hotrg3d(Scheme& s, int chi) {
     }
 }
 
+int split_fp64_steps(int kind) { return kind == TNR_HOTRG_3D ? TNR_SPLIT_FP64_STEPS_3D : TNR_SPLIT_FP64_STEPS_2D; }
+
 void Scheme::step(int chi) {
     TNR_REQUIRE(chi >= 1, TNR_ERR_INVALID_ARG, "truncrank(chi) needs chi >= 1");
     last_vals.clear();
     last_counts.clear();
     last_eps.clear();
+    // the split precision computes the leading steps exactly as the FP64 path does
+    PrecisionScope scope(*ctx, steps < split_fp64_steps(kind));
     switch (kind) {
         case TNR_TRG: step_trg(*this, chi); break;
         case TNR_BTRG: step_btrg(*this, chi); break;

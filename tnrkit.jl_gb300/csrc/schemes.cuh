@@ -5,6 +5,29 @@
 
 namespace tnr {
 
+// Split-precision runs compute their first coarse-graining steps in FP64: the norm of
+// step i enters the free energy with weight 2^-i (8^-i in 3D), so the first three 2D
+// steps (the first 3D step) carry 7/8 of it, while their tensors are still small.
+#ifndef TNR_SPLIT_FP64_STEPS_2D
+#define TNR_SPLIT_FP64_STEPS_2D 3
+#endif
+#ifndef TNR_SPLIT_FP64_STEPS_3D
+#define TNR_SPLIT_FP64_STEPS_3D 1
+#endif
+int split_fp64_steps(int kind);
+
+// switches a split-precision context to FP64 for one scope
+struct PrecisionScope {
+    Ctx& c;
+    int saved;
+    PrecisionScope(Ctx& ctx, bool fp64) : c(ctx), saved(ctx.precision) {
+        if (fp64) c.precision = TNR_PREC_F64;
+    }
+    ~PrecisionScope() { c.precision = saved; }
+    PrecisionScope(const PrecisionScope&) = delete;
+    PrecisionScope& operator=(const PrecisionScope&) = delete;
+};
+
 struct Scheme {
     int kind = 0;
     std::unique_ptr<Ctx> ctx;

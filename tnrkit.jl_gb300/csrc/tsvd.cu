@@ -3,13 +3,12 @@
 //
 // GB300 runs FP64 at ~2 DFMA/clk/SM, so FP64 work that lives on one SM (Jacobi
 // sweeps, Cholesky) is avoided on the iteration path:
-//  * randomized subspace iteration with r = min(3k, 128) columns;
-//    FP64 precision orthonormalises with shifted CholeskyQR3 (FP64 Gram, FP64
-//    Cholesky of the column-scaled Gram, one shifted and two plain passes): backward
-//    stable, so singular directions far below sigma_1 (the steep spectra of ordered
-//    phases) keep FP64 accuracy.  The split precision, whose products carry FP32-level
-//    errors anyway, aligns the basis with the current Ritz vectors (FP32 Jacobi on the
-//    r x r Gram) and orthonormalises with one or two FP32 column-scaled CholeskyQR passes;
+//  * randomized subspace iteration with r = min(3k, 128) columns, orthonormalised
+//    every half-step with shifted CholeskyQR3 (FP64 Gram and Cholesky in FP64
+//    precision; split-kernel Grams and FP32 Cholesky in split precision): stable for
+//    the steep spectra of ordered phases and for numerically low-rank matrices, whose
+//    noise columns are nearly dependent; the sigma estimates come from aligning the
+//    basis with the Ritz vectors (FP32 Jacobi on the r x r Gram) at two iterations;
 //  * the number of iterations comes from the estimated gap (sigma_r / sigma_k)^2
 //    per iteration, so the kept subspace reaches the target angle;
 //  * one final Rayleigh-Ritz in FP64: polar correction of the basis (GEMMs only),
@@ -43,13 +42,15 @@ static std::vector<double> to_host(Ctx& c, const double* d, int n) {
     return h;
 }
 
-// Q (m x r) <- orthonormal basis of span(Y); Y is overwritten.  Column-scaled CholeskyQR:
-// FP64 precision runs three passes with the FP64 Cholesky, the first shifted by
-// 11 (m r + r (r + 1)) eps (shifted CholeskyQR3, stable for any column grading); the
-// split precision runs `passes` passes with the FP32 Cholesky, the first shifted.
-static void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q, int passes) {
+// Q (m x r) <- orthonormal basis of span(Y); Y is overwritten.  Shifted CholeskyQR3 on the
+// column-scaled Gram: a shifted pass, then two more, which orthonormalises any column
+// grading and nearly dependent columns (the noise columns of a numerically low-rank M).
+// FP64 precision: FP64 Gram and Cholesky, first shift 11 (m r + r (r + 1)) eps, then none.
+// Split precision: Grams on the split kernel (FP32-level), FP32 Cholesky, shifts
+// 1e-6 max(1, r/16) then 1e-7.
+static void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q) {
     const bool f64 = c.precision == TNR_PREC_F64;
-    if (f64) passes = 3;
+    const int passes = 3;
     Buf G(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf ds(c.pool.get(), (size_t)r * sizeof(double));
     double* src = Y;
@@ -211,24 +212,21 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
     split_a_prepare(c, PM, false, M, m, m, n, r, one);
     split_a_prepare(c, PMt, true, M, m, n, m, r, one);
     gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Om.d(), n, 0.0, Y.d(), m, one);
-    orth_scaled(c, Y.d(), m, r, Uq.d(), 2);
+    orth_scaled(c, Y.d(), m, r, Uq.d());
     int need = MAXIT, it = 0;
-    const bool f64 = c.precision == TNR_PREC_F64;
     for (; it < need; ++it) {
-        // Z = M^T U; its columns aligned with the Ritz vectors of Z^T Z (FP32) give the
-        // sigma estimates, and in split precision the aligned basis is orthonormalised
+        // Z = M^T U; at two iterations its columns aligned with the Ritz vectors of Z^T Z
+        // (FP32 Jacobi) give the sigma estimates that set the iteration count
         gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, one);
-        const bool estimate = it == 0 || it == 2;
-        if (!f64 || estimate) {
+        if (it == 0 || it == 2) {
             gemm_bulk(c, true, false, r, r, n, 1.0, Z.d(), n, 0, Z.d(), n, 0, 0.0, G.d(), r, 0);
             jacobi_eigh_f32(c, G.d(), r, r, W.d(), lam.d());
             gemm_bulk(c, false, false, n, r, r, 1.0, Z.d(), n, 0, W.d(), r, 0, 0.0, Vq.d(), n, 0);
-            if (estimate) col_norms(c, Vq.d(), n, r, n, lam.d());   // ~ sigma_i (FP64)
-            if (!f64) copy_f64(c, Z.d(), Vq.d(), n * (int64_t)r);
+            col_norms(c, Vq.d(), n, r, n, lam.d());   // ~ sigma_i (FP64)
         }
-        orth_scaled(c, Z.d(), n, r, Vq.d(), it == 0 ? 2 : 1);
+        orth_scaled(c, Z.d(), n, r, Vq.d());
         gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Vq.d(), n, 0.0, Y.d(), m, one);
-        orth_scaled(c, Y.d(), m, r, Uq.d(), it == 0 ? 2 : 1);
+        orth_scaled(c, Y.d(), m, r, Uq.d());
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, lam.d(), r);
             need = std::max(it + 1, iterations_needed(est, k, r, 2, target_angle(c)));
@@ -297,19 +295,17 @@ TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk
     SplitA PMt;
     split_a_prepare(c, PMt, true, M, n, n, n, r, one);
     gemm_bulk_a(c, PMt, true, false, n, r, n, 1.0, M, n, Om.d(), n, 0.0, Y.d(), n, one);
-    orth_scaled(c, Y.d(), n, r, Q.d(), 2);
+    orth_scaled(c, Y.d(), n, r, Q.d());
     int need = MAXIT, it = 0;
-    const bool f64 = c.precision == TNR_PREC_F64;
     for (; it < need; ++it) {
         gemm_bulk_a(c, PMt, true, false, n, r, n, 1.0, M, n, Q.d(), n, 0.0, Y.d(), n, one);
-        const bool estimate = it == 0 || it == 2;
-        if (!f64 || estimate) {
+        if (it == 0 || it == 2) {
             gemm_bulk(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
             jacobi_eigh_f32(c, H.d(), r, r, W.d(), l.d());
             gemm_bulk(c, false, false, n, r, r, 1.0, Y.d(), n, 0, W.d(), r, 0, 0.0, T.d(), n, 0);
-            if (estimate) col_norms(c, T.d(), n, r, n, l.d());     // ~ |lambda_i| (FP64)
+            col_norms(c, T.d(), n, r, n, l.d());     // ~ |lambda_i| (FP64)
         }
-        orth_scaled(c, f64 ? Y.d() : T.d(), n, r, Q.d(), it == 0 ? 2 : 1);
+        orth_scaled(c, Y.d(), n, r, Q.d());
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, l.d(), r);
             need = std::max(it + 1, iterations_needed(est, k, r, 1, target_angle(c)));

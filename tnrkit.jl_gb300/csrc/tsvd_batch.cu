@@ -1,6 +1,6 @@
 // Truncated SVD of a batch of equal-shaped matrices, stepped in lockstep: the same
-// algorithm as tsvd() (randomized subspace iteration, shifted CholeskyQR3 in FP64 or
-// FP32-aligned CholeskyQR in split precision, final FP64 Rayleigh-Ritz), with every GEMM batched and every
+// algorithm as tsvd() (randomized subspace iteration orthonormalised with shifted
+// CholeskyQR3, final FP64 Rayleigh-Ritz), with every GEMM batched and every
 // one-CTA solver launched once with one CTA per instance.  The iteration count is the
 // largest any instance of the batch needs.
 #include "common.cuh"
@@ -43,11 +43,12 @@ Batch2 strided(int B, int64_t sA, int64_t sB, int64_t sC) {
     return bt;
 }
 
-// Q[b] (m x r) <- orthonormal basis of span(Y[b]) (Y overwritten), column-scaled CholeskyQR:
-// shifted CholeskyQR3 with the FP64 Cholesky in FP64 precision, `passes` FP32 passes in split
-void orth_b(Ctx& c, double* Y, int64_t m, int r, int B, double* Q, int passes) {
+// Q[b] (m x r) <- orthonormal basis of span(Y[b]) (Y overwritten): shifted CholeskyQR3 on
+// the column-scaled Gram, as orth_scaled() in tsvd.cu (FP64 Gram and Cholesky in FP64
+// precision; split-kernel Grams and FP32 Cholesky in split precision)
+void orth_b(Ctx& c, double* Y, int64_t m, int r, int B, double* Q) {
     const bool f64 = c.precision == TNR_PREC_F64;
-    if (f64) passes = 3;
+    const int passes = 3;
     Buf G(c.pool.get(), (size_t)B * r * r * sizeof(double));
     Buf ds(c.pool.get(), (size_t)B * r * sizeof(double));
     double* src = Y;
@@ -178,23 +179,20 @@ std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n,
     split_a_prepare(c, PM, false, M, m, m, n, r, strided(B, mn, 0, 0));
     split_a_prepare(c, PMt, true, M, m, n, m, r, strided(B, mn, 0, 0));
     gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Om.d(), n, 0.0, Y.d(), m, strided(B, mn, 0, mr));
-    orth_b(c, Y.d(), m, r, B, Uq.d(), 2);
+    orth_b(c, Y.d(), m, r, B, Uq.d());
     const double target = c.precision == TNR_PREC_F64 ? TNR_TARGET_F64 : 1e-9;
     int need = MAXIT, it = 0;
-    const bool f64 = c.precision == TNR_PREC_F64;
     for (; it < need; ++it) {
         gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, strided(B, mn, mr, nr));
-        const bool estimate = it == 0 || it == 2;
-        if (!f64 || estimate) {
+        if (it == 0 || it == 2) {
             gemm_bulk(c, true, false, r, r, n, 1.0, Z.d(), n, Z.d(), n, 0.0, G.d(), r, strided(B, nr, nr, rr));
             jacobi_eigh_f32(c, G.d(), r, r, W.d(), lam.d(), B, rr);
             gemm_bulk(c, false, false, n, r, r, 1.0, Z.d(), n, W.d(), r, 0.0, Vq.d(), n, strided(B, nr, rr, nr));
-            if (estimate) col_norms(c, Vq.d(), n, (int64_t)r * B, n, lam.d());
-            if (!f64) copy_f64(c, Z.d(), Vq.d(), nr * B);
+            col_norms(c, Vq.d(), n, (int64_t)r * B, n, lam.d());
         }
-        orth_b(c, Z.d(), n, r, B, Vq.d(), it == 0 ? 2 : 1);
+        orth_b(c, Z.d(), n, r, B, Vq.d());
         gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Vq.d(), n, 0.0, Y.d(), m, strided(B, mn, nr, mr));
-        orth_b(c, Y.d(), m, r, B, Uq.d(), it == 0 ? 2 : 1);
+        orth_b(c, Y.d(), m, r, B, Uq.d());
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, lam.d(), (int64_t)B * r);
             int mx = 2;
