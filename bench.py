@@ -281,8 +281,11 @@ def run_ours(args, d):
         f_ref = [tnr.free_energy(r, float(betas[i])) for r, i in zip(ref, idx)]
         rel = [abs(f_ours[i] - f_ref[j]) / abs(f_ref[j]) for j, i in enumerate(idx)]
         # scale the sample's time to the whole batch by the per-chi mix of the sample
+        worst = int(np.argmax(rel))
         plain = {"solves_per_s_sample": m / (tm["device_ms"] / 1000.0), "sample_instances": m,
-                 "max_rel_df": max(rel), "median_rel_df": statistics.median(rel)}
+                 "max_rel_df": max(rel), "median_rel_df": statistics.median(rel),
+                 "worst": {"beta": float(betas[idx[worst]]), "chi": int(chis[idx[worst]]),
+                           "f": f_ours[idx[worst]], "f_plain": f_ref[worst]}}
     elif prec == tnr.PREC_F64:
         plain = {"solves_per_s_sample": value, "sample_instances": n, "max_rel_df": 0.0, "note": "this run is the plain path"}
 

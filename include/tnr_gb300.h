@@ -171,9 +171,10 @@ int tnr_profile_read(int cls, uint64_t* launches, double* total_ms, double* work
 
 /* ---- diagnostics: one bulk GEMM through the engine's kernels ------------- */
 /* C (m x n) = op(A) op(B) for `batch` strided problems, host buffers,
- * column-major.  precision TNR_PREC_SPLIT runs the tcgen05 3xBF16 kernel and
- * returns TNR_ERR_UNSUPPORTED when that kernel declines the shape; TNR_PREC_F64
- * runs the FP64 kernel.  No reference counterpart (parity test of the
+ * column-major.  precision TNR_PREC_SPLIT runs the tcgen05 3xBF16 kernel as the
+ * contractions of a coarse-graining step do (K accumulated in chunks of 128 on
+ * fresh FP32 accumulators, chunks summed in FP64) and returns TNR_ERR_UNSUPPORTED
+ * when that kernel declines the shape; TNR_PREC_F64 runs the FP64 kernel.  No reference counterpart (parity test of the
  * contraction kernels). */
 int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k,
                    const double* A, int64_t lda, int64_t strideA,
@@ -183,10 +184,11 @@ int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t 
 /* Device time of one batched GEMM of that shape on seeded N(0,1) device operands
  * (contiguous column-major, strides m*k, k*n, m*n): *ms_out = the CUDA-event time
  * of `reps` back-to-back calls / reps, after one untimed call.  For the split
- * precision the time includes the FP64 -> BF16 plane pass.  No reference
- * counterpart (kernel measurements). */
+ * precision the time includes the FP64 -> BF16 plane pass; contraction = 1 times
+ * the contraction path (K accumulated in chunks), 0 the single-accumulation kernel
+ * of the truncated SVD's products.  No reference counterpart (kernel measurements). */
 int tnr_gemm_time(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k, int batch, int reps,
-                  double* ms_out);
+                  int contraction, double* ms_out);
 
 /* ---- allocation-free split GEMM ------------------------------------------ */
 /* No counterpart in the reference.  C = alpha * op(A) op(B) + beta * C on device

@@ -90,7 +90,7 @@ def lib():
         "tnr_profile_read": (I, [I, C.POINTER(C.c_uint64), pd, pd]),
         "tnr_debug_gemm": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, pd, C.c_int64, C.c_int64, pd, C.c_int64,
                                C.c_int64, pd, C.c_int64, C.c_int64, I]),
-        "tnr_gemm_time": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, I, I, pd]),
+        "tnr_gemm_time": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, I, I, I, pd]),
         "tnr_gemm_split_noalloc": (I, [I, I, C.c_int64, C.c_int64, C.c_int64, D, P, C.c_int64, P, C.c_int64, D, P,
                                        C.c_int64, P, C.c_char_p, Z]),
         "tnr_server_create": (I, [C.POINTER(P), Z, I, I]),
@@ -439,10 +439,11 @@ def debug_gemm(A, B, ta=False, tb=False, precision=PREC_SPLIT):
     return out if A.ndim == 3 else out[0]
 
 
-def gemm_time(m, n, k, batch=1, ta=False, tb=False, precision=PREC_SPLIT, reps=5):
-    """Average device milliseconds of one batched GEMM of this shape on seeded device operands."""
+def gemm_time(m, n, k, batch=1, ta=False, tb=False, precision=PREC_SPLIT, reps=5, contraction=False):
+    """Average device milliseconds of one batched GEMM of this shape on seeded device operands
+    (contraction=True: the contraction path, K accumulated in chunks)."""
     ms = C.c_double()
-    _check(lib().tnr_gemm_time(precision, int(ta), int(tb), m, n, k, batch, reps, C.byref(ms)))
+    _check(lib().tnr_gemm_time(precision, int(ta), int(tb), m, n, k, batch, reps, int(contraction), C.byref(ms)))
     return ms.value
 
 

@@ -459,7 +459,9 @@ int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t 
         Batch2 bt;
         bt.n1 = batch; bt.sA1 = sA; bt.sB1 = sB; bt.sC1 = sC;
         if (precision == TNR_PREC_SPLIT) {
-            bool ran = gemm_split_tc(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), ldc, bt);
+            // the contraction path: K accumulated in chunks summed in FP64
+            bool ran = gemm_split_tc(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), ldc, bt,
+                                     split_chunk_kb());
             TNR_REQUIRE(ran, TNR_ERR_UNSUPPORTED, "split kernel declined this shape");
         } else {
             gemm_f64(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), ldc, bt);
@@ -471,7 +473,7 @@ int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t 
 }
 
 int tnr_gemm_time(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k, int batch, int reps,
-                  double* ms_out) {
+                  int contraction, double* ms_out) {
     if (m < 1 || n < 1 || k < 1 || batch < 1 || reps < 1 || !ms_out)
         return fail(nullptr, TNR_ERR_INVALID_ARG, "bad gemm_time arguments");
     if (precision != TNR_PREC_F64 && precision != TNR_PREC_SPLIT)
@@ -489,7 +491,8 @@ int tnr_gemm_time(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k
         const int64_t lda = ta ? k : m, ldb = tb ? n : k;
         auto once = [&] {
             if (precision == TNR_PREC_SPLIT) {
-                bool ran = gemm_split_tc(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), m, bt);
+                bool ran = gemm_split_tc(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), m, bt,
+                                         contraction ? split_chunk_kb() : 0);
                 TNR_REQUIRE(ran, TNR_ERR_UNSUPPORTED, "split kernel declined this shape");
             } else {
                 gemm_f64(c, ta, tb, m, n, k, 1.0, dA.d(), lda, dB.d(), ldb, 0.0, dC.d(), m, bt);

@@ -184,8 +184,11 @@ struct Batch2 {
 // C = alpha * op(A) op(B) + beta * C  (column-major, strided batch)
 void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt);
+// exact_sum: a contraction of the coarse-graining step, whose split-precision products
+// accumulate K in chunks summed in FP64 (see gemm_split_tc_a)
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
-               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt);
+               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt,
+               bool exact_sum = false);
 void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
               const double* A, int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB,
               double beta, double* C, int64_t ldc, int64_t sC, int batch = 1);
@@ -193,12 +196,20 @@ void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double 
 // bulk-contraction GEMM in the context's precision (FP64 or split 3xBF16 on tcgen05)
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
                const double* A, int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB,
-               double beta, double* C, int64_t ldc, int64_t sC, int batch = 1);
+               double beta, double* C, int64_t ldc, int64_t sC, int batch = 1, bool exact_sum = false);
+
+// subspace iterations of the truncated SVD / eigensolver from sigma estimates (tsvd.cu)
+int iterations_needed(std::vector<double> v, int k, int r, int power, double target, int cap);
+int iteration_cap(const Ctx& c);
+void sigma_estimates(Ctx& c, const double* X, int64_t n, int r, int B, double* G, double* W, double* Xa, double* lam);
+
+// K blocks per accumulation chunk of the contraction GEMMs in split precision
+int split_chunk_kb();
 
 // split 3xBF16 tcgen05 GEMM (FP32 accumulate in TMEM); returns false if the shape is unsupported
 bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
                    const double* A, int64_t lda, const double* B, int64_t ldb,
-                   double beta, double* C, int64_t ldc, const Batch2& bt);
+                   double beta, double* C, int64_t ldc, const Batch2& bt, int chunk_kb = 0);
 
 // BF16 planes of one FP64 A operand, split once and reused by every product with it
 // (the matrix of a truncated SVD meets many thin right-hand sides); inactive unless the
@@ -219,7 +230,7 @@ void gemm_bulk_a(Ctx& c, const SplitA& P, bool ta, bool tb, int64_t m, int64_t n
                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
                  const Batch2& bt);
 bool gemm_split_tc_a(Ctx& c, const SplitA& P, bool tb, int64_t n, const double* B, int64_t ldb, double alpha,
-                     double beta, double* C, int64_t ldc, const Batch2& bt);
+                     double beta, double* C, int64_t ldc, const Batch2& bt, int chunk_kb = 0);
 bool split_a_build(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int64_t m, int64_t k,
                    const Batch2& bt);
 

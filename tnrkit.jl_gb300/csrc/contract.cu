@@ -133,7 +133,7 @@ DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::
         bt.sA1 = sX;
         bt.sB1 = sY;
         bt.sC1 = M_ * N_;
-        if (bulk) gemm_bulk(c, ta, tb, M_, N_, kk, 1.0, X, ldx, Yp, ldy, 0.0, Cn.p(), M_, bt);
+        if (bulk) gemm_bulk(c, ta, tb, M_, N_, kk, 1.0, X, ldx, Yp, ldy, 0.0, Cn.p(), M_, bt, true);
         else gemm_f64(c, ta, tb, M_, N_, kk, 1.0, X, ldx, Yp, ldy, 0.0, Cn.p(), M_, bt);
     };
     if (!best.swap) run(best.ta, best.tb, m, n, pa, lda, sizeA, pb, ldb, sizeB);

@@ -146,13 +146,19 @@ void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double 
 #ifndef TNR_SPLIT_MIN_MNK
 #define TNR_SPLIT_MIN_MNK 4194304.0   // m n k of one instance below which a bulk product stays FP64
 #endif
+#ifndef TNR_SPLIT_CHUNK_KB
+#define TNR_SPLIT_CHUNK_KB 2          // K blocks of 64 per FP32 accumulation chunk of a contraction
+#endif
+
+int split_chunk_kb() { return TNR_SPLIT_CHUNK_KB; }
 
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
-               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt) {
+               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt,
+               bool exact_sum) {
     // products of small instances stay on the FP64 path: the early coarse-graining steps,
     // whose norms carry the largest weights in the free energy, are all small
     if (c.precision == TNR_PREC_SPLIT && (double)m * n * k >= TNR_SPLIT_MIN_MNK &&
-        gemm_split_tc(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt))
+        gemm_split_tc(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt, exact_sum ? TNR_SPLIT_CHUNK_KB : 0))
         return;
     c.bulk_call = true;
     gemm_f64(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
@@ -175,10 +181,10 @@ void gemm_bulk_a(Ctx& c, const SplitA& P, bool ta, bool tb, int64_t m, int64_t n
 
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB, double beta, double* C,
-               int64_t ldc, int64_t sC, int batch) {
+               int64_t ldc, int64_t sC, int batch, bool exact_sum) {
     Batch2 bt;
     bt.n1 = batch; bt.sA1 = sA; bt.sB1 = sB; bt.sC1 = sC;
-    gemm_bulk(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
+    gemm_bulk(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt, exact_sum);
 }
 
 }  // namespace tnr

@@ -204,7 +204,7 @@ static void hotrg_step_y(Scheme& s, const DT& Ux) {
     DT Uxp = permuted(c, Ux, {1, 0, 2});            // [j,i,a]
     const int64_t mW = dD * dR * dU, nW = dL * kx;
     DT W2 = make_dt(c.pool.get(), {dD, dR, dU, dL, kx});
-    gemm_bulk(c, true, false, mW, nW, dL, 1.0, A1p.p(), dL, 0, Uxp.p(), dL, 0, 0.0, W2.p(), mW, 0);
+    gemm_bulk(c, true, false, mW, nW, dL, 1.0, A1p.p(), dL, 0, Uxp.p(), dL, 0, 0.0, W2.p(), mW, 0, 1, true);
     A1p = DT(); Uxp = DT();
     DT A2p = permuted(c, T, {1, 0, 3, 2});          // [e,i,k,g]
     DT V = make_dt(c.pool.get(), {dD, dR, dR, dU, kx});
@@ -215,7 +215,7 @@ static void hotrg_step_y(Scheme& s, const DT& Ux) {
         bt.sB1 = 0;
         bt.sC1 = dD * dR * dR * dU;
         gemm_bulk(c, false, false, dD * dR, dR * dU, dU * dL, 1.0, W2.p(), dD * dR, A2p.p(), dU * dL, 0.0, V.p(),
-                  dD * dR, bt);
+                  dD * dR, bt, true);
     }
     W2 = DT(); A2p = DT();
     DT Uxq = permuted(c, Ux, {1, 0, 2});            // [l,k,d]
@@ -225,7 +225,7 @@ static void hotrg_step_y(Scheme& s, const DT& Ux) {
         bt.n1 = (int)(dU * kx);
         bt.sA1 = dD * dR * dR;
         bt.sC1 = dD * kx;
-        gemm_bulk(c, false, false, dD, kx, dR * dR, 1.0, V.p(), dD, Uxq.p(), dR * dR, 0.0, O.p(), dD, bt);
+        gemm_bulk(c, false, false, dD, kx, dR * dR, 1.0, V.p(), dD, Uxq.p(), dR * dR, 0.0, O.p(), dD, bt, true);
     }
     V = DT();
     s.T = permuted(c, O, {3, 0, 2, 1});
@@ -243,7 +243,7 @@ static void hotrg_step_x(Scheme& s, const DT& Uy) {
     DT A1p = permuted(c, T, {0, 2, 3, 1});          // [a,k,e,i]
     const int64_t mW = dL * dU * dR;
     DT W = make_dt(c.pool.get(), {dL, dU, dR, dD, ky});
-    gemm_bulk(c, false, false, mW, dD * ky, dD, 1.0, A1p.p(), mW, 0, Uy.p(), dD, 0, 0.0, W.p(), mW, 0);
+    gemm_bulk(c, false, false, mW, dD * ky, dD, 1.0, A1p.p(), mW, 0, Uy.p(), dD, 0, 0.0, W.p(), mW, 0, 1, true);
     A1p = DT();
     DT V = make_dt(c.pool.get(), {dL, dU, dU, dR, ky});
     {
@@ -252,7 +252,7 @@ static void hotrg_step_x(Scheme& s, const DT& Uy) {
         bt.sA1 = dL * dU * dR * dD;
         bt.sC1 = dL * dU * dU * dR;
         gemm_bulk(c, false, false, dL * dU, dU * dR, dR * dD, 1.0, W.p(), dL * dU, T.p(), dR * dD, 0.0, V.p(),
-                  dL * dU, bt);
+                  dL * dU, bt, true);
     }
     W = DT();
     DT Tn = make_dt(c.pool.get(), {dL, ky, ky, dR});
@@ -264,7 +264,7 @@ static void hotrg_step_x(Scheme& s, const DT& Uy) {
         bt.n2 = (int)ky;                 // b
         bt.sA2 = dL * dU * dU * dR;
         bt.sC2 = dL;
-        gemm_bulk(c, false, false, dL, ky, dU * dU, 1.0, V.p(), dL, Uy.p(), dU * dU, 0.0, Tn.p(), dL * ky, bt);
+        gemm_bulk(c, false, false, dL, ky, dU * dU, 1.0, V.p(), dL, Uy.p(), dU * dU, 0.0, Tn.p(), dL * ky, bt, true);
     }
     s.T = std::move(Tn);
 }

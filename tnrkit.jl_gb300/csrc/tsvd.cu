@@ -137,18 +137,51 @@ static void transpose2d(Ctx& c, const double* in, int64_t m, int64_t n, double* 
 // iterations needed so the kept subspace reaches the target angle: one iteration
 // contracts the error by rho = (v[r-1] / v[k-1])^power, v = FP64 estimates of |values|
 // (column norms of the aligned basis) sorted descending
-static int iterations_needed(std::vector<double> v, int k, int r, int power, double target) {
+// Subspace iterations for the kept subspace to reach the target angle, from the sigma
+// estimates v: one iteration contracts the angle by (sigma_r / sigma_k)^power.  A kept
+// tail below 1e-13 sigma_1 is numerically zero (2 iterations).  `cap` bounds the count:
+// the split precision caps at 16, since its products resolve no direction below ~1e-7
+// sigma_1 and a noise ratio near 1 there would otherwise run to the FP64 cap of 40 (and
+// in a lockstep group hold every member there).
+int iterations_needed(std::vector<double> v, int k, int r, int power, double target, int cap) {
     std::sort(v.begin(), v.end(), [](double a, double b) { return std::fabs(a) > std::fabs(b); });
-    double vk = std::fabs(v[k - 1]), vr = std::fabs(v[r - 1]), v1 = std::fabs(v[0]);
+    const double vk = std::fabs(v[k - 1]), v1 = std::fabs(v[0]);
+    double vr = std::fabs(v[r - 1]);
     if (!(v1 > 0)) return 2;
-    if (vk <= 1e-13 * v1) return 2;                  // kept tail is numerically zero
+    if (vk <= 1e-13 * v1) return 2;
     vr = std::max(vr, 1e-15 * v1);
     double rho = std::pow(vr / vk, (double)power);
-    if (rho >= 0.999) return MAXIT;
+    if (rho >= 0.999) return cap;
     // +2: the column-norm estimates of the smallest values are upper bounds, and vk is an
     // estimate too; two spare iterations keep the kept subspace at the target angle
     int n = (int)std::ceil(std::log(target) / std::log(rho)) + 2;
-    return std::max(2, std::min(MAXIT, n));
+    return std::max(2, std::min(cap, n));
+}
+
+int iteration_cap(const Ctx& c) { return c.precision == TNR_PREC_F64 ? MAXIT : 16; }
+
+// sigma estimates of the columns of X (n x r, batch B of stride n r): column norms of X
+// aligned with its Ritz vectors.  One FP32 Jacobi on the FP64 Gram leaves ~1e-7 of the
+// leading directions in the small columns; FP64 precision aligns the aligned basis once
+// more (its Gram is nearly diagonal, so the second FP32 rotation removes that leakage and
+// the FP64 products keep the cancellation exact), which resolves estimates down to FP64
+// noise.  G, W: r x r scratch per matrix; Xa: n x r scratch per matrix.
+void sigma_estimates(Ctx& c, const double* X, int64_t n, int r, int B, double* G, double* W, double* Xa, double* lam) {
+    Batch2 g, rot;
+    g.n1 = B; g.sA1 = n * r; g.sB1 = n * r; g.sC1 = (int64_t)r * r;
+    rot.n1 = B; rot.sA1 = n * r; rot.sB1 = (int64_t)r * r; rot.sC1 = n * r;
+    gemm_bulk(c, true, false, r, r, n, 1.0, X, n, X, n, 0.0, G, r, g);
+    jacobi_eigh_f32(c, G, r, r, W, lam, B, (int64_t)r * r);
+    gemm_bulk(c, false, false, n, r, r, 1.0, X, n, W, r, 0.0, Xa, n, rot);
+    if (c.precision == TNR_PREC_F64) {
+        Buf X2(c.pool.get(), (size_t)B * n * r * sizeof(double));
+        gemm_f64(c, true, false, r, r, n, 1.0, Xa, n, Xa, n, 0.0, G, r, g);
+        jacobi_eigh_f32(c, G, r, r, W, lam, B, (int64_t)r * r);
+        gemm_f64(c, false, false, n, r, r, 1.0, Xa, n, W, r, 0.0, X2.d(), n, rot);
+        col_norms(c, X2.d(), n, (int64_t)r * B, n, lam);
+    } else {
+        col_norms(c, Xa, n, (int64_t)r * B, n, lam);
+    }
 }
 
 static bool debug_on() {
@@ -218,18 +251,13 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
         // Z = M^T U; at two iterations its columns aligned with the Ritz vectors of Z^T Z
         // (FP32 Jacobi) give the sigma estimates that set the iteration count
         gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, one);
-        if (it == 0 || it == 2) {
-            gemm_bulk(c, true, false, r, r, n, 1.0, Z.d(), n, 0, Z.d(), n, 0, 0.0, G.d(), r, 0);
-            jacobi_eigh_f32(c, G.d(), r, r, W.d(), lam.d());
-            gemm_bulk(c, false, false, n, r, r, 1.0, Z.d(), n, 0, W.d(), r, 0, 0.0, Vq.d(), n, 0);
-            col_norms(c, Vq.d(), n, r, n, lam.d());   // ~ sigma_i (FP64)
-        }
+        if (it == 0 || it == 2) sigma_estimates(c, Z.d(), n, r, 1, G.d(), W.d(), Vq.d(), lam.d());
         orth_scaled(c, Z.d(), n, r, Vq.d());
         gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Vq.d(), n, 0.0, Y.d(), m, one);
         orth_scaled(c, Y.d(), m, r, Uq.d());
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, lam.d(), r);
-            need = std::max(it + 1, iterations_needed(est, k, r, 2, target_angle(c)));
+            need = std::max(it + 1, iterations_needed(est, k, r, 2, target_angle(c), iteration_cap(c)));
             check_status(c, "tsvd");
         }
     }
@@ -299,16 +327,11 @@ TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk
     int need = MAXIT, it = 0;
     for (; it < need; ++it) {
         gemm_bulk_a(c, PMt, true, false, n, r, n, 1.0, M, n, Q.d(), n, 0.0, Y.d(), n, one);
-        if (it == 0 || it == 2) {
-            gemm_bulk(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
-            jacobi_eigh_f32(c, H.d(), r, r, W.d(), l.d());
-            gemm_bulk(c, false, false, n, r, r, 1.0, Y.d(), n, 0, W.d(), r, 0, 0.0, T.d(), n, 0);
-            col_norms(c, T.d(), n, r, n, l.d());     // ~ |lambda_i| (FP64)
-        }
+        if (it == 0 || it == 2) sigma_estimates(c, Y.d(), n, r, 1, H.d(), W.d(), T.d(), l.d());   // ~ |lambda_i|
         orth_scaled(c, Y.d(), n, r, Q.d());
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, l.d(), r);
-            need = std::max(it + 1, iterations_needed(est, k, r, 1, target_angle(c)));
+            need = std::max(it + 1, iterations_needed(est, k, r, 1, target_angle(c), iteration_cap(c)));
             check_status(c, "teigh");
         }
     }

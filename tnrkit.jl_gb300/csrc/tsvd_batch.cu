@@ -110,18 +110,6 @@ void final_svd_b(Ctx& c, const double* M, bool trans, int64_t m, int p, int B, i
     check_status(c, "final_svd (batched)");
 }
 
-int iterations_needed(std::vector<double> v, int k, int r, int power, double target) {
-    std::sort(v.begin(), v.end(), [](double a, double b) { return std::fabs(a) > std::fabs(b); });
-    double vk = std::fabs(v[k - 1]), vr = std::fabs(v[r - 1]), v1 = std::fabs(v[0]);
-    if (!(v1 > 0)) return 2;
-    if (vk <= 1e-13 * v1) return 2;
-    vr = std::max(vr, 1e-15 * v1);
-    double rho = std::pow(vr / vk, (double)power);
-    if (rho >= 0.999) return MAXIT;
-    int n = (int)std::ceil(std::log(target) / std::log(rho)) + 2;
-    return std::max(2, std::min(MAXIT, n));
-}
-
 // copy the leading k of every p-long vector: out[b*k + i] = in[b*p + i]
 void copy_lead(Ctx& c, const double* in, int p, int k, int B, double* out) {
     TNR_CUDA(cudaMemcpy2DAsync(out, k * sizeof(double), in, p * sizeof(double), k * sizeof(double), B,
@@ -184,12 +172,7 @@ std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n,
     int need = MAXIT, it = 0;
     for (; it < need; ++it) {
         gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, strided(B, mn, mr, nr));
-        if (it == 0 || it == 2) {
-            gemm_bulk(c, true, false, r, r, n, 1.0, Z.d(), n, Z.d(), n, 0.0, G.d(), r, strided(B, nr, nr, rr));
-            jacobi_eigh_f32(c, G.d(), r, r, W.d(), lam.d(), B, rr);
-            gemm_bulk(c, false, false, n, r, r, 1.0, Z.d(), n, W.d(), r, 0.0, Vq.d(), n, strided(B, nr, rr, nr));
-            col_norms(c, Vq.d(), n, (int64_t)r * B, n, lam.d());
-        }
+        if (it == 0 || it == 2) sigma_estimates(c, Z.d(), n, r, B, G.d(), W.d(), Vq.d(), lam.d());
         orth_b(c, Z.d(), n, r, B, Vq.d());
         gemm_bulk_a(c, PM, false, false, m, r, n, 1.0, M, m, Vq.d(), n, 0.0, Y.d(), m, strided(B, mn, nr, mr));
         orth_b(c, Y.d(), m, r, B, Uq.d());
@@ -199,7 +182,7 @@ std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n,
             for (int b = 0; b < B; ++b)
                 mx = std::max(mx, iterations_needed(std::vector<double>(est.begin() + (size_t)b * r,
                                                                         est.begin() + (size_t)(b + 1) * r),
-                                                    k, r, 2, target));
+                                                    k, r, 2, target, iteration_cap(c)));
             need = std::max(it + 1, mx);
             check_status(c, "tsvd (batched)");
         }

@@ -7,8 +7,9 @@ against FP64; it is the target of ncu captures of ``k_gemm_split_tc``.
 ``python tnrkit.jl_gb300/gemm_probe.py shapes`` times (``tnr_gemm_time``, CUDA events,
 device-resident operands) the batched products of one BTRG step of a lockstep group
 of 51 instances at chi = 48 and chi = 32 -- the contractions of the coarse-graining step
-and the products of the truncated SVD -- in both precisions, with the per-class split
-of the time (plane pass / GEMM) from the engine's launch profiler.
+(chunked accumulation; the large-K one also with a single accumulation) and the products
+of the truncated SVD -- in both precisions, with the per-class split of the time (plane
+pass / GEMM) from the engine's launch profiler.
 """
 import os
 import sys
@@ -34,12 +35,13 @@ def step_shapes(chi, batch):
     m = chi * chi
     r = min(128, (3 * chi + 7) // 8 * 8)
     return [
-        ("contract X=D.B (k=chi)", m, m, chi, batch, False, False),
-        ("contract T=X.Y (k=chi^2)", m, m, m, batch, False, False),
-        ("tsvd Y=M.Q", m, r, m, batch, False, False),
-        ("tsvd Z=M^T.U", m, r, m, batch, True, False),
-        ("tsvd gram Z^T Z", r, r, m, batch, True, False),
-        ("tsvd rotate Z.W", m, r, r, batch, False, False),
+        ("contract X=D.B (k=chi)", m, m, chi, batch, False, False, True),
+        ("contract T=X.Y (k=chi^2)", m, m, m, batch, False, False, True),
+        ("  same, one accumulation", m, m, m, batch, False, False, False),
+        ("tsvd Y=M.Q", m, r, m, batch, False, False, False),
+        ("tsvd Z=M^T.U", m, r, m, batch, True, False, False),
+        ("tsvd gram Z^T Z", r, r, m, batch, True, False, False),
+        ("tsvd rotate Z.W", m, r, r, batch, False, False, False),
     ]
 
 
@@ -47,13 +49,15 @@ def shapes_probe(tnr, reps):
     print("%-26s %6s %6s %6s %5s %6s %10s %10s %10s %10s" % ("product", "m", "n", "k", "batch", "prec", "ms",
                                                            "TF/s(2mnk)", "plane ms", "gemm ms"))
     for chi in (48, 32):
-        for name, m, n, k, b, ta, tb in step_shapes(chi, 51):
+        for name, m, n, k, b, ta, tb, con in step_shapes(chi, 51):
             for prec, tag in ((tnr.PREC_SPLIT, "split"), (tnr.PREC_F64, "f64")):
                 if prec == tnr.PREC_SPLIT and (m < 64 or n < 16 or k < 16):
                     continue
+                if prec == tnr.PREC_F64 and not con and name.startswith("  "):
+                    continue
                 tnr.profile_reset()
                 tnr.profile_enable(True)
-                ms = tnr.gemm_time(m, n, k, b, ta, tb, prec, reps)
+                ms = tnr.gemm_time(m, n, k, b, ta, tb, prec, reps, con)
                 tnr.profile_enable(False)
                 prof = tnr.profile_read()
                 calls = reps + 1
