@@ -172,8 +172,8 @@ int tnr_profile_read(int cls, uint64_t* launches, double* total_ms, double* work
 /* ---- diagnostics: one bulk GEMM through the engine's kernels ------------- */
 /* C (m x n) = op(A) op(B) for `batch` strided problems, host buffers,
  * column-major.  precision TNR_PREC_SPLIT runs the tcgen05 3xBF16 kernel as the
- * contractions of a coarse-graining step do (K accumulated in chunks of 128 on
- * fresh FP32 accumulators, chunks summed in FP64) and returns TNR_ERR_UNSUPPORTED
+ * contractions of a coarse-graining step do (K accumulated in chunks of 64 on
+ * fresh FP32 accumulators, chunks summed with round-to-nearest) and returns TNR_ERR_UNSUPPORTED
  * when that kernel declines the shape; TNR_PREC_F64 runs the FP64 kernel.  No reference counterpart (parity test of the
  * contraction kernels). */
 int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k,

@@ -167,8 +167,8 @@ def test_batch_equals_single(tnr):
 def test_split_gemm_same_sign_bias(tnr, k):
     """Same-sign operands (every Ising contraction starts so): the tensor cores truncate
     when adding into the FP32 accumulator, a bias that grows with K (-6e-6 relative at
-    K = 2304 in one accumulation).  The contraction path accumulates K in chunks of 128
-    summed in FP64, which bounds the mean relative error by 4e-7 at any K."""
+    K = 2304 in one accumulation).  The contraction path accumulates K in chunks of 64
+    summed with round-to-nearest, which bounds the mean relative error by 4e-7 at any K."""
     rng = np.random.default_rng(11)
     A = rng.uniform(0, 1, (256, k))
     B = rng.uniform(0, 1, (k, 192))

@@ -228,7 +228,7 @@ void split_a_prepare(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, i
 // gemm_bulk with a prepared A (falls back to gemm_bulk when P is inactive)
 void gemm_bulk_a(Ctx& c, const SplitA& P, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
-                 const Batch2& bt);
+                 const Batch2& bt, bool exact_sum = false);
 bool gemm_split_tc_a(Ctx& c, const SplitA& P, bool tb, int64_t n, const double* B, int64_t ldb, double alpha,
                      double beta, double* C, int64_t ldc, const Batch2& bt, int chunk_kb = 0);
 bool split_a_build(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int64_t m, int64_t k,

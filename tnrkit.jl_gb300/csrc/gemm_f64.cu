@@ -147,7 +147,7 @@ void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double 
 #define TNR_SPLIT_MIN_MNK 4194304.0   // m n k of one instance below which a bulk product stays FP64
 #endif
 #ifndef TNR_SPLIT_CHUNK_KB
-#define TNR_SPLIT_CHUNK_KB 2          // K blocks of 64 per FP32 accumulation chunk of a contraction
+#define TNR_SPLIT_CHUNK_KB 1          // K blocks of 64 per FP32 accumulation chunk of a contraction
 #endif
 
 int split_chunk_kb() { return TNR_SPLIT_CHUNK_KB; }
@@ -174,9 +174,11 @@ void split_a_prepare(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, i
 
 void gemm_bulk_a(Ctx& c, const SplitA& P, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha,
                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
-                 const Batch2& bt) {
-    if (P.active && P.m == m && P.k == k && gemm_split_tc_a(c, P, tb, n, B, ldb, alpha, beta, C, ldc, bt)) return;
-    gemm_bulk(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt);
+                 const Batch2& bt, bool exact_sum) {
+    if (P.active && P.m == m && P.k == k &&
+        gemm_split_tc_a(c, P, tb, n, B, ldb, alpha, beta, C, ldc, bt, exact_sum ? TNR_SPLIT_CHUNK_KB : 0))
+        return;
+    gemm_bulk(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt, exact_sum);
 }
 
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,

@@ -2,9 +2,10 @@
 //
 // C (FP64) = alpha * op(A) op(B) + beta * C with every FP64 operand split into three
 // BF16 planes x = x0 + x1 + x2 (each the BF16 rounding of the previous residual).
-// Six plane products x_i y_j with i + j <= 2 are accumulated in one FP32
-// accumulator in tensor memory (TMEM): about 24 bits of each operand and FP32
-// accumulation.  Smallest terms first, the leading x0 y0 last.
+// Six plane products x_i y_j with i + j <= 2 are accumulated in an FP32 accumulator
+// in tensor memory (TMEM): about 24 bits of each operand and FP32 accumulation,
+// smallest terms first, the leading x0 y0 last.  The contractions of a coarse-graining
+// step use the chunked variant below (unbiased accumulation over long K).
 //
 //  * split pass: FP64 -> BF16 planes in a K-major [batch][plane][rows][Kp] layout
 //    (shared-memory tiled transpose where the source is not K-contiguous);
@@ -686,10 +687,10 @@ bool split_a_build(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int
 }
 
 // chunk_kb > 0: the K blocks are accumulated chunk_kb at a time, each chunk on a fresh
-// FP32 accumulator and added into C in FP64.  The tensor cores truncate when they add
+// FP32 accumulator (k_gemm_split_tc_chunked).  The tensor cores truncate when they add
 // into the FP32 accumulator, a loss of about 2^-25 of its value per K = 16 step and the
 // same sign for same-sign sums (-6e-6 relative at K = 2304); chunks bound that bias by
-// the chunk length, and FP64 sums the chunks with round-to-nearest.
+// the chunk length, and the chunks are summed with round-to-nearest TwoSum.
 bool gemm_split_tc_a(Ctx& c, const SplitA& P, bool tb, int64_t n, const double* B, int64_t ldb, double alpha,
                      double beta, double* C, int64_t ldc, const Batch2& bt, int chunk_kb) {
     const int batch = bt.n1 * bt.n2;

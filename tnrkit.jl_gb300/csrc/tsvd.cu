@@ -269,7 +269,8 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
     Buf Ub(c.pool.get(), (size_t)n * r * sizeof(double));
     Buf Vb(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf sb(c.pool.get(), (size_t)r * sizeof(double));
-    gemm_f64(c, true, false, n, r, m, 1.0, M, m, 0, Uq.d(), m, 0, 0.0, Z.d(), n, 0);
+    // split precision: the projection on the tensor cores with chunked (unbiased) accumulation
+    gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, one, true);
     final_svd(c, Z.d(), false, n, r, Ub.d(), sb.d(), Vb.d());      // B^T = Ub s Vb^T -> M ~ (U Vb) s Ub^T
     gemm_f64(c, false, false, m, k, r, 1.0, Uq.d(), m, 0, Vb.d(), r, 0, 0.0, U, m, 0);
     copy_f64(c, s, sb.d(), k);
@@ -340,7 +341,7 @@ TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk
     if (debug_on()) fprintf(stderr, "[tnr] teigh n=%lld k=%d r=%d iters=%d\n", (long long)n, k, r, it);
     // final Rayleigh-Ritz in FP64
     polar(c, Q.d(), n, r);
-    gemm_f64(c, false, false, n, r, n, 1.0, M, n, 0, Q.d(), n, 0, 0.0, Y.d(), n, 0);
+    gemm_bulk_a(c, PMt, true, false, n, r, n, 1.0, M, n, Q.d(), n, 0.0, Y.d(), n, one, true);
     gemm_f64(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
     final_eigh(c, H.d(), r, W.d(), l.d());
     gemm_f64(c, false, false, n, k, r, 1.0, Q.d(), n, 0, W.d(), r, 0, 0.0, U, n, 0);

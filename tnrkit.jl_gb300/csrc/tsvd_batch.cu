@@ -192,7 +192,8 @@ std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n,
     Buf Ub(c.pool.get(), (size_t)B * nr * sizeof(double));
     Buf Vb(c.pool.get(), (size_t)B * rr * sizeof(double));
     Buf sb(c.pool.get(), (size_t)B * r * sizeof(double));
-    gemm_f64(c, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, strided(B, mn, mr, nr));
+    // split precision: the projection on the tensor cores with chunked (unbiased) accumulation
+    gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq.d(), m, 0.0, Z.d(), n, strided(B, mn, mr, nr), true);
     final_svd_b(c, Z.d(), false, n, r, B, nr, Ub.d(), sb.d(), Vb.d());
     gemm_f64(c, false, false, m, k, r, 1.0, Uq.d(), m, Vb.d(), r, 0.0, U, m, strided(B, mr, rr, m * k));
     copy_lead(c, sb.d(), r, k, B, s);
