@@ -219,6 +219,44 @@ def fp64_gemm_peak_tflops():
         return None
 
 
+def roofline(prof, cls, prec, tnr, peaks):
+    """Roofline entry of kernel class `cls` from a profiled pass: achieved = algorithmic
+    work per launch / average CUDA-event launch duration."""
+    n, ms, work = prof[cls]
+    if not n:
+        return None
+    avg_s = ms / n / 1000.0
+    if cls == "tc":
+        # algorithmic flops 2 m n k; the kernel issues six BF16 plane products per flop pair
+        achieved = work / n / avg_s / 1e12
+        peak = peaks.get("bf16_tflops")
+        return {"kernel": "k_gemm_split_tc[_chunked] (class tc)", "bound": "tensor", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                "mma_achieved": 6.0 * achieved, "mma_frac": 6.0 * achieved / peak if peak else None,
+                "traffic": None, "peak_source": "bf16_tflops of measured (MEASURED_PEAKS.json, burst)",
+                "launches": n, "work_per_launch": work / n, "avg_launch_ms": ms / n,
+                "note": "achieved = algorithmic 2mnk per launch / launch duration; mma_* = the 6 BF16 plane "
+                        "products the kernel issues per 2mnk; traffic: see profiles/"}
+    if cls in ("gemm_bulk", "gemm_f64"):
+        achieved = work / n / avg_s / 1e12
+        peak = fp64_gemm_peak_tflops()
+        return {"kernel": cls, "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run", "launches": n,
+                "work_per_launch": work / n, "avg_launch_ms": ms / n}
+    if cls in ("split", "permute"):
+        achieved = work / n / avg_s / 1e9
+        peak = peaks.get("hbm_gbs")
+        return {"kernel": cls, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": "hbm_gbs of measured (MEASURED_PEAKS.json)", "launches": n,
+                "work_per_launch": work / n, "avg_launch_ms": ms / n}
+    # one-CTA solvers (Jacobi, Cholesky): latency-bound, no throughput roofline
+    return {"kernel": cls, "bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+            "traffic": None, "launches": n, "avg_launch_ms": ms / n,
+            "note": "one CTA per matrix of a batch; bounded by its sequential sweeps, not by a pipe"}
+
+
 def run_ours(args, d):
     sys.path.insert(0, ROOT)
     import __graft_entry__ as ge
@@ -289,32 +327,30 @@ def run_ours(args, d):
     elif prec == tnr.PREC_F64:
         plain = {"solves_per_s_sample": value, "sample_instances": n, "max_rel_df": 0.0, "note": "this run is the plain path"}
 
-    # roofline of the dominant kernel class: one extra profiled pass of the same workload
+    # roofline of the dominant kernel class: one extra profiled pass of the same workload,
+    # its lockstep groups run one after another so that each launch's CUDA-event window
+    # on its stream is the kernel's own duration (concurrent groups would add queueing)
+    prev = os.environ.get("TNR_BATCH_WORKERS")
+    os.environ["TNR_BATCH_WORKERS"] = "1"
     tnr.profile_reset()
     tnr.profile_enable(True)
     schemes = make(prec)
-    tnr.run_batch(schemes, chis, maxit)
+    tm = {}
+    tnr.run_batch(schemes, chis, maxit, timing=tm)
     tnr.profile_enable(False)
     prof = tnr.profile_read()
     tnr.profile_reset()
+    if prev is None:
+        del os.environ["TNR_BATCH_WORKERS"]
+    else:
+        os.environ["TNR_BATCH_WORKERS"] = prev
     for s in schemes:
         s.close()
     dom = max(prof.items(), key=lambda kv: kv[1][1])
-    g = prof["gemm_bulk"]
-    roof = None
-    if g[0]:
-        per_launch_flops = g[2] / g[0]
-        avg_s = g[1] / g[0] / 1000.0
-        achieved = per_launch_flops / avg_s / 1e12
-        if prec == tnr.PREC_SPLIT:
-            peak, src = peaks.get("bf16_tflops"), "bf16_tflops of measured (MEASURED_PEAKS.json, burst)"
-        else:
-            peak, src = fp64_gemm_peak_tflops(), "cuBLAS DGEMM 4096^3 measured in this run (FP64 kernel)"
-        roof = {"kernel": "gemm_bulk", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": (achieved / peak) if peak else None, "traffic": None, "peak_source": src,
-                "launches": g[0], "flops_per_launch": per_launch_flops, "avg_launch_ms": g[1] / g[0],
-                "note": "algorithmic flops 2*m*n*k per launch / CUDA-event launch duration, profiled pass"}
+    roof = roofline(prof, dom[0], prec, tnr, peaks)
     shares = {k: {"launches": v[0], "ms": round(v[1], 3), "work": v[2]} for k, v in prof.items()}
+    profiled = {"device_ms": tm.get("device_ms"), "kernel_ms": sum(v[1] for v in prof.values()),
+                "note": "lockstep groups serialised (TNR_BATCH_WORKERS=1); per-class CUDA-event sums"}
 
     lats_sorted = sorted(lats)
     out = {
@@ -331,7 +367,7 @@ def run_ours(args, d):
         "p50_ms": float(np.percentile(lats_sorted, 50)), "p99_ms": float(np.percentile(lats_sorted, 99)),
         "latency_note": "per-solve completion time from batch start (all solves submitted together)",
         "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "kernel_classes": shares,
-        "dominant_class": dom[0], "plain_f64": plain,
+        "dominant_class": dom[0], "profiled_pass": profiled, "plain_f64": plain,
         "f_check": {"instance0_beta": float(betas[0]), "instance0_chi": int(chis[0]), "f": f_ours[0]},
     }
     return out, chis

@@ -329,7 +329,8 @@ def run_batch(schemes, chis, maxiters, finalize_beginning=True, timing=None):
     return [list(out[i * stride:i * stride + cnt[i]]) for i in range(n)]
 
 
-PROFILE_CLASSES = {"gemm_bulk": 0, "gemm_f64": 1, "jacobi": 2, "chol": 3, "permute": 4, "split": 5, "jacobi32": 6}
+PROFILE_CLASSES = {"gemm_bulk": 0, "gemm_f64": 1, "jacobi": 2, "chol": 3, "permute": 4, "split": 5, "jacobi32": 6,
+                   "tc": 7}
 
 
 def profile_enable(on=True):

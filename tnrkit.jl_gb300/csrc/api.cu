@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -356,7 +357,11 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
     });
     if (st0 != TNR_OK) return st0;
     // one host worker per concurrent task; a task is a lockstep group or a single handle
-    const int workers = std::min((int)tasks.size(), 32);
+    // TNR_BATCH_WORKERS (default 32) bounds the host workers; 1 runs the groups one after
+    // another (a profiling pass whose per-launch event times then exclude queueing)
+    int max_workers = 32;
+    if (const char* w = std::getenv("TNR_BATCH_WORKERS")) max_workers = std::max(1, std::min(32, std::atoi(w)));
+    const int workers = std::min((int)tasks.size(), max_workers);
     std::vector<int> status(n, TNR_OK);
     std::atomic<int> next{0};
     int dev = 0;

@@ -63,14 +63,15 @@ int sm_count();
 // per-kernel-class profiler: CUDA events around launches, algorithmic work units
 // ---------------------------------------------------------------------------
 enum ProfClass : int {
-    PROF_GEMM_BULK = 0,   // bulk contraction GEMMs (FP64 DFMA or split tcgen05), work = flops
+    PROF_GEMM_BULK = 0,   // bulk contraction / projection GEMMs run in FP64, work = flops
     PROF_GEMM_F64 = 1,    // FP64 GEMMs of the decompositions, work = flops
     PROF_JACOBI = 2,      // small Jacobi eigensolver, work = r^3
     PROF_CHOL = 3,        // Cholesky + inverse, work = r^3
     PROF_PERMUTE = 4,     // leg permutes, work = bytes moved
     PROF_SPLIT = 5,       // FP64 -> BF16 split conversion, work = bytes moved
     PROF_JACOBI32 = 6,    // FP32 Jacobi (alignment), work = r^3
-    PROF_NCLASS = 7
+    PROF_TC = 7,          // split 3xBF16 tcgen05 GEMMs, work = 2 m n k flops
+    PROF_NCLASS = 8
 };
 extern std::atomic<bool> g_prof_on;
 int prof_start(cudaStream_t s);

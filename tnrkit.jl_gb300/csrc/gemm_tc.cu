@@ -613,7 +613,7 @@ void launch_tc(Ctx& c, const CUtensorMap& mA, const CUtensorMap& mB, int64_t m, 
     int rec = prof_start(c.stream);
     k_gemm_split_tc<<<grid, NTHREADS, SMEM_BYTES, c.stream>>>(mA, mB, args);
     check_launch("gemm_split_tc");
-    prof_stop(rec, c.stream, PROF_GEMM_BULK, 2.0 * m * n * std::min<int64_t>(k - (int64_t)kb0 * BK, (int64_t)nkb * BK) * batch);
+    prof_stop(rec, c.stream, PROF_TC, 2.0 * m * n * std::min<int64_t>(k - (int64_t)kb0 * BK, (int64_t)nkb * BK) * batch);
 }
 
 void launch_tc_chunked(Ctx& c, const CUtensorMap& mA, const CUtensorMap& mB, int64_t m, int64_t n, int64_t k,
@@ -639,7 +639,7 @@ void launch_tc_chunked(Ctx& c, const CUtensorMap& mA, const CUtensorMap& mB, int
     int rec = prof_start(c.stream);
     k_gemm_split_tc_chunked<<<grid, NT_ACC, SMEM_BYTES, c.stream>>>(mA, mB, args, chunk);
     check_launch("gemm_split_tc_chunked");
-    prof_stop(rec, c.stream, PROF_GEMM_BULK, 2.0 * m * n * k * batch);
+    prof_stop(rec, c.stream, PROF_TC, 2.0 * m * n * k * batch);
 }
 
 // op(B) (k x n) as n rows of K-major planes; returns whether B is batched

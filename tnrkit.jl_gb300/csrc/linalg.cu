@@ -227,39 +227,53 @@ k_chol_inv(double* G, int r, double shift, int* status) {
         S[i + j * ld] = (T)((i >= j) ? G[e] + (i == j ? shift : 0.0) : 0.0);
     }
     __syncthreads();
+    // right-looking Cholesky, two barriers per column: the square root of the next pivot
+    // is taken by the lane that finishes its update (warp 0, lane 0 owns column k+1's
+    // diagonal) and published in `pivot` for the next iteration
+    const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+    __shared__ T pivot;
+    if (tid == 0) {
+        T d = S[0];
+        if (!(d > T(0)) || !isfinite(d)) { bad = 1; d = (T)1e-30; }
+        pivot = sqrt(d);
+    }
+    __syncthreads();
     for (int k = 0; k < r; ++k) {
-        if (tid == 0) {
-            T d = S[k + k * ld];
-            if (!(d > T(0)) || !isfinite(d)) { bad = 1; d = (T)1e-30; }
-            S[k + k * ld] = sqrt(d);
-        }
-        __syncthreads();
-        T dk = S[k + k * ld];
+        const T dk = pivot;
         for (int i = k + 1 + tid; i < r; i += nt) S[i + k * ld] /= dk;
         __syncthreads();
-        int m = r - k - 1;
-        for (int e = tid; e < m * m; e += nt) {
-            int i = k + 1 + e % m, j = k + 1 + e / m;
-            if (i >= j) S[i + j * ld] -= S[i + k * ld] * S[j + k * ld];
+        if (tid == 0) S[k + k * ld] = dk;
+        // trailing update of the lower triangle: one warp per column j, lanes over rows i >= j
+        for (int j = k + 1 + warp; j < r; j += nw) {
+            const T sj = S[j + k * ld];
+            for (int i = j + lane; i < r; i += 32) S[i + j * ld] -= S[i + k * ld] * sj;
+            if (j == k + 1 && lane == 0) {
+                T d = S[j + j * ld];
+                if (!(d > T(0)) || !isfinite(d)) { bad = 1; d = (T)1e-30; }
+                pivot = sqrt(d);
+            }
         }
         __syncthreads();
     }
-    // inverse of the lower-triangular L: column j of X = L^{-1} by forward substitution, one
-    // warp per column (lanes split the inner products).  X shares S's storage: X[i,j], i > j,
-    // sits at the transposed position S[j + i*ld] (strict upper triangle, free once L is
-    // done) and X[j,j] = 1/L[j,j] in the spare row S[r + j*ld]; L stays in the lower triangle.
-    const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-    for (int j = warp; j < r; j += nw) {
-        if (lane == 0) S[r + j * ld] = T(1) / S[j + j * ld];
-        __syncwarp();
-        for (int i = j + 1; i < r; ++i) {
-            T acc = T(0);
-            for (int kk = j + lane; kk < i; kk += 32)
-                acc += S[i + kk * ld] * (kk == j ? S[r + j * ld] : S[j + kk * ld]);
-            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) S[j + i * ld] = -acc / S[i + i * ld];
-            __syncwarp();
+    // inverse X = L^{-1} of the lower-triangular L, row by row: row i needs only the rows
+    // above it, so thread j < i computes X[i,j] = -(sum_{kk=j}^{i-1} L[i,kk] X[kk,j]) / L[i,i]
+    // (two partial sums).  X shares S's storage: X[i,j], i > j, sits at the transposed
+    // position S[j + i*ld] (strict upper triangle, free once L is done) and X[j,j] = 1/L[j,j]
+    // in the spare row S[r + j*ld]; L stays in the lower triangle.
+    for (int i = tid; i < r; i += nt) S[r + i * ld] = T(1) / S[i + i * ld];
+    __syncthreads();
+    for (int i = 1; i < r; ++i) {
+        for (int j = tid; j < i; j += nt) {
+            T a0 = S[i + j * ld] * S[r + j * ld], a1 = T(0);
+            int kk = j + 1;
+            for (; kk + 1 < i; kk += 2) {
+                a0 += S[i + kk * ld] * S[j + kk * ld];
+                a1 += S[i + (kk + 1) * ld] * S[j + (kk + 1) * ld];
+            }
+            if (kk < i) a0 += S[i + kk * ld] * S[j + kk * ld];
+            S[j + i * ld] = -(a0 + a1) * S[r + i * ld];
         }
+        __syncthreads();
     }
     __syncthreads();
     for (int e = tid; e < r * r; e += nt) {

@@ -4,6 +4,10 @@
 seeded n x n x n operands (``tnr_debug_gemm``), twice, and prints its relative error
 against FP64; it is the target of ncu captures of ``k_gemm_split_tc``.
 
+``python tnrkit.jl_gb300/gemm_probe.py contract 2304 2304 4`` runs one batched product on the
+contraction path (chunked accumulation), the target of ncu captures of
+``k_gemm_split_tc_chunked``.
+
 ``python tnrkit.jl_gb300/gemm_probe.py shapes`` times (``tnr_gemm_time``, CUDA events,
 device-resident operands) the batched products of one BTRG step of a lockstep group
 of 51 instances at chi = 48 and chi = 32 -- the contractions of the coarse-graining step
@@ -62,10 +66,18 @@ def shapes_probe(tnr, reps):
                 prof = tnr.profile_read()
                 calls = reps + 1
                 plane = prof["split"][1] / calls
-                gemm = (prof["gemm_bulk"][1] + prof["gemm_f64"][1]) / calls
+                gemm = (prof["tc"][1] + prof["gemm_bulk"][1] + prof["gemm_f64"][1]) / calls
                 tf = 2.0 * m * n * k * b / (ms * 1e-3) / 1e12
                 print("%-26s %6d %6d %6d %5d %6s %10.3f %10.1f %10.3f %10.3f" % (name, m, n, k, b, tag, ms, tf, plane,
                                                                               gemm), flush=True)
+
+
+def contract_probe(tnr, m, k, batch):
+    """One warm-up and one timed batched m x m x k product on the contraction path (the
+    chunked kernel when k > 64): the target of ncu captures of k_gemm_split_tc_chunked."""
+    ms = tnr.gemm_time(m, m, k, batch, False, False, tnr.PREC_SPLIT, 1, True)
+    print("contract m=n=%d k=%d batch=%d: %.3f ms, %.1f TFLOP/s (2mnk)" % (m, k, batch, ms,
+                                                                        2.0 * m * m * k * batch / ms / 1e9))
 
 
 def main():
@@ -74,6 +86,8 @@ def main():
     tnr = ge.package()
     if arg == "shapes":
         shapes_probe(tnr, int(sys.argv[2]) if len(sys.argv) > 2 else 3)
+    elif arg == "contract":
+        contract_probe(tnr, int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]))
     else:
         error_probe(tnr, int(arg))
 
