@@ -137,7 +137,7 @@ void run_group(Ctx& c, const std::vector<Scheme*>& mem, int chi, int maxiter, bo
     const int64_t step0 = mem[0]->steps;
     for (int i = 0; i < nsteps; ++i) {
         {
-            PrecisionScope scope(c, step0 + i < split_fp64_steps(s.kind));
+            PrecisionScope scope(c, split_step_in_fp64(s.kind, step0 + i, s.T.d, s.T.rank - 1, chi));
             if (s.kind == TNR_TRG) step_trg_b(c, s, chi);
             else step_btrg_b(c, s, chi);
         }

@@ -275,6 +275,8 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
 // the MMAs, warps 10-11 only fill the last warpgroup.  Every wait is bounded as in
 // k_gemm_split_tc.
 // ---------------------------------------------------------------------------
+constexpr int ACC_STAGES = 6;                 // one CTA per SM: a deeper ring covers the L2 latency
+constexpr int SMEM_BYTES_ACC = ACC_STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int ACC_WARPS = 8;
 // drain warps + the TMA and MMA warps, rounded up to whole warpgroups (registers are
 // granted per group of four warps, so ten warps cost as much as twelve)
@@ -310,12 +312,12 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t pad = ((raw + 1023) & ~1023u) - raw;
     unsigned char* tiles = smem_raw + pad;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + STAGES * STAGE_BYTES);
-    uint64_t* full = bars;                        // STAGES
-    uint64_t* empty = bars + STAGES;              // STAGES
-    uint64_t* acc_full = bars + 2 * STAGES;       // 2: chunk accumulated
-    uint64_t* acc_empty = bars + 2 * STAGES + 2;  // 2: chunk drained
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 4);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + ACC_STAGES * STAGE_BYTES);
+    uint64_t* full = bars;                        // ACC_STAGES
+    uint64_t* empty = bars + ACC_STAGES;              // ACC_STAGES
+    uint64_t* acc_full = bars + 2 * ACC_STAGES;       // 2: chunk accumulated
+    uint64_t* acc_empty = bars + 2 * ACC_STAGES + 2;  // 2: chunk drained
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * ACC_STAGES + 4);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile_m = blockIdx.x, tile_n = blockIdx.y, b = blockIdx.z;
@@ -323,7 +325,7 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
     const int nchunks = (nkb + chunk - 1) / chunk;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < ACC_STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -354,8 +356,8 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
             const int kbeg = c * chunk, kend = min(nkb, kbeg + chunk);
             for (int t = 0; t < NTERMS && ok; ++t)
                 for (int kb = kbeg; kb < kend; ++kb, ++it) {
-                    const int s = it % STAGES;
-                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    const int s = it % ACC_STAGES;
+                    const uint32_t ph = (uint32_t)(it / ACC_STAGES) & 1u;
                     ok = mbar_wait(&empty[s], ph ^ 1u, a.status);
                     if (!ok) break;
                     unsigned char* sa = tiles + s * STAGE_BYTES;
@@ -380,8 +382,8 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
             bool first = true;
             for (int t = 0; t < NTERMS && ok; ++t)
                 for (int kb = kbeg; kb < kend; ++kb, ++it) {
-                    const int s = it % STAGES;
-                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    const int s = it % ACC_STAGES;
+                    const uint32_t ph = (uint32_t)(it / ACC_STAGES) & 1u;
                     ok = mbar_wait(&full[s], ph, a.status);
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -581,7 +583,7 @@ bool tc_ready() {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(k_gemm_split_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        cudaFuncSetAttribute(k_gemm_split_tc_chunked, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaFuncSetAttribute(k_gemm_split_tc_chunked, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES_ACC);
     });
     return true;
 }
@@ -637,7 +639,7 @@ void launch_tc_chunked(Ctx& c, const CUtensorMap& mA, const CUtensorMap& mB, int
     args.status = c.d_status;
     dim3 grid((unsigned)((m + BM - 1) / BM), (unsigned)((n + BN - 1) / BN), (unsigned)batch);
     int rec = prof_start(c.stream);
-    k_gemm_split_tc_chunked<<<grid, NT_ACC, SMEM_BYTES, c.stream>>>(mA, mB, args, chunk);
+    k_gemm_split_tc_chunked<<<grid, NT_ACC, SMEM_BYTES_ACC, c.stream>>>(mA, mB, args, chunk);
     check_launch("gemm_split_tc_chunked");
     prof_stop(rec, c.stream, PROF_TC, 2.0 * m * n * k * batch);
 }

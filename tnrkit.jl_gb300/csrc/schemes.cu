@@ -369,13 +369,20 @@ static void step_hotrg3d(Scheme& s, int chi) {
 
 int split_fp64_steps(int kind) { return kind == TNR_HOTRG_3D ? TNR_SPLIT_FP64_STEPS_3D : TNR_SPLIT_FP64_STEPS_2D; }
 
+bool split_step_in_fp64(int kind, int64_t step, const int64_t* dims, int nlegs, int chi) {
+    if (step >= split_fp64_steps(kind)) return false;
+    for (int l = 0; l < nlegs; ++l)
+        if (dims[l] >= chi) return false;   // the bond has reached chi: a full-size step
+    return true;
+}
+
 void Scheme::step(int chi) {
     TNR_REQUIRE(chi >= 1, TNR_ERR_INVALID_ARG, "truncrank(chi) needs chi >= 1");
     last_vals.clear();
     last_counts.clear();
     last_eps.clear();
     // the split precision computes the leading steps exactly as the FP64 path does
-    PrecisionScope scope(*ctx, steps < split_fp64_steps(kind));
+    PrecisionScope scope(*ctx, split_step_in_fp64(kind, steps, T.d, T.rank, chi));
     switch (kind) {
         case TNR_TRG: step_trg(*this, chi); break;
         case TNR_BTRG: step_btrg(*this, chi); break;

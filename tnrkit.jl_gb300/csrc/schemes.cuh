@@ -5,9 +5,11 @@
 
 namespace tnr {
 
-// Split-precision runs compute their first coarse-graining steps in FP64: the norm of
-// step i enters the free energy with weight 2^-i (8^-i in 3D), so the first three 2D
-// steps (the first 3D step) carry 7/8 of it, while their tensors are still small.
+// Split-precision runs compute their first coarse-graining steps in FP64 while the bond
+// dimension is still growing (every input leg below chi): the norm of step i enters the
+// free energy with weight 2^-i (8^-i in 3D), so the first three 2D steps (the first 3D
+// step) carry 7/8 of it, while their tensors are still small.  A step whose input has
+// reached chi runs split from the start.
 #ifndef TNR_SPLIT_FP64_STEPS_2D
 #define TNR_SPLIT_FP64_STEPS_2D 3
 #endif
@@ -15,6 +17,7 @@ namespace tnr {
 #define TNR_SPLIT_FP64_STEPS_3D 1
 #endif
 int split_fp64_steps(int kind);
+bool split_step_in_fp64(int kind, int64_t step, const int64_t* dims, int nlegs, int chi);
 
 // switches a split-precision context to FP64 for one scope
 struct PrecisionScope {

@@ -1,12 +1,13 @@
 """GEMM probes through the C ABI.
 
 ``python tnrkit.jl_gb300/gemm_probe.py 4096`` runs the split-precision tcgen05 GEMM on
-seeded n x n x n operands (``tnr_debug_gemm``), twice, and prints its relative error
-against FP64; it is the target of ncu captures of ``k_gemm_split_tc``.
+seeded n x n x n operands (``tnr_debug_gemm``, the contraction path), twice, and prints its
+relative error against FP64.
 
 ``python tnrkit.jl_gb300/gemm_probe.py contract 2304 2304 4`` runs one batched product on the
 contraction path (chunked accumulation), the target of ncu captures of
-``k_gemm_split_tc_chunked``.
+``k_gemm_split_tc_chunked``; ``single`` instead of ``contract`` runs the single-accumulation
+kernel ``k_gemm_split_tc`` of the truncated SVD's products.
 
 ``python tnrkit.jl_gb300/gemm_probe.py shapes`` times (``tnr_gemm_time``, CUDA events,
 device-resident operands) the batched products of one BTRG step of a lockstep group
@@ -72,12 +73,13 @@ def shapes_probe(tnr, reps):
                                                                               gemm), flush=True)
 
 
-def contract_probe(tnr, m, k, batch):
+def contract_probe(tnr, m, k, batch, contraction=True):
     """One warm-up and one timed batched m x m x k product on the contraction path (the
-    chunked kernel when k > 64): the target of ncu captures of k_gemm_split_tc_chunked."""
-    ms = tnr.gemm_time(m, m, k, batch, False, False, tnr.PREC_SPLIT, 1, True)
-    print("contract m=n=%d k=%d batch=%d: %.3f ms, %.1f TFLOP/s (2mnk)" % (m, k, batch, ms,
-                                                                        2.0 * m * m * k * batch / ms / 1e9))
+    chunked kernel when k > 64), or with contraction=False on the single-accumulation
+    kernel of the truncated SVD's products: the targets of ncu captures."""
+    ms = tnr.gemm_time(m, m, k, batch, False, False, tnr.PREC_SPLIT, 1, contraction)
+    print("%s m=n=%d k=%d batch=%d: %.3f ms, %.1f TFLOP/s (2mnk)" % (
+        "contract" if contraction else "single", m, k, batch, ms, 2.0 * m * m * k * batch / ms / 1e9))
 
 
 def main():
@@ -86,8 +88,8 @@ def main():
     tnr = ge.package()
     if arg == "shapes":
         shapes_probe(tnr, int(sys.argv[2]) if len(sys.argv) > 2 else 3)
-    elif arg == "contract":
-        contract_probe(tnr, int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]))
+    elif arg in ("contract", "single"):
+        contract_probe(tnr, int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]), arg == "contract")
     else:
         error_probe(tnr, int(arg))
 
