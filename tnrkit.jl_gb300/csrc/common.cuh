@@ -257,9 +257,6 @@ void transpose_lead(Ctx& c, const double* in, int64_t n, int64_t p, int k, int b
 void trace2d_batched(Ctx& c, const double* T, const int64_t* d, int batch, const double* S1, const double* S2,
                      double* out);
 void scale_batched(Ctx& c, double* T, int64_t per, int batch, const double* norms);
-void decouple_rotation(Ctx& c, const double* G, int r, int kb, double* P);
-void diag_copy(Ctx& c, const double* G, int r, int kb, double* lam);
-void diag_to_host(Ctx& c, const double* G, int r, double* host);
 void fill_normal(Ctx& c, double* x, int64_t n, uint64_t seed);
 void col_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);
 void row_scale(Ctx& c, double* X, int64_t m, int64_t n, int64_t ldx, const double* s, int mode);

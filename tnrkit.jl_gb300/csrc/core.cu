@@ -508,48 +508,6 @@ void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r, in
     check_launch("polar_coeff");
 }
 
-// P = [[I, X], [-X^T, I]] with X_ij = G_ij / (G_jj - G_ii), i < kb <= j (first-order decoupling)
-__global__ void k_decouple(const double* G, int r, int kb, double* P) {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < r * r; e += gridDim.x * blockDim.x) {
-        int i = e % r, j = e / r;
-        double v = (i == j) ? 1.0 : 0.0;
-        if (i < kb && j >= kb) {
-            double den = G[j + (int64_t)j * r] - G[i + (int64_t)i * r];
-            double g = G[i + (int64_t)j * r];
-            v = (den != 0.0) ? g / den : 0.0;
-            if (fabs(v) > 0.25) v = copysign(0.25, v);
-        } else if (i >= kb && j < kb) {
-            double den = G[i + (int64_t)i * r] - G[j + (int64_t)j * r];
-            double g = G[j + (int64_t)i * r];
-            double x = (den != 0.0) ? g / den : 0.0;
-            if (fabs(x) > 0.25) x = copysign(0.25, x);
-            v = -x;
-        }
-        P[e] = v;
-    }
-}
-void decouple_rotation(Ctx& c, const double* G, int r, int kb, double* P) {
-    k_decouple<<<(r * r + 255) / 256, 256, 0, c.stream>>>(G, r, kb, P);
-    check_launch("decouple");
-}
-
-// lam[i] = G[i,i] for kb <= i < r
-__global__ void k_diag_copy(const double* G, int r, int kb, double* lam) {
-    int i = kb + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < r) lam[i] = G[i + (int64_t)i * r];
-}
-void diag_copy(Ctx& c, const double* G, int r, int kb, double* lam) {
-    if (kb >= r) return;
-    k_diag_copy<<<(r - kb + 127) / 128, 128, 0, c.stream>>>(G, r, kb, lam);
-    check_launch("diag_copy");
-}
-
-void diag_to_host(Ctx& c, const double* G, int r, double* host) {
-    TNR_CUDA(cudaMemcpy2DAsync(host, sizeof(double), G, (size_t)(r + 1) * sizeof(double), sizeof(double), r,
-                               cudaMemcpyDeviceToHost, c.stream));
-    c.sync();
-}
-
 __global__ void k_row_scale_batched(double* X, int64_t k, int64_t n_total, const double* s, int mode, int64_t n_per) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * n_total;
          e += (int64_t)gridDim.x * blockDim.x) {

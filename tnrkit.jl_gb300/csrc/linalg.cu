@@ -256,22 +256,24 @@ k_chol_inv(double* G, int r, double shift, int* status) {
         __syncthreads();
     }
     // inverse X = L^{-1} of the lower-triangular L, row by row: row i needs only the rows
-    // above it, so thread j < i computes X[i,j] = -(sum_{kk=j}^{i-1} L[i,kk] X[kk,j]) / L[i,i]
-    // (two partial sums).  X shares S's storage: X[i,j], i > j, sits at the transposed
+    // above it, so thread j < i computes X[i,j] = -(sum_{kk=j}^{i-1} L[i,kk] X[kk,j]) / L[i,i].  X shares S's storage: X[i,j], i > j, sits at the transposed
     // position S[j + i*ld] (strict upper triangle, free once L is done) and X[j,j] = 1/L[j,j]
     // in the spare row S[r + j*ld]; L stays in the lower triangle.
     for (int i = tid; i < r; i += nt) S[r + i * ld] = T(1) / S[i + i * ld];
     __syncthreads();
     for (int i = 1; i < r; ++i) {
         for (int j = tid; j < i; j += nt) {
-            T a0 = S[i + j * ld] * S[r + j * ld], a1 = T(0);
+            // four partial sums: eight independent shared-memory loads per trip
+            T a0 = S[i + j * ld] * S[r + j * ld], a1 = T(0), a2 = T(0), a3 = T(0);
             int kk = j + 1;
-            for (; kk + 1 < i; kk += 2) {
+            for (; kk + 3 < i; kk += 4) {
                 a0 += S[i + kk * ld] * S[j + kk * ld];
                 a1 += S[i + (kk + 1) * ld] * S[j + (kk + 1) * ld];
+                a2 += S[i + (kk + 2) * ld] * S[j + (kk + 2) * ld];
+                a3 += S[i + (kk + 3) * ld] * S[j + (kk + 3) * ld];
             }
-            if (kk < i) a0 += S[i + kk * ld] * S[j + kk * ld];
-            S[j + i * ld] = -(a0 + a1) * S[r + i * ld];
+            for (; kk < i; ++kk) a0 += S[i + kk * ld] * S[j + kk * ld];
+            S[j + i * ld] = -((a0 + a1) + (a2 + a3)) * S[r + i * ld];
         }
         __syncthreads();
     }
