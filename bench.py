@@ -40,7 +40,7 @@ def parse():
     p.add_argument("--instances", type=int, default=256)
     p.add_argument("--maxiter", type=int, default=30)
     p.add_argument("--seed", type=int, default=2026)
-    p.add_argument("--plain-sample", type=int, default=32,
+    p.add_argument("--plain-sample", type=int, default=64,
                    help="instances of the batch also solved on the plain FP64 path (solves/s and |df/f|)")
     p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
