@@ -75,12 +75,15 @@ static void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q) {
     if (src != Q) copy_f64(c, Q, src, m * (int64_t)r);
 }
 
-// Q <- Q (I - E/2 + 3E^2/8), E = Q^T Q - I: cubic correction to FP64 orthonormality (GEMMs only)
+// Q <- Q (I - E/2 + 3E^2/8), E = Q^T Q - I: cubic correction to FP64 orthonormality (GEMMs only).
+// Its inputs (CholeskyQR3 bases, FP32 Jacobi rotations) are orthonormal to FP32 level or better,
+// ||E|| <~ 1e-7, so one step leaves O(||E||^3) ~ 1e-21, below FP64 rounding.
+constexpr int POLAR_STEPS = 1;
 static void polar(Ctx& c, double* Q, int64_t m, int r) {
     Buf E(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf E2(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf T(c.pool.get(), (size_t)m * r * sizeof(double));
-    for (int it = 0; it < 2; ++it) {
+    for (int it = 0; it < POLAR_STEPS; ++it) {
         gemm_f64(c, true, false, r, r, m, 1.0, Q, m, 0, Q, m, 0, 0.0, E.d(), r, 0);
         add_identity(c, E.d(), r, -1.0);
         gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, 0, E.d(), r, 0, 0.0, E2.d(), r, 0);

@@ -73,12 +73,12 @@ void orth_b(Ctx& c, double* Y, int64_t m, int r, int B, double* Q) {
     if (src != Q) copy_f64(c, Q, src, m * (int64_t)r * B);
 }
 
-// Q[b] <- Q[b] (I - E/2 + 3E^2/8), E = Q^T Q - I
+// Q[b] <- Q[b] (I - E/2 + 3E^2/8), E = Q^T Q - I; one step, as polar() in tsvd.cu
 void polar_b(Ctx& c, double* Q, int64_t m, int r, int B) {
     Buf E(c.pool.get(), (size_t)B * r * r * sizeof(double));
     Buf E2(c.pool.get(), (size_t)B * r * r * sizeof(double));
     Buf T(c.pool.get(), (size_t)B * m * r * sizeof(double));
-    for (int it = 0; it < 2; ++it) {
+    for (int it = 0; it < 1; ++it) {
         gemm_f64(c, true, false, r, r, m, 1.0, Q, m, Q, m, 0.0, E.d(), r, strided(B, m * r, m * r, r * r));
         add_identity(c, E.d(), r, -1.0, B);
         gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, E.d(), r, 0.0, E2.d(), r, strided(B, r * r, r * r, r * r));
