@@ -98,3 +98,20 @@ def test_random_hotrg_tensor(tnr, oracle):
     b = oracle.random_hotrg_tensor(6, 3)
     np.testing.assert_allclose(a.array, b.a, rtol=1e-14)
     assert np.linalg.norm(a.array) == pytest.approx(1.0)
+
+
+def header_defines():
+    txt = open(os.path.join(ROOT, "include", "tnr_gb300.h")).read()
+    return {k: int(v) for k, v in re.findall(r"#define\s+(TNR_[A-Z0-9_]+)\s+(\d+)\b", txt)}
+
+
+def test_python_constants_match_header(tnr):
+    """The host layer's scheme kinds, precisions and profiler classes are the header's."""
+    d = header_defines()
+    assert (tnr.TNR_TRG, tnr.TNR_BTRG, tnr.TNR_HOTRG, tnr.TNR_HOTRG_3D) == (
+        d["TNR_TRG"], d["TNR_BTRG"], d["TNR_HOTRG"], d["TNR_HOTRG_3D"])
+    assert (tnr.PREC_F64, tnr.PREC_SPLIT) == (d["TNR_PREC_F64"], d["TNR_PREC_SPLIT"])
+    prof = {k[len("TNR_PROF_"):].lower(): v for k, v in d.items() if k.startswith("TNR_PROF_")}
+    assert prof == tnr.PROFILE_CLASSES
+    codes = sorted(v for k, v in d.items() if k.startswith("TNR_ERR_") or k == "TNR_OK")
+    assert codes == list(range(len(codes)))          # 0..8, no gaps
