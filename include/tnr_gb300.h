@@ -124,8 +124,11 @@ int tnr_timer_start(tnr_handle h);
 int tnr_timer_stop(tnr_handle h, double* ms_out);
 
 /* ---- batched runs: many independent (model, beta, chi) instances --------- */
-/* Runs run!() on n handles concurrently (one CUDA stream per handle, up to 32
- * host workers).  norms_out is n*stride doubles; n_out[i] = norms written for
+/* Runs run!() on n handles.  Fresh TRG/BTRG handles with equal kind, precision,
+ * k, initial legs, chi and maxiter form lockstep groups (one batched GEMM per
+ * contraction, one CTA per member in the small solvers); groups and the other
+ * handles run concurrently, one CUDA stream each, from up to 32 host workers
+ * (environment variable TNR_BATCH_WORKERS, 1..32).  norms_out is n*stride doubles; n_out[i] = norms written for
  * instance i.  device_ms_out (nullable) = device time from the first launch of
  * the batch to the last completion (CUDA events); latency_ms_out (nullable, n
  * entries) = host wall time from batch start to completion of instance i.
