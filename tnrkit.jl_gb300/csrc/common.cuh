@@ -55,6 +55,7 @@ enum : int {
     ST_JACOBI_NOCONV = 1,
     ST_CHOL_BREAKDOWN = 2,
     ST_NONFINITE = 4,
+    ST_TC_TIMEOUT = 8,    // a tcgen05 pipeline wait gave up: the call's results are invalid
 };
 
 int sm_count();

@@ -209,11 +209,14 @@ Ctx::~Ctx() {
 
 void Ctx::sync() { TNR_CUDA(cudaStreamSynchronize(stream)); }
 
+// Every reader of the status word goes through here, so a tensor-core pipeline timeout
+// (whose GEMM wrote zeros) fails the call whichever status bit the caller looks for.
 int Ctx::read_status_and_clear() {
     int h = 0;
     TNR_CUDA(cudaMemcpyAsync(&h, d_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
     TNR_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int), stream));
     TNR_CUDA(cudaStreamSynchronize(stream));
+    TNR_REQUIRE(!(h & ST_TC_TIMEOUT), TNR_ERR_CUDA, "tensor-core pipeline wait timed out; the results are invalid");
     return h;
 }
 

@@ -35,7 +35,6 @@ constexpr int TILE_B_BYTES = BN * BK * 2;   // 16 KB
 constexpr int STAGE_BYTES = TILE_A_BYTES + TILE_B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int NTERMS = 6;
-constexpr int ST_TC_TIMEOUT = 8;
 
 // plane pairs, smallest contributions first
 __constant__ int c_pa[NTERMS] = {2, 1, 0, 1, 0, 0};
