@@ -94,3 +94,33 @@ def test_maxiter(oracle):
     # src/utility/stopping.jl:18
     c = oracle.maxiter(3)
     assert c(2, None) and not c(3, None)
+
+
+def test_hotrg3d_gram_positive_semidefinite(oracle):
+    """test/schemes.jl:385-397 checks that the HOTRG_3D Gram matrices are positive
+    (semi)definite; here on seeded random bosonic 6-leg tensors (fermionic twists are out of
+    scope): MM^dag and M^dag M are symmetric with no eigenvalue below -1e-12 of the largest."""
+    o = oracle
+    rng = np.random.default_rng(4)
+    for d in (2, 3):
+        A1 = o.Tensor(rng.standard_normal((d,) * 6), 2)
+        A2 = o.Tensor(rng.standard_normal((d,) * 6), 2)
+        for G in (o._mmdag_3d(A1, A2), o._mdagm_3d(A1, A2)):
+            M = G.a.reshape(d * d, d * d)
+            assert np.allclose(M, M.T, atol=1e-12 * np.abs(M).max())
+            w = np.linalg.eigvalsh(M)
+            assert w.min() >= -1e-12 * w.max()
+
+
+@pytest.mark.parametrize("cls", ["TRG", "BTRG", "HOTRG"])
+@pytest.mark.parametrize("symmetry", ["Trivial", "Z2"])
+def test_space_consistency_chi7(oracle, cls, symmetry):
+    """test/spaces.jl:6-24: each scheme runs 25 iterations at chi = 7 on Trivial and Z2
+    inputs; here the norms are finite and positive and the free energy is within 1e-3 of
+    Onsager's (test/models.jl tolerance)."""
+    o = oracle
+    data = o.run(getattr(o, cls)(o.classical_ising(o.ISING_BETA_C, symmetry)), o.truncrank(7), o.maxiter(25))
+    assert len(data) == 26 and all(np.isfinite(data)) and min(data) > 0
+    sf = 4.0 if cls == "HOTRG" else 2.0
+    f = o.free_energy(data, o.ISING_BETA_C, sf)
+    assert f == pytest.approx(o.F_ONSAGER, rel=1e-3)
