@@ -115,3 +115,32 @@ def test_python_constants_match_header(tnr):
     assert prof == tnr.PROFILE_CLASSES
     codes = sorted(v for k, v in d.items() if k.startswith("TNR_ERR_") or k == "TNR_OK")
     assert codes == list(range(len(codes)))          # 0..8, no gaps
+
+
+def test_footprint_grows_and_saturates(tnr):
+    """tnr_footprint_bytes (host): grows with chi, HOTRG above BTRG, 3D above 2D, and a
+    chi far beyond any device saturates instead of wrapping around."""
+    a = [tnr.footprint_bytes("BTRG", chi, [2, 2, 2, 2]) for chi in (8, 16, 32, 64)]
+    assert a == sorted(a) and a[0] > 0
+    assert tnr.footprint_bytes("HOTRG", 32, [2] * 4) > tnr.footprint_bytes("BTRG", 32, [2] * 4)
+    assert tnr.footprint_bytes("HOTRG_3D", 16, [2] * 6) > tnr.footprint_bytes("HOTRG", 16, [2] * 4)
+    assert tnr.footprint_bytes("HOTRG_3D", 10 ** 6, [2] * 6) >= 9 * 10 ** 18
+
+
+def test_server_admission_and_errors_without_device(tnr):
+    """The serving loop's host logic: a request that can never fit the HBM budget is refused
+    at submission (TNR_ERR_ADMISSION); an admitted request on a machine without a GPU comes
+    back with TNR_ERR_NO_DEVICE through poll, and the server shuts down cleanly."""
+    srv = tnr.Server(hbm_budget_bytes=1 << 30, max_active=2)
+    T = tnr.classical_ising("Trivial")
+    try:
+        with pytest.raises(tnr.TNRError) as e:
+            srv.submit(T, "HOTRG", 256, 10)
+        assert e.value.status == 5
+        rid = srv.submit(T, "BTRG", 8, 4)
+        with pytest.raises(tnr.TNRError) as e:
+            srv.result(rid)
+        assert e.value.status == 8
+        assert srv.stats()["active"] == 0
+    finally:
+        srv.close()
