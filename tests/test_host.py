@@ -144,3 +144,17 @@ def test_server_admission_and_errors_without_device(tnr):
         assert srv.stats()["active"] == 0
     finally:
         srv.close()
+
+
+def test_run_batch_rejects_a_handle_twice(tnr):
+    """A handle is single-owner; tnr_run_batch refuses a batch that names one twice before it
+    touches the handles (the two entries are the same opaque pointer value, never dereferenced)."""
+    fake = ctypes.c_void_p(0x1000)
+    hs = (ctypes.c_void_p * 2)(fake, fake)
+    chi = (ctypes.c_int * 2)(8, 8)
+    mi = (ctypes.c_int * 2)(4, 4)
+    norms = (ctypes.c_double * 20)()
+    counts = (ctypes.c_size_t * 2)()
+    lib = tnr.lib()
+    st = lib.tnr_run_batch(hs, 2, chi, mi, 1, norms, 10, counts, None, None)
+    assert st == 1                       # TNR_ERR_INVALID_ARG

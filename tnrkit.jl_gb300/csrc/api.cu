@@ -307,6 +307,13 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
         size_t need = (size_t)std::max(maxiter[i], 1) + (finalize_beginning ? 1 : 0);
         if (need > stride) return fail(nullptr, TNR_ERR_INVALID_ARG, "stride too small for run!");
     }
+    {
+        // a handle is single-owner: the same handle twice would be driven by two workers at once
+        std::vector<tnr_handle> sorted(hs, hs + n);
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+            return fail(nullptr, TNR_ERR_INVALID_ARG, "the same handle appears twice in the batch");
+    }
     // lockstep groups: fresh TRG/BTRG schemes with equal kind, precision, k, dims, chi, maxiter
     struct Task {
         std::vector<int> idx;
@@ -320,8 +327,10 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
             bool groupable = (sc.kind == TNR_TRG || sc.kind == TNR_BTRG) && sc.steps == 0;
             std::string key;
             if (groupable) {
+                uint64_t kbits = 0;                                   // k exactly, not to 6 decimals
+                std::memcpy(&kbits, &sc.btrg_k, sizeof kbits);
                 key = std::to_string(sc.kind) + "/" + std::to_string(sc.ctx->precision) + "/" +
-                      std::to_string(sc.btrg_k) + "/" + std::to_string(chi[i]) + "/" + std::to_string(maxiter[i]);
+                      std::to_string(kbits) + "/" + std::to_string(chi[i]) + "/" + std::to_string(maxiter[i]);
                 for (int l = 0; l < sc.T.rank; ++l) key += "/" + std::to_string(sc.T.d[l]);
             }
             auto it = groupable ? key_to_task.find(key) : key_to_task.end();
