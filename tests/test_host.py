@@ -158,3 +158,9 @@ def test_run_batch_rejects_a_handle_twice(tnr):
     lib = tnr.lib()
     st = lib.tnr_run_batch(hs, 2, chi, mi, 1, norms, 10, counts, None, None)
     assert st == 1                       # TNR_ERR_INVALID_ARG
+
+
+def test_run_batch_argument_checks(tnr):
+    assert tnr.run_batch([], [], []) == []
+    with pytest.raises(ValueError):
+        tnr.run_batch([], [8], [])

@@ -311,6 +311,13 @@ def run_batch(schemes, chis, maxiters, finalize_beginning=True, timing=None):
     If ``timing`` is a dict it receives ``device_ms`` (CUDA-event span of the batch) and
     ``latency_ms`` (per-instance completion times from batch start)."""
     n = len(schemes)
+    if len(chis) != n or len(maxiters) != n:
+        raise ValueError("one chi and one maxiter per scheme")
+    if n == 0:
+        if timing is not None:
+            timing["device_ms"] = 0.0
+            timing["latency_ms"] = np.zeros(0)
+        return []
     stride = max(max(int(m), 1) for m in maxiters) + 1
     out = np.empty(n * stride)
     cnt = (C.c_size_t * n)()
