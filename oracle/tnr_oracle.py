@@ -266,6 +266,18 @@ def classical_ising(beta=ISING_BETA_C, symmetry="Z2", h=0.0):
     return Tensor(a, 2, _leg_charges(2, 2, 4, N), N)
 
 
+def classical_ising_impurity(beta=ISING_BETA_C, h=0.0):
+    """src/models/ising.jl:87-102 (Trivial): the magnetisation impurity, whose even-parity
+    entries carry sinh(h beta) and odd-parity ones cosh(h beta) (the pure tensor swaps them)."""
+    x, y = math.cosh(beta), math.sinh(beta)
+    b = np.array([[math.sqrt(x), 0.0], [0.0, math.sqrt(y)]])
+    init = np.zeros((2, 2, 2, 2))
+    for i, j, k, l in np.ndindex(2, 2, 2, 2):
+        init[i, j, k, l] = math.sinh(h * beta) if (i + j + k + l) % 2 == 0 else math.cosh(h * beta)
+    a = 2.0 * np.einsum('abcd,ia,jb,ck,dl->ijkl', init, b, b, b, b)
+    return Tensor(a, 2, None, 1)
+
+
 def classical_ising_3D(beta=ISING_BETA_C_3D, symmetry="Z2", J=1.0):
     """src/models/ising.jl:130-165 (Z2 branch; the Trivial branch is the same model in a
     different basis).  Legs: D (x) U' <- N (x) E (x) S' (x) W'."""
@@ -398,6 +410,19 @@ class HOTRG_3D:
         self.T = T.copy()
         self.svals = []
         self.eps = []
+
+
+class ImpurityHOTRG:
+    """src/schemes/impurityhotrg.jl:25-44: the pure tensor, the two first-order impurity
+    tensors and the second-order one, all of the same spaces."""
+
+    def __init__(self, T: Tensor, T_imp_order1_1: Tensor, T_imp_order1_2: Tensor, T_imp_order2: Tensor):
+        for t in (T_imp_order1_1, T_imp_order1_2):
+            assert t.a.shape == T.a.shape, "the first-order impurities need the spaces of T"
+        self.T = T.copy()
+        self.T_imp_order1_1 = T_imp_order1_1.copy()
+        self.T_imp_order1_2 = T_imp_order1_2.copy()
+        self.T_imp_order2 = T_imp_order2.copy()
 
 
 def SVD12(T: Tensor, chi):
@@ -577,6 +602,35 @@ def step_hotrg3d(scheme: HOTRG_3D, chi):
         scheme.eps += [p1, p2]
 
 
+def _combine(terms):
+    """sum of c * t for (c, t) pairs of equal-space tensors"""
+    t0 = terms[0][1]
+    return Tensor(sum(c * t.a for c, t in terms), t0.nout, t0.q, t0.N)
+
+
+def step_impurity_hotrg(scheme: ImpurityHOTRG, chi):
+    """src/schemes/impurityhotrg.jl:46-84: the y projector of the pure tensor, x-steps of the
+    pure / impurity pairs; then the x projector and y-steps, with the symmetrised averages."""
+    for proj, stepf in ((_hotrg_yproj, _hotrg_step_x), (_hotrg_xproj, _hotrg_step_y)):
+        T, T11, T12, T2 = scheme.T, scheme.T_imp_order1_1, scheme.T_imp_order1_2, scheme.T_imp_order2
+        U = proj(T, T, chi)[0]
+        st = lambda a, b: stepf(a, b, U)          # noqa: E731
+        scheme.T = st(T, T)
+        scheme.T_imp_order1_1 = _combine([(0.5, st(T11, T)), (0.5, st(T, T11))])
+        scheme.T_imp_order1_2 = _combine([(0.5, st(T12, T)), (0.5, st(T, T12))])
+        scheme.T_imp_order2 = _combine([(0.25, st(T2, T)), (0.25, st(T, T2)), (0.25, st(T11, T12)),
+                                        (0.25, st(T12, T11))])
+
+
+def finalize_impurity_hotrg(scheme: ImpurityHOTRG):
+    """src/utility/finalize.jl:91-101: the four trace norms; every tensor /= the pure one's."""
+    tr = [abs(np.einsum('abba->', t.a)) for t in (scheme.T, scheme.T_imp_order1_1, scheme.T_imp_order1_2,
+                                                  scheme.T_imp_order2)]
+    for t in (scheme.T, scheme.T_imp_order1_1, scheme.T_imp_order1_2, scheme.T_imp_order2):
+        t.a = t.a / tr[0]
+    return tuple(float(x) for x in tr)
+
+
 def step(scheme, chi):
     """``step!(scheme, truncrank(chi))`` dispatch (src/schemes/tnrscheme.jl:2)."""
     if isinstance(scheme, TRG):
@@ -587,13 +641,18 @@ def step(scheme, chi):
         step_hotrg(scheme, chi)
     elif isinstance(scheme, HOTRG_3D):
         step_hotrg3d(scheme, chi)
+    elif isinstance(scheme, ImpurityHOTRG):
+        step_impurity_hotrg(scheme, chi)
     else:
         raise TypeError(type(scheme))
     return scheme
 
 
 def finalize(scheme):
-    """src/utility/finalize.jl:4-14,62-66: trace norm, then T /= n."""
+    """src/utility/finalize.jl:4-14,62-66: trace norm, then T /= n (ImpurityHOTRG: the
+    tuple of four norms, src/utility/finalize.jl:91-101)."""
+    if isinstance(scheme, ImpurityHOTRG):
+        return finalize_impurity_hotrg(scheme)
     T = scheme.T.a
     if isinstance(scheme, (TRG, HOTRG)):
         n = abs(np.einsum('abba->', T))                 # T[1 2; 2 1]

@@ -124,3 +124,30 @@ def test_space_consistency_chi7(oracle, cls, symmetry):
     sf = 4.0 if cls == "HOTRG" else 2.0
     f = o.free_energy(data, o.ISING_BETA_C, sf)
     assert f == pytest.approx(o.F_ONSAGER, rel=1e-3)
+
+
+def test_impurity_hotrg_onsager(oracle):
+    """test/schemes.jl:400-410: ImpurityHOTRG(T, T_imp1, T_imp1, T) on the Ising model at
+    beta_c, truncrank(16), maxiter(25): the pure norms give Onsager's f to 6e-7 (sf 4)."""
+    o = oracle
+    T = o.classical_ising(o.ISING_BETA_C, "Trivial")
+    imp = o.classical_ising_impurity()
+    data = o.run(o.ImpurityHOTRG(T, imp, imp, T), o.truncrank(16), o.maxiter(25))
+    assert len(data) == 26 and all(len(d) == 4 for d in data)
+    f = o.free_energy([d[0] for d in data], o.ISING_BETA_C, 4.0)
+    assert f == pytest.approx(o.F_ONSAGER, rel=6e-7)
+
+
+@pytest.mark.parametrize("beta,m2,tol", [(0.2, 0.0, 1e-14), (1.0, 1.0, 1e-2)])
+def test_impurity_hotrg_magnetisation_limits(oracle, beta, m2, tol):
+    """test/schemes.jl:412-440: <m^2> = n_2 / n of the last step tends to 0 at high
+    temperature (atol 1e-14) and to 1 at low temperature (rtol 1e-2), truncrank(8)."""
+    o = oracle
+    T = o.classical_ising(beta, "Trivial")
+    imp = o.classical_ising_impurity(beta)
+    data = o.run(o.ImpurityHOTRG(T, imp, imp, o.classical_ising(beta, "Trivial")), o.truncrank(8), o.maxiter(25))
+    got = data[-1][3] / data[-1][0]
+    if m2 == 0.0:
+        assert abs(got) <= tol
+    else:
+        assert got == pytest.approx(m2, rel=tol)
