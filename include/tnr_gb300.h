@@ -43,6 +43,7 @@ extern "C" {
 #define TNR_BTRG      2   /* btrg.jl:132-200   */
 #define TNR_HOTRG     3   /* hotrg.jl:27-160   */
 #define TNR_HOTRG_3D  4   /* hotrg3d.jl:27-135 */
+#define TNR_IMPURITY_HOTRG 5 /* impurityhotrg.jl:25-84; created by tnr_create_impurity_hotrg */
 
 /* ---- arithmetic of the bulk contractions -------------------------------- */
 #define TNR_PREC_F64    0  /* plain path: every operation in FP64                      */
@@ -75,6 +76,19 @@ int tnr_create(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
 /* Same, from a device pointer (column-major FP64) already in GPU memory. */
 int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
                       const double* device_data, const tnr_options* opts);
+
+/* ImpurityHOTRG(T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)
+ * (impurityhotrg.jl:25-44): four host tensors of the same dims (4 legs, column-major).
+ * tnr_step steps all four (impurityhotrg.jl:46-84); tnr_finalize returns the pure norm and
+ * tnr_finalize_impurity the four norms of finalize!(::ImpurityHOTRG) (finalize.jl:91-101). */
+int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double* T,
+                              const double* T_imp_order1_1, const double* T_imp_order1_2,
+                              const double* T_imp_order2, const tnr_options* opts);
+int tnr_finalize_impurity(tnr_handle h, double* norms4_out);
+/* run! with ImpurityHOTRG_Finalizer (tnrscheme.jl:28): 4 norms per entry (pure, +1, -1,
+ * second order) into norms_out (cap doubles); *n_out = entries written. */
+int tnr_run_impurity(tnr_handle h, int chi, int maxiter, int finalize_beginning,
+                     double* norms_out, size_t cap, size_t* n_out);
 
 /* One coarse-graining step with truncrank(chi).
  * Replaces step!(scheme, trunc) (tnrscheme.jl:2; trg.jl:94, btrg.jl:166,

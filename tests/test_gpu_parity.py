@@ -126,6 +126,25 @@ def test_hotrg_random_single_step(tnr, oracle, chi, seed):
     np.testing.assert_allclose(eps, ref, rtol=1e-6)
 
 
+def test_impurity_hotrg(tnr, oracle):
+    """ImpurityHOTRG (src/schemes/impurityhotrg.jl:46-84, finalize.jl:91-101) on the Ising
+    model at beta_c with the magnetisation impurity, truncrank(16), 4 steps: the four norms
+    of every step (pure, +1, -1, second order) against the oracle to 1e-10.  The first-order
+    impurity is Z2-odd, so its trace vanishes up to rounding: an absolute floor of 1e-12 of
+    the largest norm covers those entries."""
+    o = oracle
+    T, imp = tnr.classical_ising("Trivial"), tnr.classical_ising_impurity()
+    s = tnr.ImpurityHOTRG(T, imp, imp, T)
+    d = np.array(tnr.run(s, tnr.truncrank(16), tnr.maxiter(4)))
+    To, impo = o.classical_ising(o.ISING_BETA_C, "Trivial"), o.classical_ising_impurity()
+    do = np.array(o.run(o.ImpurityHOTRG(To, impo, impo, To), o.truncrank(16), o.maxiter(4)))
+    assert d.shape == do.shape == (5, 4)
+    np.testing.assert_allclose(d, do, rtol=1e-10, atol=1e-12 * np.abs(do).max())
+    # the handle keeps HOTRG's API: one more step and finalize (the four norms) work on it
+    tnr.step(s, tnr.truncrank(16))
+    assert len(tnr.finalize(s)) == 4
+
+
 def test_edge_cases(tnr, oracle):
     o = oracle
     T, To = tnr.classical_ising("Trivial"), o.classical_ising(symmetry="Trivial")

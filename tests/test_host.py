@@ -70,11 +70,13 @@ def test_no_device_is_an_error_not_a_crash(tnr):
     assert e.value.status in (8, 4)
 
 
-@pytest.mark.parametrize("name", ["ising", "ising_triv", "potts3", "clock6", "clock3", "ising3d"])
+@pytest.mark.parametrize("name", ["ising", "ising_triv", "ising_impurity", "potts3", "clock6", "clock3", "ising3d"])
 def test_models_match_oracle(tnr, oracle, name):
     o = oracle
     if name == "ising":
         a, b = tnr.classical_ising("Z2"), o.classical_ising(symmetry="Z2")
+    elif name == "ising_impurity":
+        a, b = tnr.classical_ising_impurity(0.41, 0.3), o.classical_ising_impurity(0.41, 0.3)
     elif name == "ising_triv":
         a, b = tnr.classical_ising("Trivial", 0.37), o.classical_ising(0.37, "Trivial")
     elif name == "potts3":

@@ -19,14 +19,14 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .models import (SymTensor, classical_clock, classical_ising, classical_ising_3D, classical_potts,  # noqa: F401
-                     f_onsager, ising_beta_c, ising_beta_c_3D, ising_βc, ising_βc_3D, potts_beta_c, potts_βc,
-                     random_hotrg_tensor)
+from .models import (SymTensor, classical_clock, classical_ising, classical_ising_3D, classical_ising_impurity,  # noqa: F401
+                     classical_potts, f_onsager, ising_beta_c, ising_beta_c_3D, ising_βc, ising_βc_3D, potts_beta_c,
+                     potts_βc, random_hotrg_tensor)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("TNR_GB300_LIB") or os.path.join(HERE, "libtnr_gb300.so")
 
-TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D = 1, 2, 3, 4
+TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG = 1, 2, 3, 4, 5
 PREC_F64, PREC_SPLIT = 0, 1
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "iteration cap reached",
           4: "CUDA error", 5: "admission refused", 6: "non-finite value", 7: "unsupported", 8: "no device"}
@@ -37,7 +37,8 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_timer_stop", "tnr_run_batch", "tnr_device_info", "tnr_version", "tnr_kernel_launches",
            "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm", "tnr_gemm_time",
            "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_poll",
-           "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes"]
+           "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes", "tnr_create_impurity_hotrg",
+           "tnr_finalize_impurity", "tnr_run_impurity"]
 
 
 class TNRError(RuntimeError):
@@ -73,6 +74,9 @@ def lib():
         "tnr_step": (I, [P, I]),
         "tnr_finalize": (I, [P, pd]),
         "tnr_run": (I, [P, I, I, I, pd, Z, pz]),
+        "tnr_create_impurity_hotrg": (I, [C.POINTER(P), pi64, pd, pd, pd, pd, C.c_void_p]),
+        "tnr_finalize_impurity": (I, [P, pd]),
+        "tnr_run_impurity": (I, [P, I, I, I, pd, Z, pz]),
         "tnr_free_energy": (D, [pd, Z, D, D, D]),
         "tnr_get_tensor": (I, [P, pd, Z, pi64, C.POINTER(I)]),
         "tnr_singular_values": (I, [P, pd, Z, pz, C.POINTER(C.c_int32), Z, pz]),
@@ -274,6 +278,33 @@ class HOTRG_3D(_Scheme):
     scalefactor = 8.0
 
 
+class ImpurityHOTRG(_Scheme):
+    """``ImpurityHOTRG(T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)``
+    (src/schemes/impurityhotrg.jl:25-84): four tensors of the same spaces; ``run`` returns
+    the (pure, +1, -1, second-order) norm tuples of finalize!(::ImpurityHOTRG)."""
+    kind = TNR_IMPURITY_HOTRG
+    scalefactor = 4.0
+
+    def __init__(self, T, T_imp_order1_1, T_imp_order1_2, T_imp_order2, precision=PREC_F64, seed=0, stream=None):
+        arrs = [np.asfortranarray(np.asarray(_as_sym(t).array, dtype=np.float64))
+                for t in (T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)]
+        if any(a.ndim != 4 or a.shape != arrs[0].shape for a in arrs):
+            raise ValueError("ImpurityHOTRG needs four 4-leg tensors of the same dims")
+        L = lib()
+        o = Options()
+        L.tnr_default_options(C.byref(o))
+        o.precision = precision
+        o.seed = seed
+        o.stream = stream
+        dims = (C.c_int64 * 4)(*arrs[0].shape)
+        pp = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
+        h = C.c_void_p()
+        _check(L.tnr_create_impurity_hotrg(C.byref(h), dims, pp[0], pp[1], pp[2], pp[3], C.byref(o)))
+        self._h = h
+        self.precision = precision
+        self.symmetry_n = 1
+
+
 def step(scheme, trunc):
     """``step!(scheme, truncrank(chi))``"""
     _check(lib().tnr_step(scheme._h, int(trunc.howmany)), scheme._h)
@@ -281,7 +312,11 @@ def step(scheme, trunc):
 
 
 def finalize(scheme):
-    """``finalize!(scheme)``: trace norm n, T /= n; returns n."""
+    """``finalize!(scheme)``: trace norm n, T /= n; returns n (ImpurityHOTRG: the four norms)."""
+    if isinstance(scheme, ImpurityHOTRG):
+        out = np.empty(4)
+        _check(lib().tnr_finalize_impurity(scheme._h, out.ctypes.data_as(C.POINTER(C.c_double))), scheme._h)
+        return tuple(out)
     n = C.c_double()
     _check(lib().tnr_finalize(scheme._h, C.byref(n)), scheme._h)
     return n.value
@@ -295,6 +330,12 @@ def run(scheme, trunc, crit, finalize_beginning=True, verbosity=0):
         raise TypeError("only maxiter(n) runs on the device path")
     nsteps = max(crit.n, 1)
     cap = nsteps + 1
+    if isinstance(scheme, ImpurityHOTRG):
+        out = np.empty(4 * cap)
+        n = C.c_size_t()
+        _check(lib().tnr_run_impurity(scheme._h, int(trunc.howmany), int(crit.n), 1 if finalize_beginning else 0,
+                                      out.ctypes.data_as(C.POINTER(C.c_double)), out.size, C.byref(n)), scheme._h)
+        return [tuple(out[4 * i:4 * i + 4]) for i in range(n.value)]
     out = np.empty(cap)
     n = C.c_size_t()
     _check(lib().tnr_run(scheme._h, int(trunc.howmany), int(crit.n), 1 if finalize_beginning else 0,

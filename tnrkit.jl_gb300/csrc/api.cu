@@ -147,6 +147,66 @@ int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
     return create_common(out, kind, nlegs, dims, data, true, opts);
 }
 
+int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double* T, const double* T11,
+                              const double* T12, const double* T2, const tnr_options* opts) {
+    if (!out) return fail(nullptr, TNR_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (!dims || !T || !T11 || !T12 || !T2) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL tensor or dims");
+    for (int l = 0; l < 4; ++l)
+        if (dims[l] < 1) return fail(nullptr, TNR_ERR_INVALID_ARG, "leg dimension < 1");
+    if (dims[0] != dims[3] || dims[1] != dims[2])
+        return fail(nullptr, TNR_ERR_INVALID_ARG, "ImpurityHOTRG needs d1 == d4 and d2 == d3");
+    tnr_handle h = nullptr;
+    int st = create_common(&h, TNR_HOTRG, 4, dims, T, false, opts);
+    if (st != TNR_OK) return st;
+    st = guarded(h, [&] {
+        Scheme& s = h->s;
+        const int64_t n = dims[0] * dims[1] * dims[2] * dims[3];
+        const double* src[3] = {T11, T12, T2};
+        DT* dst[3] = {&s.I11, &s.I12, &s.I2};
+        for (int i = 0; i < 3; ++i) {
+            for (int64_t e = 0; e < n; ++e)
+                TNR_REQUIRE(std::isfinite(src[i][e]), TNR_ERR_NONFINITE, "non-finite entry in an impurity tensor");
+            *dst[i] = make_dt(s.ctx->pool.get(), {dims[0], dims[1], dims[2], dims[3]});
+            TNR_CUDA(cudaMemcpyAsync(dst[i]->p(), src[i], n * sizeof(double), cudaMemcpyHostToDevice, s.ctx->stream));
+        }
+        s.kind = TNR_IMPURITY_HOTRG;
+        s.ctx->sync();
+    });
+    if (st != TNR_OK) {
+        tnr_destroy(h);
+        return st;
+    }
+    *out = h;
+    return TNR_OK;
+}
+
+int tnr_finalize_impurity(tnr_handle h, double* norms4_out) {
+    if (!h || !norms4_out) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        TNR_REQUIRE(s.kind == TNR_IMPURITY_HOTRG, TNR_ERR_INVALID_ARG, "not an ImpurityHOTRG handle");
+        Buf d4(s.ctx->pool.get(), 4 * sizeof(double));
+        s.finalize_impurity_async(d4.d());
+        TNR_CUDA(cudaMemcpyAsync(norms4_out, d4.d(), 4 * sizeof(double), cudaMemcpyDeviceToHost, s.ctx->stream));
+        s.ctx->sync();
+        for (int i = 0; i < 4; ++i)
+            TNR_REQUIRE(std::isfinite(norms4_out[i]), TNR_ERR_NONFINITE, "finalize!: non-finite norm");
+    });
+}
+
+int tnr_run_impurity(tnr_handle h, int chi, int maxiter, int finalize_beginning, double* norms_out, size_t cap,
+                     size_t* n_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        const size_t need = 4 * ((size_t)std::max(maxiter, 1) + (finalize_beginning ? 1 : 0));
+        TNR_REQUIRE(norms_out && cap >= need, TNR_ERR_INVALID_ARG, "norms_out too small for run!");
+        std::vector<double> v = h->s.run_impurity(chi, maxiter, finalize_beginning != 0);
+        std::memcpy(norms_out, v.data(), v.size() * sizeof(double));
+        if (n_out) *n_out = v.size() / 4;
+    });
+}
+
 int tnr_step(tnr_handle h, int chi) {
     if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
     return guarded(h, [&] { h->s.step(chi); });

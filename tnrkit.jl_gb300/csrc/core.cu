@@ -511,6 +511,16 @@ void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r, in
     check_launch("polar_coeff");
 }
 
+__global__ void k_lincomb2(double* out, int64_t n, double a, const double* x, double b, const double* y) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        out[e] = a * x[e] + b * y[e];
+}
+void lincomb2(Ctx& c, double* out, int64_t n, double a, const double* x, double b, const double* y) {
+    if (!n) return;
+    k_lincomb2<<<grid_for(n, 256), 256, 0, c.stream>>>(out, n, a, x, b, y);
+    check_launch("lincomb2");
+}
+
 __global__ void k_row_scale_batched(double* X, int64_t k, int64_t n_total, const double* s, int mode, int64_t n_per) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * n_total;
          e += (int64_t)gridDim.x * blockDim.x) {

@@ -195,18 +195,18 @@ static DT hotrg_yproj(Scheme& s, const DT& T, int chi) {
 //   T'[a,b,g,d] = Ux[i,j,a] Ux[k,l,d] A2[i,e,g,k] A1[j,b,e,l]
 // as W2[b,l,e,i,a] = A1p[j,(b,l,e)] Uxp[j,(i,a)];  V[b,l,k,g,a] = W2[(b,l),(e,i)] A2p[(e,i),(k,g)] per a;
 //    O[b,d,g,a] = V[b,(l,k)] Uxq[(l,k),d] per (g,a);  T' = O permuted (a,b,g,d).
-static void hotrg_step_y(Scheme& s, const DT& Ux) {
-    Ctx& c = *s.ctx;
-    const DT& T = s.T;
-    const int64_t dL = T.d[0], dD = T.d[1], dU = T.d[2], dR = T.d[3], kx = Ux.d[2];
+// (A1 and A2 of equal dims: the pure tensor twice for HOTRG, impurity pairs for ImpurityHOTRG)
+static DT hotrg_step_y2(Ctx& c, const DT& A1, const DT& A2, const DT& Ux) {
+    const int64_t dL = A1.d[0], dD = A1.d[1], dU = A1.d[2], dR = A1.d[3], kx = Ux.d[2];
     TNR_REQUIRE(Ux.d[0] == dL && Ux.d[1] == dL && dL == dR && dD == dU, TNR_ERR_INVALID_ARG, "HOTRG y-step dims");
-    DT A1p = permuted(c, T, {0, 1, 3, 2});          // [j,b,l,e]
+    for (int l = 0; l < 4; ++l) TNR_REQUIRE(A2.d[l] == A1.d[l], TNR_ERR_INVALID_ARG, "HOTRG y-step: A1/A2 dims differ");
+    DT A1p = permuted(c, A1, {0, 1, 3, 2});         // [j,b,l,e]
     DT Uxp = permuted(c, Ux, {1, 0, 2});            // [j,i,a]
     const int64_t mW = dD * dR * dU, nW = dL * kx;
     DT W2 = make_dt(c.pool.get(), {dD, dR, dU, dL, kx});
     gemm_bulk(c, true, false, mW, nW, dL, 1.0, A1p.p(), dL, 0, Uxp.p(), dL, 0, 0.0, W2.p(), mW, 0, 1, true);
     A1p = DT(); Uxp = DT();
-    DT A2p = permuted(c, T, {1, 0, 3, 2});          // [e,i,k,g]
+    DT A2p = permuted(c, A2, {1, 0, 3, 2});         // [e,i,k,g]
     DT V = make_dt(c.pool.get(), {dD, dR, dR, dU, kx});
     {
         Batch2 bt;
@@ -228,19 +228,20 @@ static void hotrg_step_y(Scheme& s, const DT& Ux) {
         gemm_bulk(c, false, false, dD, kx, dR * dR, 1.0, V.p(), dD, Uxq.p(), dR * dR, 0.0, O.p(), dD, bt, true);
     }
     V = DT();
-    s.T = permuted(c, O, {3, 0, 2, 1});
+    return permuted(c, O, {3, 0, 2, 1});
 }
+
+static void hotrg_step_y(Scheme& s, const DT& Ux) { s.T = hotrg_step_y2(*s.ctx, s.T, s.T, Ux); }
 
 // _step_hotrg_x (src/schemes/hotrg.jl:62-80):
 //   T'[a,b,c,d] = A1[a,i,k,e] A2[e,j,l,d] Uy[i,j,b] Uy[k,l,c]
 // as W[a,k,e,j,b] = A1p[(a,k,e),i] Uy[i,(j,b)];  V[a,k,l,d,b] = W[(a,k),(e,j)] A2[(e,j),(l,d)] per b;
 //    T'[a,b,c,d] = V[a,(k,l)] Uy[(k,l),c] per (d,b), written in place (ldc = dL*ky).
-static void hotrg_step_x(Scheme& s, const DT& Uy) {
-    Ctx& c = *s.ctx;
-    const DT& T = s.T;
-    const int64_t dL = T.d[0], dD = T.d[1], dU = T.d[2], dR = T.d[3], ky = Uy.d[2];
+static DT hotrg_step_x2(Ctx& c, const DT& A1, const DT& A2, const DT& Uy) {
+    const int64_t dL = A1.d[0], dD = A1.d[1], dU = A1.d[2], dR = A1.d[3], ky = Uy.d[2];
     TNR_REQUIRE(Uy.d[0] == dD && Uy.d[1] == dD && dL == dR && dD == dU, TNR_ERR_INVALID_ARG, "HOTRG x-step dims");
-    DT A1p = permuted(c, T, {0, 2, 3, 1});          // [a,k,e,i]
+    for (int l = 0; l < 4; ++l) TNR_REQUIRE(A2.d[l] == A1.d[l], TNR_ERR_INVALID_ARG, "HOTRG x-step: A1/A2 dims differ");
+    DT A1p = permuted(c, A1, {0, 2, 3, 1});         // [a,k,e,i]
     const int64_t mW = dL * dU * dR;
     DT W = make_dt(c.pool.get(), {dL, dU, dR, dD, ky});
     gemm_bulk(c, false, false, mW, dD * ky, dD, 1.0, A1p.p(), mW, 0, Uy.p(), dD, 0, 0.0, W.p(), mW, 0, 1, true);
@@ -251,7 +252,7 @@ static void hotrg_step_x(Scheme& s, const DT& Uy) {
         bt.n1 = (int)ky;
         bt.sA1 = dL * dU * dR * dD;
         bt.sC1 = dL * dU * dU * dR;
-        gemm_bulk(c, false, false, dL * dU, dU * dR, dR * dD, 1.0, W.p(), dL * dU, T.p(), dR * dD, 0.0, V.p(),
+        gemm_bulk(c, false, false, dL * dU, dU * dR, dR * dD, 1.0, W.p(), dL * dU, A2.p(), dR * dD, 0.0, V.p(),
                   dL * dU, bt, true);
     }
     W = DT();
@@ -266,8 +267,10 @@ static void hotrg_step_x(Scheme& s, const DT& Uy) {
         bt.sC2 = dL;
         gemm_bulk(c, false, false, dL, ky, dU * dU, 1.0, V.p(), dL, Uy.p(), dU * dU, 0.0, Tn.p(), dL * ky, bt, true);
     }
-    s.T = std::move(Tn);
+    return Tn;
 }
+
+static void hotrg_step_x(Scheme& s, const DT& Uy) { s.T = hotrg_step_x2(*s.ctx, s.T, s.T, Uy); }
 
 // step!(::HOTRG) (src/schemes/hotrg.jl:154-160)
 static void step_hotrg(Scheme& s, int chi) {
@@ -275,6 +278,35 @@ static void step_hotrg(Scheme& s, int chi) {
     hotrg_step_y(s, Ux);
     DT Uy = hotrg_yproj(s, s.T, chi);
     hotrg_step_x(s, Uy);
+}
+
+// step!(::ImpurityHOTRG) (src/schemes/impurityhotrg.jl:46-84): the y projector of the pure
+// tensor with x-steps of the pure / impurity pairs, then the x projector with y-steps;
+// first-order impurities average the two placements, the second order the four
+static void step_impurity_hotrg(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    for (int half = 0; half < 2; ++half) {
+        const DT U = half == 0 ? hotrg_yproj(s, s.T, chi) : hotrg_xproj(s, s.T, chi);
+        auto st = [&](const DT& A1, const DT& A2) {
+            return half == 0 ? hotrg_step_x2(c, A1, A2, U) : hotrg_step_y2(c, A1, A2, U);
+        };
+        auto mix = [&](DT a, const DT& b, double w) {     // w a + w b, into a
+            lincomb2(c, a.p(), a.size(), w, a.p(), w, b.p());
+            return a;
+        };
+        DT T = st(s.T, s.T);
+        DT I11 = mix(st(s.I11, s.T), st(s.T, s.I11), 0.5);
+        DT I12 = mix(st(s.I12, s.T), st(s.T, s.I12), 0.5);
+        DT I2 = mix(st(s.I2, s.T), st(s.T, s.I2), 0.25);
+        {
+            DT cross = mix(st(s.I11, s.I12), st(s.I12, s.I11), 0.25);
+            lincomb2(c, I2.p(), I2.size(), 1.0, I2.p(), 1.0, cross.p());
+        }
+        s.T = std::move(T);
+        s.I11 = std::move(I11);
+        s.I12 = std::move(I12);
+        s.I2 = std::move(I2);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -388,6 +420,7 @@ void Scheme::step(int chi) {
         case TNR_BTRG: step_btrg(*this, chi); break;
         case TNR_HOTRG: step_hotrg(*this, chi); break;
         case TNR_HOTRG_3D: step_hotrg3d(*this, chi); break;
+        case TNR_IMPURITY_HOTRG: step_impurity_hotrg(*this, chi); break;
         default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
     }
     ++steps;
@@ -396,6 +429,13 @@ void Scheme::step(int chi) {
 // finalize! (src/utility/finalize.jl:4-14,62-66): norm into *d_norm, T /= norm
 void Scheme::finalize_async(double* d_norm) {
     Ctx& c = *ctx;
+    if (kind == TNR_IMPURITY_HOTRG) {
+        // the pure norm; the impurity norms go to scratch (run_impurity reads all four)
+        Buf d4(c.pool.get(), 4 * sizeof(double));
+        finalize_impurity_async(d4.d());
+        copy_f64(c, d_norm, d4.d(), 1);
+        return;
+    }
     switch (kind) {
         case TNR_TRG:
         case TNR_HOTRG: trace2d(c, T.p(), T.d, d_norm); break;
@@ -404,6 +444,33 @@ void Scheme::finalize_async(double* d_norm) {
         default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
     }
     scale_inplace(c, T.p(), T.size(), d_norm);
+}
+
+// finalize!(::ImpurityHOTRG) (src/utility/finalize.jl:91-101)
+void Scheme::finalize_impurity_async(double* d4) {
+    Ctx& c = *ctx;
+    const DT* ts[4] = {&T, &I11, &I12, &I2};
+    for (int i = 0; i < 4; ++i) trace2d(c, ts[i]->p(), ts[i]->d, d4 + i);
+    for (int i = 0; i < 4; ++i) scale_inplace(c, ts[i]->p(), ts[i]->size(), d4);
+}
+
+std::vector<double> Scheme::run_impurity(int chi, int maxiter, bool finalize_beginning) {
+    Ctx& c = *ctx;
+    TNR_REQUIRE(kind == TNR_IMPURITY_HOTRG, TNR_ERR_INVALID_ARG, "run_impurity needs an ImpurityHOTRG handle");
+    const int nsteps = std::max(maxiter, 1);
+    const int nn = nsteps + (finalize_beginning ? 1 : 0);
+    Buf norms(c.pool.get(), (size_t)nn * 4 * sizeof(double));
+    int at = 0;
+    if (finalize_beginning) finalize_impurity_async(norms.d() + 4 * (at++));
+    for (int i = 0; i < nsteps; ++i) {
+        step(chi);
+        finalize_impurity_async(norms.d() + 4 * (at++));
+    }
+    check_finite(c, norms.d(), 4 * (int64_t)nn);
+    std::vector<double> h = dvec_to_host(c, norms.d(), 4 * nn);
+    int st = c.read_status_and_clear();
+    TNR_REQUIRE(!(st & ST_NONFINITE), TNR_ERR_NONFINITE, "run!: non-finite norm");
+    return h;
 }
 
 double Scheme::finalize() {

@@ -36,6 +36,7 @@ struct Scheme {
     std::unique_ptr<Ctx> ctx;
     DT T;
     DT S1, S2;                     // BTRG diagonal bond tensors
+    DT I11, I12, I2;               // ImpurityHOTRG: +1 / -1 first-order and second-order impurity tensors
     double btrg_k = -0.5;
     int64_t steps = 0;
     int64_t max_slice_entries = int64_t(1) << 31;   // HOTRG_3D slicing budget (entries)
@@ -48,6 +49,10 @@ struct Scheme {
     void finalize_async(double* d_norm);
     double finalize();
     std::vector<double> run(int chi, int maxiter, bool finalize_beginning);
+    // ImpurityHOTRG: the four trace norms (pure, +1, -1, second order) into d4[0..3]; every
+    // tensor is divided by the pure norm
+    void finalize_impurity_async(double* d4);
+    std::vector<double> run_impurity(int chi, int maxiter, bool finalize_beginning);   // 4 per entry
     void record(const TsvdOut& r);
 };
 

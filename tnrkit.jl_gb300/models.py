@@ -59,6 +59,17 @@ def classical_ising(symmetry="Z2", beta=ising_βc, h=0.0):
     return SymTensor(np.ascontiguousarray(a), _charges(2, 4, N), N)
 
 
+def classical_ising_impurity(beta=ising_βc, h=0.0):
+    """``classical_ising_impurity(Trivial, β; h)`` (ising.jl:87-102): the magnetisation impurity,
+    whose even-parity entries carry sinh(hβ) and odd-parity ones cosh(hβ)."""
+    x, y = math.cosh(beta), math.sinh(beta)
+    w = np.array([math.sqrt(x), math.sqrt(y)])
+    par = np.add.outer(np.add.outer(np.arange(2), np.arange(2)), np.add.outer(np.arange(2), np.arange(2))) % 2
+    init = np.where(par == 0, math.sinh(h * beta), math.cosh(h * beta))
+    a = 2.0 * init * w[:, None, None, None] * w[None, :, None, None] * w[None, None, :, None] * w[None, None, None, :]
+    return SymTensor(np.ascontiguousarray(a), None, 1)
+
+
 def classical_ising_3D(symmetry="Z2", beta=ising_βc_3D, J=1.0):
     """``classical_ising_3D(Z2Irrep, β; J)`` (ising.jl:149-165): legs D, U', N, E, S', W'."""
     x, y = math.cosh(beta * J), math.sinh(beta * J)
