@@ -425,6 +425,17 @@ class ImpurityHOTRG:
         self.T_imp_order2 = T_imp_order2.copy()
 
 
+class ImpurityTRG:
+    """src/schemes/impuritytrg.jl:37-59: the pure tensor and impurity tensors on the four
+    sites of a plaquette, all of the same spaces."""
+
+    def __init__(self, T: Tensor, T_imp1: Tensor, T_imp2: Tensor, T_imp3: Tensor, T_imp4: Tensor):
+        for t in (T_imp1, T_imp2, T_imp3, T_imp4):
+            assert t.a.shape == T.a.shape, "the impurities need the spaces of T"
+        self.T = T.copy()
+        self.T_imp = [t.copy() for t in (T_imp1, T_imp2, T_imp3, T_imp4)]
+
+
 def SVD12(T: Tensor, chi):
     """src/utility/projectors.jl:211-217: U*sqrt(s), sqrt(s)*V."""
     U, s, Vh, _, bq = svd_trunc(T, 2, chi)
@@ -444,6 +455,43 @@ def step_trg(scheme: TRG, chi):
     a, q, N = _ein('bpq,arp,rsc,sqd->abcd', D, B, C, A, path=[(0, 1), (0, 1), (0, 1)])
     scheme.T = Tensor(a, 2, q, N)
     scheme.svals += [s1, s2]
+
+
+def _trg_contract(D, B, C, A):
+    """T[-1 -2; -3 -4] := D[-2; 1 2] B[-1; 4 1] C[4 3; -3] A[3 2; -4] (src/schemes/trg.jl:98-99)"""
+    a, q, N = _ein('bpq,arp,rsc,sqd->abcd', D, B, C, A, path=[(0, 1), (0, 1), (0, 1)])
+    return Tensor(a, 2, q, N)
+
+
+def step_impurity_trg(scheme: ImpurityTRG, chi):
+    """src/schemes/impuritytrg.jl:63-91: SVD12 of sites 1 and 3 and the pure tensor, of
+    sites 2 and 4 and the pure tensor transposed ((2,4),(1,3)); five TRG contractions."""
+    tp = lambda t: permute(t, (1, 3, 0, 2), 2)       # noqa: E731
+    I1, I2, I3, I4 = scheme.T_imp
+    A1, B1, _ = SVD12(I1, chi)
+    C2, D2, _ = SVD12(tp(I2), chi)
+    A3, B3, _ = SVD12(I3, chi)
+    C4, D4, _ = SVD12(tp(I4), chi)
+    Ap, Bp, _ = SVD12(scheme.T, chi)
+    Cp, Dp, _ = SVD12(tp(scheme.T), chi)
+    scheme.T = _trg_contract(Dp, Bp, Cp, Ap)
+    scheme.T_imp = [_trg_contract(Dp, B1, C2, Ap), _trg_contract(D2, B3, Cp, Ap),
+                    _trg_contract(D4, Bp, Cp, A3), _trg_contract(Dp, Bp, C4, A1)]
+
+
+def finalize_impurity_trg(scheme: ImpurityTRG):
+    """src/utility/finalize.jl:75-88: every tensor /= the pure trace norm, then the norm of
+    the four impurities contracted around the plaquette
+    T_imp1[5 4; 6 1] T_imp2[1 2; 7 5] T_imp3[3 7; 2 8] T_imp4[8 6; 4 3]."""
+    npure = abs(np.einsum('abba->', scheme.T.a))
+    scheme.T.a = scheme.T.a / npure
+    for t in scheme.T_imp:
+        t.a = t.a / npure
+    t1, t2, t3, t4 = (t.a for t in scheme.T_imp)
+    x = np.einsum('edfa,abge->dfbg', t1, t2)
+    y = np.einsum('cgbh,hfdc->gbfd', t3, t4)
+    nimp = abs(np.einsum('dfbg,gbfd->', x, y))
+    return float(npure), float(nimp)
 
 
 def pseudopow(s, a, tol=EPS ** 0.75):
@@ -643,6 +691,8 @@ def step(scheme, chi):
         step_hotrg3d(scheme, chi)
     elif isinstance(scheme, ImpurityHOTRG):
         step_impurity_hotrg(scheme, chi)
+    elif isinstance(scheme, ImpurityTRG):
+        step_impurity_trg(scheme, chi)
     else:
         raise TypeError(type(scheme))
     return scheme
@@ -653,6 +703,8 @@ def finalize(scheme):
     tuple of four norms, src/utility/finalize.jl:91-101)."""
     if isinstance(scheme, ImpurityHOTRG):
         return finalize_impurity_hotrg(scheme)
+    if isinstance(scheme, ImpurityTRG):
+        return finalize_impurity_trg(scheme)
     T = scheme.T.a
     if isinstance(scheme, (TRG, HOTRG)):
         n = abs(np.einsum('abba->', T))                 # T[1 2; 2 1]

@@ -151,3 +151,28 @@ def test_impurity_hotrg_magnetisation_limits(oracle, beta, m2, tol):
         assert abs(got) <= tol
     else:
         assert got == pytest.approx(m2, rel=tol)
+
+
+def test_impurity_trg_onsager(oracle):
+    """test/schemes.jl:443-452: ImpurityTRG(T, T_imp, T, T, T) on the Ising model at beta_c,
+    truncrank(24), maxiter(25): the pure norms give Onsager's f to 2e-6 (sf 2)."""
+    o = oracle
+    T = o.classical_ising(o.ISING_BETA_C, "Trivial")
+    data = o.run(o.ImpurityTRG(T, o.classical_ising_impurity(), T, T, T), o.truncrank(24), o.maxiter(25))
+    assert len(data) == 26 and all(len(d) == 2 for d in data)
+    f = o.free_energy([d[0] for d in data], o.ISING_BETA_C)
+    assert f == pytest.approx(o.F_ONSAGER, rel=2e-6)
+
+
+@pytest.mark.parametrize("beta,h,m,tol", [(0.1, 0.0, 0.0, 1e-4), (2.0, 1e-6, 1.0, 1e-4)])
+def test_impurity_trg_magnetisation_limits(oracle, beta, h, m, tol):
+    """test/schemes.jl:454-480: <sigma> = n_imp / n_pure of the last step tends to 0 at high
+    temperature (atol 1e-4) and to 1 at low temperature in a tiny field (rtol 1e-4), chi 16."""
+    o = oracle
+    T = o.classical_ising(beta, "Trivial", h=h)
+    data = o.run(o.ImpurityTRG(T, o.classical_ising_impurity(beta, h=h), T, T, T), o.truncrank(16), o.maxiter(25))
+    got = data[-1][1] / data[-1][0]
+    if m == 0.0:
+        assert abs(got) <= tol
+    else:
+        assert got == pytest.approx(m, rel=tol)
