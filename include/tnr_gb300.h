@@ -44,6 +44,7 @@ extern "C" {
 #define TNR_HOTRG     3   /* hotrg.jl:27-160   */
 #define TNR_HOTRG_3D  4   /* hotrg3d.jl:27-135 */
 #define TNR_IMPURITY_HOTRG 5 /* impurityhotrg.jl:25-84; created by tnr_create_impurity_hotrg */
+#define TNR_IMPURITY_TRG   6 /* impuritytrg.jl:37-91; created by tnr_create_impurity_trg */
 
 /* ---- arithmetic of the bulk contractions -------------------------------- */
 #define TNR_PREC_F64    0  /* plain path: every operation in FP64                      */
@@ -84,9 +85,16 @@ int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
 int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double* T,
                               const double* T_imp_order1_1, const double* T_imp_order1_2,
                               const double* T_imp_order2, const tnr_options* opts);
-int tnr_finalize_impurity(tnr_handle h, double* norms4_out);
-/* run! with ImpurityHOTRG_Finalizer (tnrscheme.jl:28): 4 norms per entry (pure, +1, -1,
- * second order) into norms_out (cap doubles); *n_out = entries written. */
+/* ImpurityTRG(T, T_imp1, T_imp2, T_imp3, T_imp4) (impuritytrg.jl:37-59): five host tensors
+ * of the same dims; tnr_step steps all five (impuritytrg.jl:63-91). */
+int tnr_create_impurity_trg(tnr_handle* out, const int64_t* dims, const double* T, const double* T_imp1,
+                            const double* T_imp2, const double* T_imp3, const double* T_imp4,
+                            const tnr_options* opts);
+/* finalize! of an impurity scheme: ImpurityHOTRG writes 4 norms (pure, +1, -1, second order;
+ * finalize.jl:91-101), ImpurityTRG 2 (pure, plaquette of the four impurities; finalize.jl:75-88). */
+int tnr_finalize_impurity(tnr_handle h, double* norms_out);
+/* run! with ImpurityHOTRG_Finalizer / ImpurityTRG_Finalizer (tnrscheme.jl:27-28): 4 or 2 norms
+ * per entry into norms_out (cap doubles); *n_out = entries written. */
 int tnr_run_impurity(tnr_handle h, int chi, int maxiter, int finalize_beginning,
                      double* norms_out, size_t cap, size_t* n_out);
 

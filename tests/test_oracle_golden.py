@@ -176,3 +176,66 @@ def test_impurity_trg_magnetisation_limits(oracle, beta, h, m, tol):
         assert abs(got) <= tol
     else:
         assert got == pytest.approx(m, rel=tol)
+
+
+def test_impurity_trg_plaquette_depends_on_svd_signs(oracle, monkeypatch):
+    """The reference's ImpurityTRG contracts factors of an impurity's SVD12 with factors of
+    the pure tensor's (src/schemes/impuritytrg.jl:84-88), so its plaquette norm after a step
+    moves when an SVD flips the sign of a kept vector, while the pure norms and the
+    converged <sigma> = n_imp/n_pure do not.  Random sign flips in the oracle's SVD12 show
+    both: the GPU parity test holds the engine to the sign-free quantities only."""
+    o = oracle
+    beta, h = 0.5, 0.05
+    T, imp = o.classical_ising(beta, "Trivial", h=h), o.classical_ising_impurity(beta, h=h)
+    a = np.array(o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(3)))
+    svd12, rng = o.SVD12, np.random.default_rng(0)
+
+    def flipped(t, chi):
+        A, B, s = svd12(t, chi)
+        f = rng.choice([-1.0, 1.0], size=s.shape)
+        A.a = A.a * f
+        B.a = B.a * f[:, None, None]
+        return A, B, s
+
+    monkeypatch.setattr(o, "SVD12", flipped)
+    b = np.array(o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(3)))
+    np.testing.assert_allclose(b[:, 0], a[:, 0], rtol=1e-13)
+    assert b[0, 1] == pytest.approx(a[0, 1], rel=1e-13)
+    assert np.abs(b[1:, 1] / a[1:, 1] - 1).max() > 1e-3
+    T, imp = o.classical_ising(2.0, "Trivial", h=1e-6), o.classical_ising_impurity(2.0, h=1e-6)
+    b = o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(25))
+    monkeypatch.setattr(o, "SVD12", svd12)
+    a = o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(25))
+    assert b[-1][1] / b[-1][0] == pytest.approx(a[-1][1] / a[-1][0], rel=1e-10)
+
+
+def test_impurity_trg_high_temperature_needs_parity_pure_vectors(oracle, monkeypatch):
+    """The reference's high-temperature check (test/schemes.jl:454-467, |<sigma>| <= 1e-4 at
+    beta = 0.1) holds because LAPACK returns parity-pure singular vectors inside the
+    degenerate pairs of the Z2-odd impurity's SVD.  Any other orthonormal basis of those
+    pairs is an equally valid SVD, yet it mixes parities across sites of the plaquette and
+    leaves <sigma> at O(1e-2): random rotations inside every degenerate group show it."""
+    o = oracle
+    svd12, rng = o.SVD12, np.random.default_rng(0)
+
+    def rotated(t, chi):
+        A, B, s = svd12(t, chi)
+        Q, i = np.eye(len(s)), 0
+        while i < len(s):
+            j = i + 1
+            while j < len(s) and abs(s[j] - s[i]) <= 1e-10 * s[0]:
+                j += 1
+            if j - i > 1:
+                Q[i:j, i:j] = np.linalg.qr(rng.standard_normal((j - i, j - i)))[0]
+            i = j
+        A.a = np.einsum('abk,kl->abl', A.a, Q)
+        B.a = np.einsum('lk,kcd->lcd', Q.T, B.a)
+        return A, B, s
+
+    T, imp = o.classical_ising(0.1, "Trivial"), o.classical_ising_impurity(0.1)
+    a = o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(25))
+    monkeypatch.setattr(o, "SVD12", rotated)
+    b = o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(25))
+    np.testing.assert_allclose([x[0] for x in b], [x[0] for x in a], rtol=1e-10)
+    assert abs(a[-1][1] / a[-1][0]) <= 1e-4
+    assert max(abs(x[1] / x[0]) for x in b) > 1e-3

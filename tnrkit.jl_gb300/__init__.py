@@ -26,7 +26,7 @@ from .models import (SymTensor, classical_clock, classical_ising, classical_isin
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("TNR_GB300_LIB") or os.path.join(HERE, "libtnr_gb300.so")
 
-TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG = 1, 2, 3, 4, 5
+TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG = 1, 2, 3, 4, 5, 6
 PREC_F64, PREC_SPLIT = 0, 1
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "iteration cap reached",
           4: "CUDA error", 5: "admission refused", 6: "non-finite value", 7: "unsupported", 8: "no device"}
@@ -38,7 +38,7 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm", "tnr_gemm_time",
            "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_poll",
            "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes", "tnr_create_impurity_hotrg",
-           "tnr_finalize_impurity", "tnr_run_impurity"]
+           "tnr_create_impurity_trg", "tnr_finalize_impurity", "tnr_run_impurity"]
 
 
 class TNRError(RuntimeError):
@@ -75,6 +75,7 @@ def lib():
         "tnr_finalize": (I, [P, pd]),
         "tnr_run": (I, [P, I, I, I, pd, Z, pz]),
         "tnr_create_impurity_hotrg": (I, [C.POINTER(P), pi64, pd, pd, pd, pd, C.c_void_p]),
+        "tnr_create_impurity_trg": (I, [C.POINTER(P), pi64, pd, pd, pd, pd, pd, C.c_void_p]),
         "tnr_finalize_impurity": (I, [P, pd]),
         "tnr_run_impurity": (I, [P, I, I, I, pd, Z, pz]),
         "tnr_free_energy": (D, [pd, Z, D, D, D]),
@@ -278,18 +279,16 @@ class HOTRG_3D(_Scheme):
     scalefactor = 8.0
 
 
-class ImpurityHOTRG(_Scheme):
-    """``ImpurityHOTRG(T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)``
-    (src/schemes/impurityhotrg.jl:25-84): four tensors of the same spaces; ``run`` returns
-    the (pure, +1, -1, second-order) norm tuples of finalize!(::ImpurityHOTRG)."""
-    kind = TNR_IMPURITY_HOTRG
-    scalefactor = 4.0
+class _ImpurityScheme(_Scheme):
+    """A pure tensor and impurity tensors of the same spaces, stepped together on the device;
+    finalize!/run! return a tuple of ``norms`` norms per entry."""
+    norms = 1
+    _create = ""
 
-    def __init__(self, T, T_imp_order1_1, T_imp_order1_2, T_imp_order2, precision=PREC_F64, seed=0, stream=None):
-        arrs = [np.asfortranarray(np.asarray(_as_sym(t).array, dtype=np.float64))
-                for t in (T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)]
+    def _make(self, tensors, precision, seed, stream):
+        arrs = [np.asfortranarray(np.asarray(_as_sym(t).array, dtype=np.float64)) for t in tensors]
         if any(a.ndim != 4 or a.shape != arrs[0].shape for a in arrs):
-            raise ValueError("ImpurityHOTRG needs four 4-leg tensors of the same dims")
+            raise ValueError(f"{type(self).__name__} needs {len(arrs)} 4-leg tensors of the same dims")
         L = lib()
         o = Options()
         L.tnr_default_options(C.byref(o))
@@ -299,10 +298,36 @@ class ImpurityHOTRG(_Scheme):
         dims = (C.c_int64 * 4)(*arrs[0].shape)
         pp = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
         h = C.c_void_p()
-        _check(L.tnr_create_impurity_hotrg(C.byref(h), dims, pp[0], pp[1], pp[2], pp[3], C.byref(o)))
+        _check(getattr(L, self._create)(C.byref(h), dims, *pp, C.byref(o)))
         self._h = h
         self.precision = precision
         self.symmetry_n = 1
+
+
+class ImpurityHOTRG(_ImpurityScheme):
+    """``ImpurityHOTRG(T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)``
+    (src/schemes/impurityhotrg.jl:25-84): four tensors of the same spaces; ``run`` returns
+    the (pure, +1, -1, second-order) norm tuples of finalize!(::ImpurityHOTRG)."""
+    kind = TNR_IMPURITY_HOTRG
+    scalefactor = 4.0
+    norms = 4
+    _create = "tnr_create_impurity_hotrg"
+
+    def __init__(self, T, T_imp_order1_1, T_imp_order1_2, T_imp_order2, precision=PREC_F64, seed=0, stream=None):
+        self._make((T, T_imp_order1_1, T_imp_order1_2, T_imp_order2), precision, seed, stream)
+
+
+class ImpurityTRG(_ImpurityScheme):
+    """``ImpurityTRG(T, T_imp1, T_imp2, T_imp3, T_imp4)`` (src/schemes/impuritytrg.jl:37-59):
+    the pure tensor and the four sites of an impurity plaquette; ``run`` returns the
+    (pure, plaquette) norm tuples of finalize!(::ImpurityTRG) (src/utility/finalize.jl:75-88)."""
+    kind = TNR_IMPURITY_TRG
+    scalefactor = 2.0
+    norms = 2
+    _create = "tnr_create_impurity_trg"
+
+    def __init__(self, T, T_imp1, T_imp2, T_imp3, T_imp4, precision=PREC_F64, seed=0, stream=None):
+        self._make((T, T_imp1, T_imp2, T_imp3, T_imp4), precision, seed, stream)
 
 
 def step(scheme, trunc):
@@ -312,9 +337,9 @@ def step(scheme, trunc):
 
 
 def finalize(scheme):
-    """``finalize!(scheme)``: trace norm n, T /= n; returns n (ImpurityHOTRG: the four norms)."""
-    if isinstance(scheme, ImpurityHOTRG):
-        out = np.empty(4)
+    """``finalize!(scheme)``: trace norm n, T /= n; returns n (impurity schemes: a tuple of norms)."""
+    if isinstance(scheme, _ImpurityScheme):
+        out = np.empty(scheme.norms)
         _check(lib().tnr_finalize_impurity(scheme._h, out.ctypes.data_as(C.POINTER(C.c_double))), scheme._h)
         return tuple(out)
     n = C.c_double()
@@ -330,12 +355,13 @@ def run(scheme, trunc, crit, finalize_beginning=True, verbosity=0):
         raise TypeError("only maxiter(n) runs on the device path")
     nsteps = max(crit.n, 1)
     cap = nsteps + 1
-    if isinstance(scheme, ImpurityHOTRG):
-        out = np.empty(4 * cap)
+    if isinstance(scheme, _ImpurityScheme):
+        k = scheme.norms
+        out = np.empty(k * cap)
         n = C.c_size_t()
         _check(lib().tnr_run_impurity(scheme._h, int(trunc.howmany), int(crit.n), 1 if finalize_beginning else 0,
                                       out.ctypes.data_as(C.POINTER(C.c_double)), out.size, C.byref(n)), scheme._h)
-        return [tuple(out[4 * i:4 * i + 4]) for i in range(n.value)]
+        return [tuple(out[k * i:k * i + k]) for i in range(n.value)]
     out = np.empty(cap)
     n = C.c_size_t()
     _check(lib().tnr_run(scheme._h, int(trunc.howmany), int(crit.n), 1 if finalize_beginning else 0,

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -147,30 +148,35 @@ int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
     return create_common(out, kind, nlegs, dims, data, true, opts);
 }
 
-int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double* T, const double* T11,
-                              const double* T12, const double* T2, const tnr_options* opts) {
+// A scheme holding impurity tensors beside the pure one: all share the pure tensor's dims
+static int create_impurity(tnr_handle* out, int kind, const char* name, const int64_t* dims, const double* T,
+                           std::initializer_list<const double*> imps, const tnr_options* opts) {
     if (!out) return fail(nullptr, TNR_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
-    if (!dims || !T || !T11 || !T12 || !T2) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL tensor or dims");
+    bool null_arg = !dims || !T;
+    for (const double* p : imps) null_arg = null_arg || !p;
+    if (null_arg) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL tensor or dims");
     for (int l = 0; l < 4; ++l)
         if (dims[l] < 1) return fail(nullptr, TNR_ERR_INVALID_ARG, "leg dimension < 1");
     if (dims[0] != dims[3] || dims[1] != dims[2])
-        return fail(nullptr, TNR_ERR_INVALID_ARG, "ImpurityHOTRG needs d1 == d4 and d2 == d3");
+        return fail(nullptr, TNR_ERR_INVALID_ARG, std::string(name) + " needs d1 == d4 and d2 == d3");
     tnr_handle h = nullptr;
-    int st = create_common(&h, TNR_HOTRG, 4, dims, T, false, opts);
+    int st = create_common(&h, kind == TNR_IMPURITY_HOTRG ? TNR_HOTRG : TNR_TRG, 4, dims, T, false, opts);
     if (st != TNR_OK) return st;
     st = guarded(h, [&] {
         Scheme& s = h->s;
         const int64_t n = dims[0] * dims[1] * dims[2] * dims[3];
-        const double* src[3] = {T11, T12, T2};
-        DT* dst[3] = {&s.I11, &s.I12, &s.I2};
-        for (int i = 0; i < 3; ++i) {
+        DT* hotrg_dst[3] = {&s.I11, &s.I12, &s.I2};
+        int i = 0;
+        for (const double* src : imps) {
             for (int64_t e = 0; e < n; ++e)
-                TNR_REQUIRE(std::isfinite(src[i][e]), TNR_ERR_NONFINITE, "non-finite entry in an impurity tensor");
-            *dst[i] = make_dt(s.ctx->pool.get(), {dims[0], dims[1], dims[2], dims[3]});
-            TNR_CUDA(cudaMemcpyAsync(dst[i]->p(), src[i], n * sizeof(double), cudaMemcpyHostToDevice, s.ctx->stream));
+                TNR_REQUIRE(std::isfinite(src[e]), TNR_ERR_NONFINITE, "non-finite entry in an impurity tensor");
+            DT& dst = kind == TNR_IMPURITY_HOTRG ? *hotrg_dst[i] : s.site[i];
+            dst = make_dt(s.ctx->pool.get(), {dims[0], dims[1], dims[2], dims[3]});
+            TNR_CUDA(cudaMemcpyAsync(dst.p(), src, n * sizeof(double), cudaMemcpyHostToDevice, s.ctx->stream));
+            ++i;
         }
-        s.kind = TNR_IMPURITY_HOTRG;
+        s.kind = kind;
         s.ctx->sync();
     });
     if (st != TNR_OK) {
@@ -181,17 +187,29 @@ int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double
     return TNR_OK;
 }
 
-int tnr_finalize_impurity(tnr_handle h, double* norms4_out) {
-    if (!h || !norms4_out) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
+int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double* T, const double* T11,
+                              const double* T12, const double* T2, const tnr_options* opts) {
+    return create_impurity(out, TNR_IMPURITY_HOTRG, "ImpurityHOTRG", dims, T, {T11, T12, T2}, opts);
+}
+
+int tnr_create_impurity_trg(tnr_handle* out, const int64_t* dims, const double* T, const double* T_imp1,
+                            const double* T_imp2, const double* T_imp3, const double* T_imp4,
+                            const tnr_options* opts) {
+    return create_impurity(out, TNR_IMPURITY_TRG, "ImpurityTRG", dims, T, {T_imp1, T_imp2, T_imp3, T_imp4}, opts);
+}
+
+int tnr_finalize_impurity(tnr_handle h, double* norms_out) {
+    if (!h || !norms_out) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
     return guarded(h, [&] {
         Scheme& s = h->s;
-        TNR_REQUIRE(s.kind == TNR_IMPURITY_HOTRG, TNR_ERR_INVALID_ARG, "not an ImpurityHOTRG handle");
-        Buf d4(s.ctx->pool.get(), 4 * sizeof(double));
-        s.finalize_impurity_async(d4.d());
-        TNR_CUDA(cudaMemcpyAsync(norms4_out, d4.d(), 4 * sizeof(double), cudaMemcpyDeviceToHost, s.ctx->stream));
+        const int np = s.norms_per_entry();
+        TNR_REQUIRE(np > 1, TNR_ERR_INVALID_ARG, "not an impurity scheme handle");
+        Buf d(s.ctx->pool.get(), 4 * sizeof(double));
+        s.finalize_multi_async(d.d());
+        TNR_CUDA(cudaMemcpyAsync(norms_out, d.d(), np * sizeof(double), cudaMemcpyDeviceToHost, s.ctx->stream));
         s.ctx->sync();
-        for (int i = 0; i < 4; ++i)
-            TNR_REQUIRE(std::isfinite(norms4_out[i]), TNR_ERR_NONFINITE, "finalize!: non-finite norm");
+        for (int i = 0; i < np; ++i)
+            TNR_REQUIRE(std::isfinite(norms_out[i]), TNR_ERR_NONFINITE, "finalize!: non-finite norm");
     });
 }
 
@@ -199,11 +217,13 @@ int tnr_run_impurity(tnr_handle h, int chi, int maxiter, int finalize_beginning,
                      size_t* n_out) {
     if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
     return guarded(h, [&] {
-        const size_t need = 4 * ((size_t)std::max(maxiter, 1) + (finalize_beginning ? 1 : 0));
+        const size_t np = (size_t)h->s.norms_per_entry();
+        TNR_REQUIRE(np > 1, TNR_ERR_INVALID_ARG, "not an impurity scheme handle");
+        const size_t need = np * ((size_t)std::max(maxiter, 1) + (finalize_beginning ? 1 : 0));
         TNR_REQUIRE(norms_out && cap >= need, TNR_ERR_INVALID_ARG, "norms_out too small for run!");
         std::vector<double> v = h->s.run_impurity(chi, maxiter, finalize_beginning != 0);
         std::memcpy(norms_out, v.data(), v.size() * sizeof(double));
-        if (n_out) *n_out = v.size() / 4;
+        if (n_out) *n_out = v.size() / np;
     });
 }
 

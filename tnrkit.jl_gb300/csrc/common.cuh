@@ -267,6 +267,8 @@ void sum_squares(Ctx& c, const double* x, int64_t n, double* out);
 void scale_inplace(Ctx& c, double* x, int64_t n, const double* inv_scale_ptr);
 void fill_identity(Ctx& c, double* x, int64_t m, int64_t n);
 void copy_f64(Ctx& c, double* dst, const double* src, int64_t n);
+// dst[0] = |src[0]|
+void abs_copy(Ctx& c, double* dst, const double* src);
 // out[i] = a x[i] + b y[i] (out may alias x or y)
 void lincomb2(Ctx& c, double* out, int64_t n, double a, const double* x, double b, const double* y);
 

@@ -511,6 +511,12 @@ void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r, in
     check_launch("polar_coeff");
 }
 
+__global__ void k_abs_copy(double* dst, const double* src) { dst[0] = fabs(src[0]); }
+void abs_copy(Ctx& c, double* dst, const double* src) {
+    k_abs_copy<<<1, 1, 0, c.stream>>>(dst, src);
+    check_launch("abs_copy");
+}
+
 __global__ void k_lincomb2(double* out, int64_t n, double a, const double* x, double b, const double* y) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
         out[e] = a * x[e] + b * y[e];

@@ -53,6 +53,14 @@ static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B) {
     s.record(r);
 }
 
+// T[-1 -2;-3 -4] = D[-2;1 2] B[-1;4 1] C[4 3;-3] A[3 2;-4]  (src/schemes/trg.jl:98-99)
+//   D[b,p,q] B[a,r,p] C[r,s,c] A[s,q,d]
+static DT trg_contract(Ctx& c, const DT& D, const DT& B, const DT& C, const DT& A) {
+    DT X = contract(c, D, {Lb, Lp, Lq}, B, {La, Lr, Lp}, {La, Lb, Lq, Lr});
+    DT Y = contract(c, C, {Lr, Ls, Lc}, A, {Ls, Lq, Ld}, {Lq, Lr, Lc, Ld});
+    return contract(c, X, {La, Lb, Lq, Lr}, Y, {Lq, Lr, Lc, Ld}, {La, Lb, Lc, Ld});
+}
+
 // step!(::TRG) (src/schemes/trg.jl:94-100)
 static void step_trg(Scheme& s, int chi) {
     Ctx& c = *s.ctx;
@@ -63,12 +71,37 @@ static void step_trg(Scheme& s, int chi) {
     DT Tp = permuted(c, T, {1, 3, 0, 2});           // transpose(T, ((2,4),(1,3)))
     svd12(s, Tp, chi, C, D);                        // C[i2,i4,k'], D[k',i1,i3]
     Tp = DT();
-    // T[-1 -2;-3 -4] = D[-2;1 2] B[-1;4 1] C[4 3;-3] A[3 2;-4]
-    //   D[b,p,q] B[a,r,p] C[r,s,c] A[s,q,d]
-    DT X = contract(c, D, {Lb, Lp, Lq}, B, {La, Lr, Lp}, {La, Lb, Lq, Lr});
-    DT Y = contract(c, C, {Lr, Ls, Lc}, A, {Ls, Lq, Ld}, {Lq, Lr, Lc, Ld});
-    A = DT(); B = DT(); C = DT(); D = DT();
-    s.T = contract(c, X, {La, Lb, Lq, Lr}, Y, {Lq, Lr, Lc, Ld}, {La, Lb, Lc, Ld});
+    s.T = trg_contract(c, D, B, C, A);
+}
+
+// step!(::ImpurityTRG) (src/schemes/impuritytrg.jl:63-91): SVD12 of sites 1 and 3 and of the
+// pure tensor, and of sites 2 and 4 and the pure tensor transposed ((2,4),(1,3)); the new
+// pure and site tensors are five TRG contractions of those factors
+static void step_impurity_trg(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    TNR_REQUIRE(s.T.d[0] == s.T.d[3] && s.T.d[1] == s.T.d[2], TNR_ERR_INVALID_ARG,
+                "ImpurityTRG needs d1 == d4 and d2 == d3");
+    auto svd_t = [&](const DT& t, DT& C, DT& D) {
+        DT tp = permuted(c, t, {1, 3, 0, 2});
+        svd12(s, tp, chi, C, D);
+    };
+    DT A1, B1, C2, D2, A3, B3, C4, D4, Ap, Bp, Cp, Dp;
+    svd12(s, s.site[0], chi, A1, B1);
+    svd_t(s.site[1], C2, D2);
+    svd12(s, s.site[2], chi, A3, B3);
+    svd_t(s.site[3], C4, D4);
+    svd12(s, s.T, chi, Ap, Bp);
+    svd_t(s.T, Cp, Dp);
+    DT T = trg_contract(c, Dp, Bp, Cp, Ap);
+    DT S1 = trg_contract(c, Dp, B1, C2, Ap);
+    DT S2 = trg_contract(c, D2, B3, Cp, Ap);
+    DT S3 = trg_contract(c, D4, Bp, Cp, A3);
+    DT S4 = trg_contract(c, Dp, Bp, C4, A1);
+    s.T = std::move(T);
+    s.site[0] = std::move(S1);
+    s.site[1] = std::move(S2);
+    s.site[2] = std::move(S3);
+    s.site[3] = std::move(S4);
 }
 
 // step!(::BTRG) (src/schemes/btrg.jl:166-200)
@@ -421,6 +454,7 @@ void Scheme::step(int chi) {
         case TNR_HOTRG: step_hotrg(*this, chi); break;
         case TNR_HOTRG_3D: step_hotrg3d(*this, chi); break;
         case TNR_IMPURITY_HOTRG: step_impurity_hotrg(*this, chi); break;
+        case TNR_IMPURITY_TRG: step_impurity_trg(*this, chi); break;
         default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
     }
     ++steps;
@@ -429,10 +463,10 @@ void Scheme::step(int chi) {
 // finalize! (src/utility/finalize.jl:4-14,62-66): norm into *d_norm, T /= norm
 void Scheme::finalize_async(double* d_norm) {
     Ctx& c = *ctx;
-    if (kind == TNR_IMPURITY_HOTRG) {
-        // the pure norm; the impurity norms go to scratch (run_impurity reads all four)
+    if (kind == TNR_IMPURITY_HOTRG || kind == TNR_IMPURITY_TRG) {
+        // the pure norm; the impurity norms go to scratch (run_impurity reads them all)
         Buf d4(c.pool.get(), 4 * sizeof(double));
-        finalize_impurity_async(d4.d());
+        finalize_multi_async(d4.d());
         copy_f64(c, d_norm, d4.d(), 1);
         return;
     }
@@ -454,20 +488,45 @@ void Scheme::finalize_impurity_async(double* d4) {
     for (int i = 0; i < 4; ++i) scale_inplace(c, ts[i]->p(), ts[i]->size(), d4);
 }
 
+// finalize!(::ImpurityTRG) (src/utility/finalize.jl:75-88): every tensor /= the pure trace
+// norm, then |T_imp1[5 4;6 1] T_imp2[1 2;7 5] T_imp3[3 7;2 8] T_imp4[8 6;4 3]|
+void Scheme::finalize_impurity_trg_async(double* d2) {
+    Ctx& c = *ctx;
+    trace2d(c, T.p(), T.d, d2);
+    scale_inplace(c, T.p(), T.size(), d2);
+    for (int i = 0; i < 4; ++i) scale_inplace(c, site[i].p(), site[i].size(), d2);
+    // labels 1..8 -> a..h; X[4,6,2,7] = T1[5,4,6,1] T2[1,2,7,5]; Y[7,2,6,4] = T3[3,7,2,8] T4[8,6,4,3]
+    DT X = contract(c, site[0], {Le, Ld, Lf, La}, site[1], {La, Lb, Lg, Le}, {Ld, Lf, Lb, Lg});
+    DT Y = contract(c, site[2], {Lc, Lg, Lb, Lh}, site[3], {Lh, Lf, Ld, Lc}, {Lg, Lb, Lf, Ld});
+    // the closing contraction over all four legs, as a 1 x 1 product (a unit leg on each side)
+    std::vector<int64_t> dx = X.dims(), dy = Y.dims();
+    dx.push_back(1);
+    dy.push_back(1);
+    DT Z = contract(c, X.p(), dx, {Ld, Lf, Lb, Lg, Lx}, Y.p(), dy, {Lg, Lb, Lf, Ld, Ly}, {Lx, Ly}, false);
+    abs_copy(c, d2 + 1, Z.p());
+}
+
+void Scheme::finalize_multi_async(double* d) {
+    if (kind == TNR_IMPURITY_HOTRG) finalize_impurity_async(d);
+    else if (kind == TNR_IMPURITY_TRG) finalize_impurity_trg_async(d);
+    else throw Error(TNR_ERR_INVALID_ARG, "not an impurity scheme");
+}
+
 std::vector<double> Scheme::run_impurity(int chi, int maxiter, bool finalize_beginning) {
     Ctx& c = *ctx;
-    TNR_REQUIRE(kind == TNR_IMPURITY_HOTRG, TNR_ERR_INVALID_ARG, "run_impurity needs an ImpurityHOTRG handle");
+    const int np = norms_per_entry();
+    TNR_REQUIRE(np > 1, TNR_ERR_INVALID_ARG, "run_impurity needs an impurity scheme handle");
     const int nsteps = std::max(maxiter, 1);
     const int nn = nsteps + (finalize_beginning ? 1 : 0);
-    Buf norms(c.pool.get(), (size_t)nn * 4 * sizeof(double));
+    Buf norms(c.pool.get(), (size_t)nn * np * sizeof(double));
     int at = 0;
-    if (finalize_beginning) finalize_impurity_async(norms.d() + 4 * (at++));
+    if (finalize_beginning) finalize_multi_async(norms.d() + np * (at++));
     for (int i = 0; i < nsteps; ++i) {
         step(chi);
-        finalize_impurity_async(norms.d() + 4 * (at++));
+        finalize_multi_async(norms.d() + np * (at++));
     }
-    check_finite(c, norms.d(), 4 * (int64_t)nn);
-    std::vector<double> h = dvec_to_host(c, norms.d(), 4 * nn);
+    check_finite(c, norms.d(), (int64_t)np * nn);
+    std::vector<double> h = dvec_to_host(c, norms.d(), (int64_t)np * nn);
     int st = c.read_status_and_clear();
     TNR_REQUIRE(!(st & ST_NONFINITE), TNR_ERR_NONFINITE, "run!: non-finite norm");
     return h;

@@ -37,6 +37,7 @@ struct Scheme {
     DT T;
     DT S1, S2;                     // BTRG diagonal bond tensors
     DT I11, I12, I2;               // ImpurityHOTRG: +1 / -1 first-order and second-order impurity tensors
+    DT site[4];                    // ImpurityTRG: impurity tensors on the four plaquette sites
     double btrg_k = -0.5;
     int64_t steps = 0;
     int64_t max_slice_entries = int64_t(1) << 31;   // HOTRG_3D slicing budget (entries)
@@ -52,7 +53,11 @@ struct Scheme {
     // ImpurityHOTRG: the four trace norms (pure, +1, -1, second order) into d4[0..3]; every
     // tensor is divided by the pure norm
     void finalize_impurity_async(double* d4);
-    std::vector<double> run_impurity(int chi, int maxiter, bool finalize_beginning);   // 4 per entry
+    // ImpurityTRG: the pure trace norm and the plaquette norm of the four impurities into d2[0..1]
+    void finalize_impurity_trg_async(double* d2);
+    int norms_per_entry() const { return kind == TNR_IMPURITY_HOTRG ? 4 : kind == TNR_IMPURITY_TRG ? 2 : 1; }
+    void finalize_multi_async(double* d);
+    std::vector<double> run_impurity(int chi, int maxiter, bool finalize_beginning);   // norms_per_entry() each
     void record(const TsvdOut& r);
 };
 
