@@ -214,7 +214,8 @@ def test_impurity_trg_high_temperature_needs_parity_pure_vectors(oracle, monkeyp
     beta = 0.1) holds because LAPACK returns parity-pure singular vectors inside the
     degenerate pairs of the Z2-odd impurity's SVD.  Any other orthonormal basis of those
     pairs is an equally valid SVD, yet it mixes parities across sites of the plaquette and
-    leaves <sigma> at O(1e-2): random rotations inside every degenerate group show it."""
+    leaves <sigma> at O(1e-2): random rotations inside every degenerate group show it.  The
+    engine's canonical basis inside degenerate groups, restated here, restores the check."""
     o = oracle
     svd12, rng = o.SVD12, np.random.default_rng(0)
 
@@ -232,10 +233,34 @@ def test_impurity_trg_high_temperature_needs_parity_pure_vectors(oracle, monkeyp
         B.a = np.einsum('lk,kcd->lcd', Q.T, B.a)
         return A, B, s
 
+    def canonical(t, chi):
+        """The engine's canonical basis (degenerate_basis): inside each group of values equal
+        to 1e-11 s_0, the eigenbasis of U_g^T diag(d) U_g, d_r = frac((r + 1) golden ratio)."""
+        A, B, s = rotated(t, chi)
+        m = A.a.shape[0] * A.a.shape[1]
+        d = ((np.arange(m) + 1) * 0.6180339887498949) % 1.0
+        i = 0
+        while i < len(s):
+            j = i + 1
+            while j < len(s) and abs(s[j] - s[i]) <= 1e-11 * s[0]:
+                j += 1
+            if j - i > 1:
+                U = A.a[..., i:j].reshape(m, j - i)
+                W = np.linalg.eigh(U.T @ (d[:, None] * U))[1]
+                A.a[..., i:j] = np.einsum('abk,kl->abl', A.a[..., i:j], W)
+                B.a[i:j] = np.einsum('lk,kcd->lcd', W.T, B.a[i:j])
+            i = j
+        return A, B, s
+
     T, imp = o.classical_ising(0.1, "Trivial"), o.classical_ising_impurity(0.1)
     a = o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(25))
     monkeypatch.setattr(o, "SVD12", rotated)
     b = o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(25))
+    monkeypatch.setattr(o, "SVD12", canonical)
+    c = o.run(o.ImpurityTRG(T, imp, T, T, T), o.truncrank(16), o.maxiter(25))
     np.testing.assert_allclose([x[0] for x in b], [x[0] for x in a], rtol=1e-10)
+    np.testing.assert_allclose([x[0] for x in c], [x[0] for x in a], rtol=1e-10)
     assert abs(a[-1][1] / a[-1][0]) <= 1e-4
     assert max(abs(x[1] / x[0]) for x in b) > 1e-3
+    # the canonical basis undoes any rotation: every step's ratio is back at rounding level
+    assert max(abs(x[1] / x[0]) for x in c) <= 1e-10

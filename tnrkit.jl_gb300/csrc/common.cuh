@@ -267,6 +267,17 @@ void sum_squares(Ctx& c, const double* x, int64_t n, double* out);
 void scale_inplace(Ctx& c, double* x, int64_t n, const double* inv_scale_ptr);
 void fill_identity(Ctx& c, double* x, int64_t m, int64_t n);
 void copy_f64(Ctx& c, double* dst, const double* src, int64_t n);
+// Canonical singular vectors inside degenerate groups.  vals: the k kept singular values
+// (descending); U (m x k, ld m) and Vt (k x n, ld k) of one SVD.  Values within
+// TNR_DEGENERATE_REL * vals[0] of a group's first value form a group; inside each group
+// the vectors are rotated (U <- U W, Vt <- W^T Vt, W orthogonal) to the eigenbasis of
+// U_g^T diag(d) U_g for the fixed sequence d_r = frac((r + 1) * golden ratio).  That basis is
+// unique for distinct eigenvalues, and it is parity-pure whenever the group's span splits
+// into vectors of disjoint row supports (a Z2 block structure).  Singleton columns are
+// left bit-for-bit unchanged.  With a degenerate group present, k above the Jacobi
+// solver's size (160) is refused.
+#define TNR_DEGENERATE_REL 1e-11
+void degenerate_basis(Ctx& c, const std::vector<double>& vals, double* U, int64_t m, double* Vt, int64_t n);
 // dst[0] = |src[0]|
 void abs_copy(Ctx& c, double* dst, const double* src);
 // out[i] = a x[i] + b y[i] (out may alias x or y)

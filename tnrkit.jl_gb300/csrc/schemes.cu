@@ -40,7 +40,9 @@ void Scheme::record(const TsvdOut& r) {
 }
 
 // SVD12 (src/utility/projectors.jl:211-217): M4 as (d1 d2) x (d3 d4) -> A = U sqrt(s), B = sqrt(s) V
-static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B) {
+// canonical: inside every group of kept singular values equal to within the degeneracy
+// tolerance, the singular vectors are rotated to a fixed basis (degenerate_basis)
+static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B, bool canonical = false) {
     Ctx& c = *s.ctx;
     int64_t m = M4.d[0] * M4.d[1], n = M4.d[2] * M4.d[3];
     int k = (int)std::min<int64_t>(chi, std::min(m, n));
@@ -48,6 +50,7 @@ static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B) {
     B = make_dt(c.pool.get(), {(int64_t)k, M4.d[2], M4.d[3]});
     Buf sv(c.pool.get(), (size_t)k * sizeof(double));
     TsvdOut r = tsvd(c, M4.p(), m, n, k, A.p(), sv.d(), B.p());
+    if (canonical) degenerate_basis(c, r.vals, A.p(), m, B.p(), n);
     col_scale(c, A.p(), m, k, m, sv.d(), 1);
     row_scale(c, B.p(), k, n, k, sv.d(), 1);
     s.record(r);
@@ -76,21 +79,24 @@ static void step_trg(Scheme& s, int chi) {
 
 // step!(::ImpurityTRG) (src/schemes/impuritytrg.jl:63-91): SVD12 of sites 1 and 3 and of the
 // pure tensor, and of sites 2 and 4 and the pure tensor transposed ((2,4),(1,3)); the new
-// pure and site tensors are five TRG contractions of those factors
+// pure and site tensors are five TRG contractions of those factors.  The contractions pair
+// factors of different SVDs, so the result depends on the basis each SVD picks inside a
+// degenerate group; the canonical basis keeps the vectors of a Z2-odd impurity's degenerate
+// pairs parity-pure (the choice LAPACK happens to make on such block-structured matrices)
 static void step_impurity_trg(Scheme& s, int chi) {
     Ctx& c = *s.ctx;
     TNR_REQUIRE(s.T.d[0] == s.T.d[3] && s.T.d[1] == s.T.d[2], TNR_ERR_INVALID_ARG,
                 "ImpurityTRG needs d1 == d4 and d2 == d3");
     auto svd_t = [&](const DT& t, DT& C, DT& D) {
         DT tp = permuted(c, t, {1, 3, 0, 2});
-        svd12(s, tp, chi, C, D);
+        svd12(s, tp, chi, C, D, true);
     };
     DT A1, B1, C2, D2, A3, B3, C4, D4, Ap, Bp, Cp, Dp;
-    svd12(s, s.site[0], chi, A1, B1);
+    svd12(s, s.site[0], chi, A1, B1, true);
     svd_t(s.site[1], C2, D2);
-    svd12(s, s.site[2], chi, A3, B3);
+    svd12(s, s.site[2], chi, A3, B3, true);
     svd_t(s.site[3], C4, D4);
-    svd12(s, s.T, chi, Ap, Bp);
+    svd12(s, s.T, chi, Ap, Bp, true);
     svd_t(s.T, Cp, Dp);
     DT T = trg_contract(c, Dp, Bp, Cp, Ap);
     DT S1 = trg_contract(c, Dp, B1, C2, Ap);
