@@ -45,6 +45,7 @@ extern "C" {
 #define TNR_HOTRG_3D  4   /* hotrg3d.jl:27-135 */
 #define TNR_IMPURITY_HOTRG 5 /* impurityhotrg.jl:25-84; created by tnr_create_impurity_hotrg */
 #define TNR_IMPURITY_TRG   6 /* impuritytrg.jl:37-91; created by tnr_create_impurity_trg */
+#define TNR_CORRELATION_HOTRG 7 /* correlationhotrg.jl:29-250; created by tnr_create_correlation_hotrg */
 
 /* ---- arithmetic of the bulk contractions -------------------------------- */
 #define TNR_PREC_F64    0  /* plain path: every operation in FP64                      */
@@ -90,6 +91,19 @@ int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double
 int tnr_create_impurity_trg(tnr_handle* out, const int64_t* dims, const double* T, const double* T_imp1,
                             const double* T_imp2, const double* T_imp3, const double* T_imp4,
                             const tnr_options* opts);
+/* CorrelationHOTRG(Tpure, Timp1, Timp2, dist) (correlationhotrg.jl:51-68): two first-order
+ * impurities 2^dist sites apart, merged into one at step dist (dist >= 0).  tnr_step runs
+ * step! with its phase finalizer (correlationhotrg.jl:92-135); tnr_finalize and tnr_run do not
+ * apply to it. */
+int tnr_create_correlation_hotrg(tnr_handle* out, const int64_t* dims, const double* Tpure, const double* Timp1,
+                                 const double* Timp2, int dist, const tnr_options* opts);
+/* run!(::CorrelationHOTRG) (correlationhotrg.jl:138-162): maxiter steps (maxiter > dist), three
+ * norms per step into norms_out (cap doubles): (n, n_1, n_2) before the merge, (n, n_imp, n_imp)
+ * from it on (finalize.jl:104-124); *n_out = steps written. */
+int tnr_run_correlation(tnr_handle h, int chi, int maxiter, double* norms_out, size_t cap, size_t* n_out);
+/* |tr Timp_final| / |tr Tpure| of a CorrelationHOTRG handle after the merge: the correlation
+ * the reference's tests read (test/schemes.jl:506,517,530). */
+int tnr_correlation_ratio(tnr_handle h, double* out);
 /* finalize! of an impurity scheme: ImpurityHOTRG writes 4 norms (pure, +1, -1, second order;
  * finalize.jl:91-101), ImpurityTRG 2 (pure, plaquette of the four impurities; finalize.jl:75-88). */
 int tnr_finalize_impurity(tnr_handle h, double* norms_out);

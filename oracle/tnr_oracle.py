@@ -425,6 +425,22 @@ class ImpurityHOTRG:
         self.T_imp_order2 = T_imp_order2.copy()
 
 
+class CorrelationHOTRG:
+    """src/schemes/correlationhotrg.jl:29-69: the pure tensor and two first-order impurities
+    2^dist sites apart; after dist steps they merge into one impurity (Timp_final)."""
+
+    def __init__(self, Tpure: Tensor, Timp1: Tensor, Timp2: Tensor, dist: int):
+        assert dist >= 0, "Distance must be non-negative"
+        for t in (Timp1, Timp2):
+            assert t.a.shape == Tpure.a.shape, "the impurities need the spaces of Tpure"
+        self.Tpure = Tpure.copy()
+        self.Timp1 = Timp1.copy()
+        self.Timp2 = Timp2.copy()
+        self.Timp_final = None
+        self.dist = dist
+        self.iter = 0
+
+
 class ImpurityTRG:
     """src/schemes/impuritytrg.jl:37-59: the pure tensor and impurity tensors on the four
     sites of a plaquette, all of the same spaces."""
@@ -670,6 +686,67 @@ def step_impurity_hotrg(scheme: ImpurityHOTRG, chi):
                                         (0.25, st(T12, T11))])
 
 
+def _correlation_phase(scheme: CorrelationHOTRG):
+    """src/schemes/correlationhotrg.jl:175-183: 1 for the first dist steps, 2 for the merge, then 3."""
+    if scheme.iter < scheme.dist:
+        return 1
+    return 2 if scheme.iter == scheme.dist else 3
+
+
+def step_correlation_hotrg(scheme: CorrelationHOTRG, chi):
+    """src/schemes/correlationhotrg.jl:92-135,185-250: the y projector of the pure tensor and
+    x-steps, then the x projector and y-steps (the order of ImpurityHOTRG); an impurity step is
+    the average of the (impurity, pure) and (pure, impurity) steps.  Phase 2's x-step merges the
+    two impurities (their average, both orders); finalize! follows (src/utility/finalize.jl:104-124):
+    phase 1 returns (n, n_1, n_2), phases 2 and 3 (n, n_imp, n_imp), every tensor /= n."""
+    phase = _correlation_phase(scheme)
+    for half, (proj, stepf) in enumerate(((_hotrg_yproj, _hotrg_step_x), (_hotrg_xproj, _hotrg_step_y))):
+        T = scheme.Tpure
+        U = proj(T, T, chi)[0]
+        st = lambda a, b: stepf(a, b, U)                                   # noqa: E731
+        sym = lambda a, b: _combine([(0.5, st(a, b)), (0.5, st(b, a))])   # noqa: E731
+        if phase == 1:
+            scheme.Timp1 = sym(scheme.Timp1, T)
+            scheme.Timp2 = sym(scheme.Timp2, T)
+        elif phase == 2 and half == 0:
+            scheme.Timp_final = sym(scheme.Timp1, scheme.Timp2)
+        else:
+            scheme.Timp_final = sym(scheme.Timp_final, T)
+        scheme.Tpure = st(T, T)
+    tr = lambda t: abs(np.einsum('abba->', t.a))                           # noqa: E731
+    n = tr(scheme.Tpure)
+    if phase == 1:
+        out = (float(n), float(tr(scheme.Timp1)), float(tr(scheme.Timp2)))
+        live = (scheme.Tpure, scheme.Timp1, scheme.Timp2)
+    else:
+        ni = float(tr(scheme.Timp_final))
+        out = (float(n), ni, ni)
+        live = (scheme.Tpure, scheme.Timp_final)
+        if phase == 2:
+            scheme.Timp1 = scheme.Timp2 = None
+    for t in live:
+        t.a = t.a / n
+    scheme.iter += 1
+    return out
+
+
+def run_correlation(scheme: CorrelationHOTRG, trunc, crit):
+    """run!(::CorrelationHOTRG) (src/schemes/correlationhotrg.jl:138-162): no finalize at the
+    beginning; each step returns its own 3-tuple; maxiter must exceed dist."""
+    assert crit.n > scheme.dist, "niter must be larger than dist"
+    data, steps, go = [], 0, True
+    while go:
+        data.append(step_correlation_hotrg(scheme, trunc.howmany))
+        steps += 1
+        go = crit(steps, data)
+    return data
+
+
+def correlation_ratio(scheme: CorrelationHOTRG):
+    """|tr Timp_final| / |tr Tpure| (test/schemes.jl:506,517,530)."""
+    return float(abs(np.einsum('abba->', scheme.Timp_final.a)) / abs(np.einsum('abba->', scheme.Tpure.a)))
+
+
 def finalize_impurity_hotrg(scheme: ImpurityHOTRG):
     """src/utility/finalize.jl:91-101: the four trace norms; every tensor /= the pure one's."""
     tr = [abs(np.einsum('abba->', t.a)) for t in (scheme.T, scheme.T_imp_order1_1, scheme.T_imp_order1_2,
@@ -743,7 +820,10 @@ class maxiter:
 
 
 def run(scheme, trunc: truncrank, crit: maxiter, finalize_beginning=True, verbosity=0):
-    """src/schemes/tnrscheme.jl:33-57 with the default Finalizer (finalize!, Float64)."""
+    """src/schemes/tnrscheme.jl:33-57 with the default Finalizer (finalize!, Float64);
+    CorrelationHOTRG has its own run! (run_correlation)."""
+    if isinstance(scheme, CorrelationHOTRG):
+        return run_correlation(scheme, trunc, crit)
     data = []
     if finalize_beginning:
         data.append(finalize(scheme))

@@ -166,3 +166,21 @@ def test_run_batch_argument_checks(tnr):
     assert tnr.run_batch([], [], []) == []
     with pytest.raises(ValueError):
         tnr.run_batch([], [8], [])
+
+
+def test_correlation_hotrg_argument_checks(tnr):
+    """CorrelationHOTRG refuses a negative distance in the host layer and in the C ABI, before
+    any device work (src/schemes/correlationhotrg.jl:57)."""
+    T = tnr.classical_ising("Trivial")
+    with pytest.raises(ValueError):
+        tnr.CorrelationHOTRG(T, T, T, -1)
+    a = np.asfortranarray(T.array)
+    p = a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    dims = (ctypes.c_int64 * 4)(*a.shape)
+    h = ctypes.c_void_p()
+    L = tnr.lib()
+    assert L.tnr_create_correlation_hotrg(ctypes.byref(h), dims, p, p, p, -1, None) == header_defines()["TNR_ERR_INVALID_ARG"]
+    assert not h.value
+    bad = np.ones((2, 2, 2, 2))
+    with pytest.raises(ValueError):
+        tnr.CorrelationHOTRG(np.ones((2, 2, 2)), bad, bad, 1)

@@ -264,3 +264,40 @@ def test_impurity_trg_high_temperature_needs_parity_pure_vectors(oracle, monkeyp
     assert max(abs(x[1] / x[0]) for x in b) > 1e-3
     # the canonical basis undoes any rotation: every step's ratio is back at rounding level
     assert max(abs(x[1] / x[0]) for x in c) <= 1e-10
+
+
+def test_correlation_hotrg_onsager(oracle):
+    """test/schemes.jl:483-493: CorrelationHOTRG(T, T_imp, T_imp, 5) at beta_c, truncrank(16),
+    maxiter(25); the pure norms give Onsager's f to 1e-4 with scalefactor 4, initial_size 4."""
+    o = oracle
+    T, imp = o.classical_ising(o.ISING_BETA_C, "Trivial"), o.classical_ising_impurity()
+    data = o.run(o.CorrelationHOTRG(T, imp, imp, 5), o.truncrank(16), o.maxiter(25))
+    assert len(data) == 25 and all(len(d) == 3 for d in data)
+    f = o.free_energy([d[0] for d in data], o.ISING_BETA_C, scalefactor=4.0, initial_size=4.0)
+    assert f == pytest.approx(o.F_ONSAGER, rel=1e-4)
+
+
+@pytest.mark.parametrize("beta,want,rtol", [(0.2, 7.396177e-6, 1e-5), (None, 0.2981409, 1e-5), (3.0, 1.0, 1e-4)])
+def test_correlation_hotrg_magnetisation_correlation(oracle, beta, want, rtol):
+    """test/schemes.jl:495-531: |tr Timp_final| / |tr Tpure| after 25 steps of
+    CorrelationHOTRG(T, T_imp, T_imp, 5), truncrank(16): 7.396177e-6 at beta = 0.2, 0.2981409 at
+    beta_c (both rtol 1e-5) and 1 at beta = 3 (rtol 1e-4).  The merge happens at step 5: the
+    norms switch from (n, n_1, n_2) to (n, n_imp, n_imp) there."""
+    o = oracle
+    beta = o.ISING_BETA_C if beta is None else beta
+    T, imp = o.classical_ising(beta, "Trivial"), o.classical_ising_impurity(beta)
+    s = o.CorrelationHOTRG(T, imp, imp, 5)
+    data = o.run(s, o.truncrank(16), o.maxiter(25))
+    assert s.Timp1 is None and s.Timp2 is None and s.iter == 25
+    assert all(d[1] == d[2] for d in data[5:])
+    assert o.correlation_ratio(s) == pytest.approx(want, rel=rtol)
+
+
+def test_correlation_hotrg_rejects_short_runs(oracle):
+    """run!(::CorrelationHOTRG) asserts niter > dist; the constructor asserts dist >= 0."""
+    o = oracle
+    T, imp = o.classical_ising(o.ISING_BETA_C, "Trivial"), o.classical_ising_impurity()
+    with pytest.raises(AssertionError):
+        o.run(o.CorrelationHOTRG(T, imp, imp, 3), o.truncrank(8), o.maxiter(3))
+    with pytest.raises(AssertionError):
+        o.CorrelationHOTRG(T, imp, imp, -1)

@@ -1,9 +1,10 @@
-"""GPU parity of ImpurityTRG against the oracle, through the C ABI.
+"""GPU parity of ImpurityTRG and CorrelationHOTRG against the oracle, through the C ABI.
 
 ImpurityTRG's plaquette norm after a step depends on the basis each SVD picks (signs and
 rotations inside degenerate groups); the engine fixes a canonical basis inside degenerate
 groups (degenerate_basis), which keeps the Z2-odd impurity's degenerate pairs parity-pure.
-This file runs after the other GPU tests.
+CorrelationHOTRG uses one isometry for every tensor of a step, so all its outputs are
+basis-free.  This file runs after the other GPU tests.
 """
 import numpy as np
 import pytest
@@ -55,3 +56,35 @@ def test_impurity_trg_high_temperature(tnr):
     d = tnr.run(tnr.ImpurityTRG(T, imp, T, T, T), tnr.truncrank(16), tnr.maxiter(25))
     assert len(d) == 26
     assert max(abs(x[1] / x[0]) for x in d) <= 1e-4
+
+
+def test_correlation_hotrg(tnr, oracle):
+    """CorrelationHOTRG (src/schemes/correlationhotrg.jl:92-250, finalize.jl:104-124) with the
+    magnetisation impurity at both ends.  At beta_c, dist 2, truncrank(16), 6 steps, every
+    step's three norms against the oracle to 1e-10 (the phase-1 traces of the Z2-odd
+    impurities vanish up to rounding: an absolute floor of 1e-12 of the largest norm); then
+    the reference's own checks at dist 5, 25 steps (test/schemes.jl:483-531): Onsager's f to
+    1e-4 and the correlation |tr Timp_final| / |tr Tpure| at beta = 0.2, beta_c and 3, each
+    against the reference's value and (beta = 0.2, beta_c) the oracle's to 1e-8."""
+    o = oracle
+    T, imp = tnr.classical_ising("Trivial"), tnr.classical_ising_impurity()
+    To, impo = o.classical_ising(o.ISING_BETA_C, "Trivial"), o.classical_ising_impurity()
+    d = np.array(tnr.run(tnr.CorrelationHOTRG(T, imp, imp, 2), tnr.truncrank(16), tnr.maxiter(6)))
+    do = np.array(o.run(o.CorrelationHOTRG(To, impo, impo, 2), o.truncrank(16), o.maxiter(6)))
+    assert d.shape == do.shape == (6, 3)
+    np.testing.assert_allclose(d, do, rtol=1e-10, atol=1e-12 * np.abs(do).max())
+    for beta, want, rtol in [(0.2, 7.396177e-6, 1e-5), (tnr.ising_βc, 0.2981409, 1e-5), (3.0, 1.0, 1e-4)]:
+        T, imp = tnr.classical_ising("Trivial", beta), tnr.classical_ising_impurity(beta)
+        s = tnr.CorrelationHOTRG(T, imp, imp, 5)
+        d = tnr.run(s, tnr.truncrank(16), tnr.maxiter(25))
+        assert len(d) == 25
+        got = s.correlation()
+        assert got == pytest.approx(want, rel=rtol)
+        if beta == tnr.ising_βc:
+            f = tnr.free_energy([x[0] for x in d], beta, scalefactor=4.0, initial_size=4.0)
+            assert f == pytest.approx(tnr.f_onsager, rel=1e-4)
+        if beta < 1.0:
+            To, impo = o.classical_ising(beta, "Trivial"), o.classical_ising_impurity(beta)
+            so = o.CorrelationHOTRG(To, impo, impo, 5)
+            o.run(so, o.truncrank(16), o.maxiter(25))
+            assert got == pytest.approx(o.correlation_ratio(so), rel=1e-8)

@@ -26,7 +26,7 @@ from .models import (SymTensor, classical_clock, classical_ising, classical_isin
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("TNR_GB300_LIB") or os.path.join(HERE, "libtnr_gb300.so")
 
-TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG = 1, 2, 3, 4, 5, 6
+TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG, TNR_CORRELATION_HOTRG = range(1, 8)
 PREC_F64, PREC_SPLIT = 0, 1
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "iteration cap reached",
           4: "CUDA error", 5: "admission refused", 6: "non-finite value", 7: "unsupported", 8: "no device"}
@@ -38,7 +38,8 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm", "tnr_gemm_time",
            "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_poll",
            "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes", "tnr_create_impurity_hotrg",
-           "tnr_create_impurity_trg", "tnr_finalize_impurity", "tnr_run_impurity"]
+           "tnr_create_impurity_trg", "tnr_finalize_impurity", "tnr_run_impurity", "tnr_create_correlation_hotrg",
+           "tnr_run_correlation", "tnr_correlation_ratio"]
 
 
 class TNRError(RuntimeError):
@@ -77,6 +78,9 @@ def lib():
         "tnr_create_impurity_hotrg": (I, [C.POINTER(P), pi64, pd, pd, pd, pd, C.c_void_p]),
         "tnr_create_impurity_trg": (I, [C.POINTER(P), pi64, pd, pd, pd, pd, pd, C.c_void_p]),
         "tnr_finalize_impurity": (I, [P, pd]),
+        "tnr_create_correlation_hotrg": (I, [C.POINTER(P), pi64, pd, pd, pd, I, C.c_void_p]),
+        "tnr_run_correlation": (I, [P, I, I, pd, Z, pz]),
+        "tnr_correlation_ratio": (I, [P, pd]),
         "tnr_run_impurity": (I, [P, I, I, I, pd, Z, pz]),
         "tnr_free_energy": (D, [pd, Z, D, D, D]),
         "tnr_get_tensor": (I, [P, pd, Z, pi64, C.POINTER(I)]),
@@ -285,7 +289,7 @@ class _ImpurityScheme(_Scheme):
     norms = 1
     _create = ""
 
-    def _make(self, tensors, precision, seed, stream):
+    def _make(self, tensors, precision, seed, stream, *extra):
         arrs = [np.asfortranarray(np.asarray(_as_sym(t).array, dtype=np.float64)) for t in tensors]
         if any(a.ndim != 4 or a.shape != arrs[0].shape for a in arrs):
             raise ValueError(f"{type(self).__name__} needs {len(arrs)} 4-leg tensors of the same dims")
@@ -298,7 +302,7 @@ class _ImpurityScheme(_Scheme):
         dims = (C.c_int64 * 4)(*arrs[0].shape)
         pp = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
         h = C.c_void_p()
-        _check(getattr(L, self._create)(C.byref(h), dims, *pp, C.byref(o)))
+        _check(getattr(L, self._create)(C.byref(h), dims, *pp, *extra, C.byref(o)))
         self._h = h
         self.precision = precision
         self.symmetry_n = 1
@@ -330,6 +334,28 @@ class ImpurityTRG(_ImpurityScheme):
         self._make((T, T_imp1, T_imp2, T_imp3, T_imp4), precision, seed, stream)
 
 
+class CorrelationHOTRG(_ImpurityScheme):
+    """``CorrelationHOTRG(Tpure, Timp1, Timp2, dist)`` (src/schemes/correlationhotrg.jl:29-68): two
+    first-order impurities 2^dist sites apart, merged into one at step dist.  ``run`` returns the
+    (n, n_1, n_2) / (n, n_imp, n_imp) tuple of every step (correlationhotrg.jl:138-162); ``step``
+    runs step! with its phase finalizer; ``correlation()`` is |tr Timp_final| / |tr Tpure|."""
+    kind = TNR_CORRELATION_HOTRG
+    scalefactor = 4.0
+    norms = 3
+    _create = "tnr_create_correlation_hotrg"
+
+    def __init__(self, Tpure, Timp1, Timp2, dist, precision=PREC_F64, seed=0, stream=None):
+        if int(dist) < 0:
+            raise ValueError("Distance must be non-negative")
+        self.dist = int(dist)
+        self._make((Tpure, Timp1, Timp2), precision, seed, stream, self.dist)
+
+    def correlation(self):
+        out = C.c_double()
+        _check(lib().tnr_correlation_ratio(self._h, C.byref(out)), self._h)
+        return out.value
+
+
 def step(scheme, trunc):
     """``step!(scheme, truncrank(chi))``"""
     _check(lib().tnr_step(scheme._h, int(trunc.howmany)), scheme._h)
@@ -338,6 +364,8 @@ def step(scheme, trunc):
 
 def finalize(scheme):
     """``finalize!(scheme)``: trace norm n, T /= n; returns n (impurity schemes: a tuple of norms)."""
+    if isinstance(scheme, CorrelationHOTRG):
+        raise TypeError("CorrelationHOTRG finalizes inside step!; use run or step")
     if isinstance(scheme, _ImpurityScheme):
         out = np.empty(scheme.norms)
         _check(lib().tnr_finalize_impurity(scheme._h, out.ctypes.data_as(C.POINTER(C.c_double))), scheme._h)
@@ -355,6 +383,14 @@ def run(scheme, trunc, crit, finalize_beginning=True, verbosity=0):
         raise TypeError("only maxiter(n) runs on the device path")
     nsteps = max(crit.n, 1)
     cap = nsteps + 1
+    if isinstance(scheme, CorrelationHOTRG):
+        if crit.n <= scheme.dist:
+            raise ValueError("niter must be larger than dist")
+        out = np.empty(3 * crit.n)
+        n = C.c_size_t()
+        _check(lib().tnr_run_correlation(scheme._h, int(trunc.howmany), int(crit.n),
+                                         out.ctypes.data_as(C.POINTER(C.c_double)), out.size, C.byref(n)), scheme._h)
+        return [tuple(out[3 * i:3 * i + 3]) for i in range(n.value)]
     if isinstance(scheme, _ImpurityScheme):
         k = scheme.norms
         out = np.empty(k * cap)

@@ -150,7 +150,7 @@ int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
 
 // A scheme holding impurity tensors beside the pure one: all share the pure tensor's dims
 static int create_impurity(tnr_handle* out, int kind, const char* name, const int64_t* dims, const double* T,
-                           std::initializer_list<const double*> imps, const tnr_options* opts) {
+                           std::initializer_list<const double*> imps, const tnr_options* opts, int dist = 0) {
     if (!out) return fail(nullptr, TNR_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
     bool null_arg = !dims || !T;
@@ -160,23 +160,26 @@ static int create_impurity(tnr_handle* out, int kind, const char* name, const in
         if (dims[l] < 1) return fail(nullptr, TNR_ERR_INVALID_ARG, "leg dimension < 1");
     if (dims[0] != dims[3] || dims[1] != dims[2])
         return fail(nullptr, TNR_ERR_INVALID_ARG, std::string(name) + " needs d1 == d4 and d2 == d3");
+    if (dist < 0) return fail(nullptr, TNR_ERR_INVALID_ARG, "Distance must be non-negative");
     tnr_handle h = nullptr;
-    int st = create_common(&h, kind == TNR_IMPURITY_HOTRG ? TNR_HOTRG : TNR_TRG, 4, dims, T, false, opts);
+    int st = create_common(&h, kind == TNR_IMPURITY_TRG ? TNR_TRG : TNR_HOTRG, 4, dims, T, false, opts);
     if (st != TNR_OK) return st;
     st = guarded(h, [&] {
         Scheme& s = h->s;
         const int64_t n = dims[0] * dims[1] * dims[2] * dims[3];
         DT* hotrg_dst[3] = {&s.I11, &s.I12, &s.I2};
+        DT* corr_dst[2] = {&s.C1, &s.C2};
         int i = 0;
         for (const double* src : imps) {
             for (int64_t e = 0; e < n; ++e)
                 TNR_REQUIRE(std::isfinite(src[e]), TNR_ERR_NONFINITE, "non-finite entry in an impurity tensor");
-            DT& dst = kind == TNR_IMPURITY_HOTRG ? *hotrg_dst[i] : s.site[i];
+            DT& dst = kind == TNR_IMPURITY_HOTRG ? *hotrg_dst[i] : kind == TNR_CORRELATION_HOTRG ? *corr_dst[i] : s.site[i];
             dst = make_dt(s.ctx->pool.get(), {dims[0], dims[1], dims[2], dims[3]});
             TNR_CUDA(cudaMemcpyAsync(dst.p(), src, n * sizeof(double), cudaMemcpyHostToDevice, s.ctx->stream));
             ++i;
         }
         s.kind = kind;
+        s.corr_dist = dist;
         s.ctx->sync();
     });
     if (st != TNR_OK) {
@@ -196,6 +199,41 @@ int tnr_create_impurity_trg(tnr_handle* out, const int64_t* dims, const double* 
                             const double* T_imp2, const double* T_imp3, const double* T_imp4,
                             const tnr_options* opts) {
     return create_impurity(out, TNR_IMPURITY_TRG, "ImpurityTRG", dims, T, {T_imp1, T_imp2, T_imp3, T_imp4}, opts);
+}
+
+int tnr_create_correlation_hotrg(tnr_handle* out, const int64_t* dims, const double* Tpure, const double* Timp1,
+                                 const double* Timp2, int dist, const tnr_options* opts) {
+    return create_impurity(out, TNR_CORRELATION_HOTRG, "CorrelationHOTRG", dims, Tpure, {Timp1, Timp2}, opts, dist);
+}
+
+int tnr_run_correlation(tnr_handle h, int chi, int maxiter, double* norms_out, size_t cap, size_t* n_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        TNR_REQUIRE(h->s.kind == TNR_CORRELATION_HOTRG, TNR_ERR_INVALID_ARG, "not a CorrelationHOTRG handle");
+        TNR_REQUIRE(maxiter > h->s.corr_dist, TNR_ERR_INVALID_ARG, "run!: maxiter must be larger than dist");
+        TNR_REQUIRE(norms_out && cap >= 3 * (size_t)maxiter, TNR_ERR_INVALID_ARG, "norms_out too small for run!");
+        std::vector<double> v = h->s.run_correlation(chi, maxiter);
+        std::memcpy(norms_out, v.data(), v.size() * sizeof(double));
+        if (n_out) *n_out = v.size() / 3;
+    });
+}
+
+int tnr_correlation_ratio(tnr_handle h, double* out) {
+    if (!h || !out) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        TNR_REQUIRE(s.kind == TNR_CORRELATION_HOTRG, TNR_ERR_INVALID_ARG, "not a CorrelationHOTRG handle");
+        TNR_REQUIRE(s.Cf.size() > 0, TNR_ERR_INVALID_ARG, "the impurities have not merged yet (steps <= dist)");
+        Buf d2(s.ctx->pool.get(), 2 * sizeof(double));
+        trace2d(*s.ctx, s.T.p(), s.T.d, d2.d());
+        trace2d(*s.ctx, s.Cf.p(), s.Cf.d, d2.d() + 1);
+        double tr[2];
+        TNR_CUDA(cudaMemcpyAsync(tr, d2.d(), sizeof tr, cudaMemcpyDeviceToHost, s.ctx->stream));
+        s.ctx->sync();
+        TNR_REQUIRE(std::isfinite(tr[0]) && std::isfinite(tr[1]) && tr[0] > 0, TNR_ERR_NONFINITE,
+                    "correlation: non-finite or zero trace");
+        *out = tr[1] / tr[0];
+    });
 }
 
 int tnr_finalize_impurity(tnr_handle h, double* norms_out) {

@@ -447,7 +447,65 @@ bool split_step_in_fp64(int kind, int64_t step, const int64_t* dims, int nlegs, 
     return true;
 }
 
-void Scheme::step(int chi) {
+// step!(::CorrelationHOTRG) with its finalizer (src/schemes/correlationhotrg.jl:92-135,175-250;
+// src/utility/finalize.jl:104-124).  Phase 1 (the first dist steps) carries both impurities, phase
+// 2 merges them in its x-step, phase 3 carries the merged one; each half step is the y projector
+// of the pure tensor and x-steps, then the x projector and y-steps, an impurity step being the
+// average of the (impurity, pure) and (pure, impurity) steps.  d3: (n, n_1, n_2) or (n, n_imp, n_imp).
+static void step_correlation_hotrg(Scheme& s, int chi, double* d3) {
+    Ctx& c = *s.ctx;
+    const int phase = s.steps < s.corr_dist ? 1 : (s.steps == s.corr_dist ? 2 : 3);
+    for (int half = 0; half < 2; ++half) {
+        const DT U = half == 0 ? hotrg_yproj(s, s.T, chi) : hotrg_xproj(s, s.T, chi);
+        auto st = [&](const DT& A1, const DT& A2) {
+            return half == 0 ? hotrg_step_x2(c, A1, A2, U) : hotrg_step_y2(c, A1, A2, U);
+        };
+        auto sym = [&](const DT& a, const DT& b) {       // (st(a, b) + st(b, a)) / 2
+            DT x = st(a, b);
+            DT y = st(b, a);
+            lincomb2(c, x.p(), x.size(), 0.5, x.p(), 0.5, y.p());
+            return x;
+        };
+        DT T = st(s.T, s.T);
+        if (phase == 1) {
+            DT a = sym(s.C1, s.T);
+            DT b = sym(s.C2, s.T);
+            s.C1 = std::move(a);
+            s.C2 = std::move(b);
+        } else if (phase == 2 && half == 0) {
+            s.Cf = sym(s.C1, s.C2);
+        } else {
+            s.Cf = sym(s.Cf, s.T);
+        }
+        s.T = std::move(T);
+    }
+    trace2d(c, s.T.p(), s.T.d, d3);
+    if (phase == 1) {
+        trace2d(c, s.C1.p(), s.C1.d, d3 + 1);
+        trace2d(c, s.C2.p(), s.C2.d, d3 + 2);
+        for (DT* t : {&s.T, &s.C1, &s.C2}) scale_inplace(c, t->p(), t->size(), d3);
+    } else {
+        trace2d(c, s.Cf.p(), s.Cf.d, d3 + 1);
+        copy_f64(c, d3 + 2, d3 + 1, 1);
+        for (DT* t : {&s.T, &s.Cf}) scale_inplace(c, t->p(), t->size(), d3);
+        if (phase == 2) {
+            s.C1 = DT();
+            s.C2 = DT();
+        }
+    }
+}
+
+std::vector<double> Scheme::run_correlation(int chi, int maxiter) {
+    Ctx& c = *ctx;
+    TNR_REQUIRE(kind == TNR_CORRELATION_HOTRG, TNR_ERR_INVALID_ARG, "run_correlation needs a CorrelationHOTRG handle");
+    TNR_REQUIRE(maxiter > corr_dist, TNR_ERR_INVALID_ARG, "run!: maxiter must be larger than dist");
+    Buf norms(c.pool.get(), (size_t)maxiter * 3 * sizeof(double));
+    for (int i = 0; i < maxiter; ++i) step(chi, norms.d() + 3 * i);
+    check_finite(c, norms.d(), 3 * (int64_t)maxiter);
+    return dvec_to_host(c, norms.d(), 3 * (int64_t)maxiter);
+}
+
+void Scheme::step(int chi, double* d_corr) {
     TNR_REQUIRE(chi >= 1, TNR_ERR_INVALID_ARG, "truncrank(chi) needs chi >= 1");
     last_vals.clear();
     last_counts.clear();
@@ -461,6 +519,11 @@ void Scheme::step(int chi) {
         case TNR_HOTRG_3D: step_hotrg3d(*this, chi); break;
         case TNR_IMPURITY_HOTRG: step_impurity_hotrg(*this, chi); break;
         case TNR_IMPURITY_TRG: step_impurity_trg(*this, chi); break;
+        case TNR_CORRELATION_HOTRG: {
+            Buf scratch(ctx->pool.get(), d_corr ? 0 : 3 * sizeof(double));
+            step_correlation_hotrg(*this, chi, d_corr ? d_corr : scratch.d());
+            break;
+        }
         default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
     }
     ++steps;
@@ -469,6 +532,8 @@ void Scheme::step(int chi) {
 // finalize! (src/utility/finalize.jl:4-14,62-66): norm into *d_norm, T /= norm
 void Scheme::finalize_async(double* d_norm) {
     Ctx& c = *ctx;
+    TNR_REQUIRE(kind != TNR_CORRELATION_HOTRG, TNR_ERR_INVALID_ARG,
+                "CorrelationHOTRG finalizes inside step!: run it with tnr_run_correlation");
     if (kind == TNR_IMPURITY_HOTRG || kind == TNR_IMPURITY_TRG) {
         // the pure norm; the impurity norms go to scratch (run_impurity reads them all)
         Buf d4(c.pool.get(), 4 * sizeof(double));

@@ -38,6 +38,8 @@ struct Scheme {
     DT S1, S2;                     // BTRG diagonal bond tensors
     DT I11, I12, I2;               // ImpurityHOTRG: +1 / -1 first-order and second-order impurity tensors
     DT site[4];                    // ImpurityTRG: impurity tensors on the four plaquette sites
+    DT C1, C2, Cf;                 // CorrelationHOTRG: the two first-order impurities, then the merged one
+    int corr_dist = 0;             // CorrelationHOTRG: the impurities merge at step corr_dist (2^dist apart)
     double btrg_k = -0.5;
     int64_t steps = 0;
     int64_t max_slice_entries = int64_t(1) << 31;   // HOTRG_3D slicing budget (entries)
@@ -46,7 +48,9 @@ struct Scheme {
     std::vector<double> last_eps;  // (eps, eps') pairs of the last step
     std::string err;
 
-    void step(int chi);
+    // d_corr: CorrelationHOTRG's three norms of the step (device, may be null)
+    void step(int chi, double* d_corr = nullptr);
+    std::vector<double> run_correlation(int chi, int maxiter);   // three norms per step
     void finalize_async(double* d_norm);
     double finalize();
     std::vector<double> run(int chi, int maxiter, bool finalize_beginning);
