@@ -796,6 +796,98 @@ def finalize(scheme):
     return float(n)
 
 
+# ---------------------------------------------------------------------------
+# finalizers on the fixed-point tensor (src/utility/cft.jl, src/utility/finalize.jl:17-41)
+# ---------------------------------------------------------------------------
+
+def unit_tensor(scheme):
+    """The tensor the fixed-point finalizers read: T itself, or for BTRG
+    T_unit[-1 -2; -3 -4] = T[1 2; -3 -4] S1[-2; 2] S2[-1; 1] (src/utility/cft.jl:42-43), i.e.
+    T[a, b, c, d] S1[b] S2[a] with the diagonal bond tensors."""
+    T = scheme.T.a
+    if isinstance(scheme, BTRG):
+        return T * scheme.S1[None, :, None, None] * scheme.S2[:, None, None, None]
+    return T
+
+
+def transfer_matrix(scheme, unitcell=1):
+    """The column transfer matrix of cft_data / ground_state_degeneracy (src/utility/cft.jl:7-15,
+    278-296): unitcell copies of T_unit joined along the horizontal legs into a ring,
+    indices [i, -i, -(i + u), i + 1] with the last leg closing on the first; rows are the
+    upper legs (-1..-u), columns the lower ones.  unitcell 1: M[b, c] = sum_a T[a, b, c, a]."""
+    T = unit_tensor(scheme)
+    d = T.shape
+    X = np.einsum('abcd->adbc', T)                      # X[a, a', b, c]: T as a map on the horizontal leg
+    cur = X
+    for _ in range(unitcell - 1):
+        cur = np.einsum('xy...,yzbc->xz...bc', cur, X)
+    M = np.einsum('xx...->...', cur)                     # close the ring: [b1, c1, b2, c2, ...]
+    u = unitcell
+    perm = [2 * i for i in range(u)] + [2 * i + 1 for i in range(u)]
+    M = M.transpose(perm)
+    return M.reshape(d[1] ** u, d[2] ** u)
+
+
+def cft_data(scheme, v=1.0, unitcell=1, is_real=True):
+    """src/utility/cft.jl:5-37 (BTRG :39-73): the transfer matrix's eigenvalues, sorted by
+    magnitude (descending), those with real part <= 0 or magnitude <= 1e-12 dropped, as
+    unitcell / (2 pi v) log(lambda_1 / lambda)."""
+    lam = np.linalg.eigvals(transfer_matrix(scheme, unitcell))
+    lam = lam[np.argsort(-np.abs(lam), kind='stable')]
+    lam = lam[lam.real > 0]
+    lam = lam[np.abs(lam) > 1e-12]
+    if is_real:
+        lam = lam.real
+    return unitcell * (1.0 / (2.0 * math.pi * v)) * np.log(lam[0] / lam)
+
+
+def ground_state_degeneracy(scheme, unitcell=1):
+    """src/utility/cft.jl:278-340: exp of the Shannon entropy of |lambda / tr(D)| over the
+    transfer matrix's nonzero eigenvalues."""
+    lam = np.linalg.eigvals(transfer_matrix(scheme, unitcell))
+    p = np.abs(lam / lam.sum())
+    p = p[p != 0]
+    return float(np.exp(-np.sum(p * np.log(p))))
+
+
+def gu_wen_ratio(scheme):
+    """src/utility/cft.jl:374-396: X1 = |T[1 2; 2 1]|^2 / |T[1 2; 2 3] T[3 4; 4 1]| and
+    X2 = |T[1 2; 2 1]|^2 / |T[1 2; 3 4] T[4 3; 2 1]| of T_unit."""
+    T = unit_tensor(scheme)
+    one = abs(np.einsum('abba->', T))
+    M = np.einsum('abbc->ac', T)
+    x1 = abs(np.einsum('ac,ca->', M, M))
+    x2 = abs(np.einsum('abcd,dcba->', T, T))
+    return one ** 2 / x1, one ** 2 / x2
+
+
+def central_charge(scheme, n):
+    """src/utility/cft.jl:256-269: log(sigma_1) 6 / pi of M[-1; -2] = T[1 -1; -2 1] / n (BTRG:
+    T[1 -1; 3 2] S1[3; -2] S2[2; 1] / n, i.e. sum_a T[a, b, c, a] S1[c] S2[a] / n)."""
+    T = scheme.T.a
+    if isinstance(scheme, BTRG):
+        M = np.einsum('abca,c,a->bc', T, scheme.S1, scheme.S2) / n
+    else:
+        M = np.einsum('abca->bc', T) / n
+    return float(math.log(np.linalg.svd(M, compute_uv=False)[0]) * 6.0 / math.pi)
+
+
+def finalize_two_by_two(scheme):
+    """src/utility/finalize.jl:17-41: n = |T[7 1; 5 4] T[4 2; 6 7] T[3 6; 2 8] T[8 5; 1 3]| over a
+    2 x 2 plaquette (BTRG: with S1 on the bonds 1 and 6 and S2 on 8 and 4), T /= n^(1/4);
+    returns n^(1/4)."""
+    T = scheme.T.a
+    T1 = T2 = T4 = T
+    if isinstance(scheme, BTRG):
+        T1 = T * scheme.S1[None, :, None, None] * scheme.S2[None, None, None, :]
+        T2 = T * scheme.S1[None, :, None, None]
+        T4 = T * scheme.S2[None, None, None, :]
+    n = abs(np.einsum('gaed,dbfg,cfbh,heac->', T1, T2, T, T4, optimize=True))
+    r = n ** 0.25
+    scheme.T.a = T / r
+    return float(r)
+
+
 def _btrg_trace(T, S1, S2):
     """sum_{a,b} T[a,b,b,a] S1[b] S2[a] for diagonal S1 (leg 2) and S2 (leg 1)."""
     d1, d2 = T.shape[0], T.shape[1]

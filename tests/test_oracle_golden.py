@@ -301,3 +301,78 @@ def test_correlation_hotrg_rejects_short_runs(oracle):
         o.run(o.CorrelationHOTRG(T, imp, imp, 3), o.truncrank(8), o.maxiter(3))
     with pytest.raises(AssertionError):
         o.CorrelationHOTRG(T, imp, imp, -1)
+
+
+ISING_CFT_EXACT = (1 / 8, 1.0)        # the first two scaling dimensions above the identity (src/models/ising.jl:3-4)
+
+
+@pytest.mark.parametrize("cls,chi,n,tol1,tol2", [("TRG", 24, 10, 2e-4, 1e-2), ("BTRG", 24, 10, 3e-4, 2e-2),
+                                                 ("HOTRG", 16, 4, 6e-4, 1e-2)])
+def test_cft_data_ising(oracle, cls, chi, n, tol1, tol2):
+    """test/schemes.jl:25-33, 64-70, 101-107: cft_data of the Z2 Ising tensor at beta_c after
+    run!(truncrank(chi), maxiter(n)); the first two scaling dimensions after the identity."""
+    o = oracle
+    s = getattr(o, cls)(o.classical_ising())
+    o.run(s, o.truncrank(chi), o.maxiter(n))
+    cft = o.cft_data(s)
+    assert cft[0] == 0.0
+    assert cft[1] == pytest.approx(ISING_CFT_EXACT[0], rel=tol1)
+    assert cft[2] == pytest.approx(ISING_CFT_EXACT[1], rel=tol2)
+
+
+@pytest.mark.parametrize("cls,chi", [("TRG", 16), ("BTRG", 16), ("HOTRG", 12)])
+def test_ground_state_degeneracy_and_gu_wen(oracle, cls, chi):
+    """test/schemes.jl:35-54, 72-90, 109-127: 20 steps at beta_c -+ 0.01: the disordered fixed
+    point has GSD = X1 = X2 = 1, the ordered one 2 (rtol 1e-2 each)."""
+    o = oracle
+    for db, want in [(-0.01, 1.0), (0.01, 2.0)]:
+        s = getattr(o, cls)(o.classical_ising(o.ISING_BETA_C + db))
+        o.run(s, o.truncrank(chi), o.maxiter(20))
+        x1, x2 = o.gu_wen_ratio(s)
+        assert o.ground_state_degeneracy(s) == pytest.approx(want, rel=1e-2)
+        assert x1 == pytest.approx(want, rel=1e-2)
+        assert x2 == pytest.approx(want, rel=1e-2)
+
+
+def test_transfer_matrix_ring(oracle):
+    """The unitcell-u transfer matrix is the ring of u tensors of cft.jl:7-15: for u = 1 its
+    entries are sum_a T[a, b, c, a], for u = 2 sum_{a1, a2} T[a1, b1, c1, a2] T[a2, b2, c2, a1]
+    with rows (b1, b2) and columns (c1, c2)."""
+    o = oracle
+    rng = np.random.default_rng(3)
+    s = o.TRG(o.Tensor(rng.standard_normal((3, 2, 2, 3)), 2, None, 1))
+    T = s.T.a
+    M1 = o.transfer_matrix(s, 1)
+    np.testing.assert_allclose(M1, np.einsum('abca->bc', T), rtol=1e-14)
+    M2 = o.transfer_matrix(s, 2).reshape(2, 2, 2, 2)          # [b1, b2, c1, c2]
+    np.testing.assert_allclose(M2, np.einsum('xbcy,yefx->becf', T, T), rtol=1e-13)
+
+
+def test_two_by_two_finalizer(oracle):
+    """src/utility/finalize.jl:17-41: the 2 x 2 plaquette norm (BTRG with its bond weights,
+    against the network written with explicit diagonal bond matrices); after the division a
+    second call returns 1."""
+    o = oracle
+    for cls in ("TRG", "BTRG"):
+        s = getattr(o, cls)(o.classical_ising(o.ISING_BETA_C, "Trivial"))
+        o.run(s, o.truncrank(12), o.maxiter(6))
+        T = s.T.a
+        if cls == "BTRG":
+            S1, S2 = np.diag(s.S1), np.diag(s.S2)
+            n = abs(np.einsum('kaih,hb,bfjk,cf,gjcl,dg,lied,ea->', T, S2, T, S1, T, S2, T, S1, optimize=True))
+        else:
+            n = abs(np.einsum('gaed,dbfg,cfbh,heac->', T, T, T, T, optimize=True))
+        assert o.finalize_two_by_two(s) == pytest.approx(n ** 0.25, rel=1e-13)
+        assert o.finalize_two_by_two(s) == pytest.approx(1.0, rel=1e-13)
+
+
+def test_central_charge_ising_trg(oracle):
+    """finalize_central_charge! (src/utility/finalize.jl:145-148, cft.jl:256-260) on TRG's Ising
+    flow at beta_c, truncrank(24): c = 1/2 of the Ising CFT, to 1e-2 between steps 13 and 15."""
+    o = oracle
+    s = o.TRG(o.classical_ising())
+    o.run(s, o.truncrank(24), o.maxiter(12))
+    for _ in range(3):
+        o.step(s, 24)
+        n = o.finalize(s)
+        assert o.central_charge(s, n) == pytest.approx(0.5, abs=1e-2)
