@@ -104,6 +104,23 @@ int tnr_run_correlation(tnr_handle h, int chi, int maxiter, double* norms_out, s
 /* |tr Timp_final| / |tr Tpure| of a CorrelationHOTRG handle after the merge: the correlation
  * the reference's tests read (test/schemes.jl:506,517,530). */
 int tnr_correlation_ratio(tnr_handle h, double* out);
+/* Finalizers (src/utility/finalize.jl): TNR_FINALIZER_DEFAULT is finalize! (the trace norm),
+ * TNR_FINALIZER_TWO_BY_TWO is two_by_two_Finalizer (finalize.jl:17-41,151: the 2 x 2 plaquette
+ * norm n, T /= n^(1/4), entry n^(1/4); TRG, BTRG and HOTRG).  tnr_set_finalizer selects the one
+ * tnr_finalize and tnr_run use, as run!(scheme, trunc, crit, finalizer) does. */
+#define TNR_FINALIZER_DEFAULT    0
+#define TNR_FINALIZER_TWO_BY_TWO 1
+int tnr_set_finalizer(tnr_handle h, int finalizer);
+/* eig_full of the column transfer matrix M[b, c] = sum_a T_unit[a, b, c, a] of a 2D scheme
+ * (TRG, BTRG with its bond weights, HOTRG; cft.jl:5-73, 278-340): the eigenvalues, re + i im, in
+ * no particular order (the caller sorts and filters as cft_data / ground_state_degeneracy do).
+ * unitcell must be 1; M above 256 x 256 is refused. */
+int tnr_transfer_eigvals(tnr_handle h, int unitcell, double* re, double* im, size_t cap, size_t* n_out);
+/* gu_wen_ratio (cft.jl:374-396): X1 = |T[1 2;2 1]|^2 / |T[1 2;2 3] T[3 4;4 1]|,
+ * X2 = |T[1 2;2 1]|^2 / |T[1 2;3 4] T[4 3;2 1]| of T_unit. */
+int tnr_gu_wen_ratio(tnr_handle h, double* x1, double* x2);
+/* central_charge(scheme, n) (cft.jl:256-269): log(sigma_1) 6 / pi of M[-1;-2] = T[1 -1;-2 1] / n. */
+int tnr_central_charge(tnr_handle h, double n, double* c_out);
 /* finalize! of an impurity scheme: ImpurityHOTRG writes 4 norms (pure, +1, -1, second order;
  * finalize.jl:91-101), ImpurityTRG 2 (pure, plaquette of the four impurities; finalize.jl:75-88). */
 int tnr_finalize_impurity(tnr_handle h, double* norms_out);

@@ -911,19 +911,21 @@ class maxiter:
         return steps < self.n
 
 
-def run(scheme, trunc: truncrank, crit: maxiter, finalize_beginning=True, verbosity=0):
-    """src/schemes/tnrscheme.jl:33-57 with the default Finalizer (finalize!, Float64);
-    CorrelationHOTRG has its own run! (run_correlation)."""
+def run(scheme, trunc: truncrank, crit: maxiter, finalize_beginning=True, verbosity=0, finalizer=None):
+    """src/schemes/tnrscheme.jl:33-57 with the default Finalizer (finalize!, Float64), or the
+    given finalizer function (e.g. finalize_two_by_two); CorrelationHOTRG has its own run!
+    (run_correlation)."""
     if isinstance(scheme, CorrelationHOTRG):
         return run_correlation(scheme, trunc, crit)
+    fin = finalize if finalizer is None else finalizer
     data = []
     if finalize_beginning:
-        data.append(finalize(scheme))
+        data.append(fin(scheme))
     steps = 0
     go = True
     while go:
         step(scheme, trunc.howmany)
-        data.append(finalize(scheme))
+        data.append(fin(scheme))
         steps += 1
         go = crit(steps, data)
     return data

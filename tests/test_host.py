@@ -4,6 +4,7 @@ constructors match the oracle's."""
 import ctypes
 import os
 import re
+import sys
 
 import numpy as np
 import pytest
@@ -112,6 +113,10 @@ def test_python_constants_match_header(tnr):
     d = header_defines()
     assert (tnr.TNR_TRG, tnr.TNR_BTRG, tnr.TNR_HOTRG, tnr.TNR_HOTRG_3D) == (
         d["TNR_TRG"], d["TNR_BTRG"], d["TNR_HOTRG"], d["TNR_HOTRG_3D"])
+    assert (tnr.TNR_IMPURITY_HOTRG, tnr.TNR_IMPURITY_TRG, tnr.TNR_CORRELATION_HOTRG) == (
+        d["TNR_IMPURITY_HOTRG"], d["TNR_IMPURITY_TRG"], d["TNR_CORRELATION_HOTRG"])
+    assert (tnr.default_Finalizer.code, tnr.two_by_two_Finalizer.code) == (
+        d["TNR_FINALIZER_DEFAULT"], d["TNR_FINALIZER_TWO_BY_TWO"])
     assert (tnr.PREC_F64, tnr.PREC_SPLIT) == (d["TNR_PREC_F64"], d["TNR_PREC_SPLIT"])
     prof = {k[len("TNR_PROF_"):].lower(): v for k, v in d.items() if k.startswith("TNR_PROF_")}
     assert prof == tnr.PROFILE_CLASSES
@@ -184,3 +189,67 @@ def test_correlation_hotrg_argument_checks(tnr):
     bad = np.ones((2, 2, 2, 2))
     with pytest.raises(ValueError):
         tnr.CorrelationHOTRG(np.ones((2, 2, 2)), bad, bad, 1)
+
+
+HQR_SHIM = """
+#include "hqr.cuh"
+extern "C" int hqr_eigvals(double* a, int n, double* wr, double* wi, double* work) {
+    return tnr::real_eigvals(a, n, wr, wi, work);
+}
+"""
+
+
+def _match(x, y):
+    """largest distance of a greedy one-to-one matching of two multisets of complex numbers"""
+    y, err = list(y), 0.0
+    for v in x:
+        i = int(np.argmin([abs(v - u) for u in y]))
+        err = max(err, abs(v - y[i]))
+        y.pop(i)
+    return err
+
+
+def test_transfer_eigvals_routine_on_the_host(tmp_path):
+    """The eigenvalue routine the device runs for cft_data / ground_state_degeneracy
+    (csrc/hqr.cuh: Hessenberg reduction and Francis double-shift QR) is one source for host and
+    device; compiled here with g++ it matches LAPACK's eigenvalues on random matrices up to
+    n = 160 and on structured ones (zero, identity, triangular, repeated, rotation blocks,
+    nilpotent, rank-deficient), and on the oracle's fixed-point transfer matrices."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    src = tmp_path / "shim.cpp"
+    src.write_text(HQR_SHIM)
+    so = tmp_path / "libhqr.so"
+    subprocess.run(["g++", "-O2", "-shared", "-fPIC", "-I", os.path.join(ROOT, "tnrkit.jl_gb300", "csrc"),
+                    "-o", str(so), str(src)], check=True)
+    L = ctypes.CDLL(str(so))
+    pd = ctypes.POINTER(ctypes.c_double)
+
+    def eig(A):
+        n = A.shape[0]
+        a = np.array(A, dtype=np.float64, order="F")
+        wr, wi, w = np.zeros(n), np.zeros(n), np.zeros(max(n, 1))
+        st = L.hqr_eigvals(a.ctypes.data_as(pd), n, wr.ctypes.data_as(pd), wi.ctypes.data_as(pd), w.ctypes.data_as(pd))
+        assert st == 0
+        return wr + 1j * wi
+
+    rng = np.random.default_rng(0)
+    for n in (1, 2, 3, 5, 16, 24, 64, 160):
+        for _ in range(3):
+            A = rng.standard_normal((n, n))
+            ref = np.linalg.eigvals(A)
+            assert _match(eig(A), ref) <= 1e-12 * max(1.0, np.abs(ref).max())
+    Q = np.linalg.qr(rng.standard_normal((5, 5)))[0]
+    for A in (np.zeros((5, 5)), np.eye(6), np.triu(rng.standard_normal((7, 7))), np.diag([3.0, 3.0, 1.0, 1.0]),
+              np.kron(np.eye(3), np.array([[0.0, -2.0], [2.0, 0.0]])), np.ones((6, 6)), np.diag(np.ones(6), 1),
+              Q @ np.diag([1.0, 1e-8, 1e-16, 0.0, -0.5]) @ Q.T):
+        assert _match(eig(A), np.linalg.eigvals(A)) <= 1e-13 * max(1.0, np.abs(A).max())
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tnr_oracle as o
+    s = o.TRG(o.classical_ising())
+    o.run(s, o.truncrank(24), o.maxiter(10))
+    M = o.transfer_matrix(s)
+    ref = np.linalg.eigvals(M)
+    assert _match(eig(M), ref) <= 1e-13 * np.abs(ref).max()

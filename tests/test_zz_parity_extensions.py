@@ -88,3 +88,71 @@ def test_correlation_hotrg(tnr, oracle):
             so = o.CorrelationHOTRG(To, impo, impo, 5)
             o.run(so, o.truncrank(16), o.maxiter(25))
             assert got == pytest.approx(o.correlation_ratio(so), rel=1e-8)
+
+
+ISING_CFT_EXACT = (1 / 8, 1.0)        # src/models/ising.jl:3-4
+
+
+@pytest.mark.parametrize("cls,chi,n,tol1,tol2", [("TRG", 24, 10, 2e-4, 1e-2), ("BTRG", 24, 10, 3e-4, 2e-2),
+                                                 ("HOTRG", 16, 4, 6e-4, 1e-2)])
+def test_cft_data(tnr, oracle, cls, chi, n, tol1, tol2):
+    """cft_data (src/utility/cft.jl:5-73) from the device's transfer-matrix eigenvalues: the
+    reference's Ising checks (test/schemes.jl:25-33, 64-70, 101-107) and the first eight
+    values against the oracle to 1e-9."""
+    o = oracle
+    s = getattr(tnr, cls)(tnr.classical_ising())
+    tnr.run(s, tnr.truncrank(chi), tnr.maxiter(n))
+    so = getattr(o, cls)(o.classical_ising())
+    o.run(so, o.truncrank(chi), o.maxiter(n))
+    cft, ref = tnr.cft_data(s), o.cft_data(so)
+    assert cft[1] == pytest.approx(ISING_CFT_EXACT[0], rel=tol1)
+    assert cft[2] == pytest.approx(ISING_CFT_EXACT[1], rel=tol2)
+    np.testing.assert_allclose(cft[:8], ref[:8], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("cls,chi", [("TRG", 16), ("BTRG", 16), ("HOTRG", 12)])
+def test_ground_state_degeneracy_and_gu_wen(tnr, oracle, cls, chi):
+    """ground_state_degeneracy and gu_wen_ratio (src/utility/cft.jl:278-396) at beta_c -+ 0.01
+    after 20 steps: the reference's checks (1 and 2, rtol 1e-2; test/schemes.jl:35-54) and the
+    oracle's values to 1e-8 where the run has no tie at the cut (BTRG at beta_c - 0.01 has one)."""
+    o = oracle
+    for db, want in [(-0.01, 1.0), (0.01, 2.0)]:
+        s = getattr(tnr, cls)(tnr.classical_ising("Z2", tnr.ising_βc + db))
+        tnr.run(s, tnr.truncrank(chi), tnr.maxiter(20))
+        gsd, (x1, x2) = tnr.ground_state_degeneracy(s), tnr.gu_wen_ratio(s)
+        for v in (gsd, x1, x2):
+            assert v == pytest.approx(want, rel=1e-2)
+        if cls == "BTRG" and db < 0:
+            continue
+        so = getattr(o, cls)(o.classical_ising(o.ISING_BETA_C + db))
+        o.run(so, o.truncrank(chi), o.maxiter(20))
+        assert gsd == pytest.approx(o.ground_state_degeneracy(so), rel=1e-8)
+        np.testing.assert_allclose((x1, x2), o.gu_wen_ratio(so), rtol=1e-8)
+
+
+def test_central_charge_trg(tnr, oracle):
+    """finalize_central_charge! (src/utility/finalize.jl:145-148, cft.jl:256-260) on TRG at
+    beta_c, truncrank(24): c = 1/2 to 1e-2 and the oracle's value to 1e-9 at steps 13, 14."""
+    o = oracle
+    s, so = tnr.TRG(tnr.classical_ising()), o.TRG(o.classical_ising())
+    tnr.run(s, tnr.truncrank(24), tnr.maxiter(12))
+    o.run(so, o.truncrank(24), o.maxiter(12))
+    for _ in range(2):
+        tnr.step(s, tnr.truncrank(24))
+        o.step(so, 24)
+        c, co = tnr.central_charge(s, tnr.finalize(s)), o.central_charge(so, o.finalize(so))
+        assert c == pytest.approx(0.5, abs=1e-2)
+        assert c == pytest.approx(co, abs=1e-9)
+
+
+@pytest.mark.parametrize("cls,chi,n", [("TRG", 16, 6), ("BTRG", 16, 6), ("HOTRG", 12, 4)])
+def test_two_by_two_finalizer(tnr, oracle, cls, chi, n):
+    """run! with two_by_two_Finalizer (src/utility/finalize.jl:17-41,151): every entry
+    n^(1/4) against the oracle to 1e-10; the scheme keeps the finalizer for a later finalize."""
+    o = oracle
+    s = getattr(tnr, cls)(tnr.classical_ising())
+    d = tnr.run(s, tnr.truncrank(chi), tnr.maxiter(n), tnr.two_by_two_Finalizer)
+    do = o.run(getattr(o, cls)(o.classical_ising()), o.truncrank(chi), o.maxiter(n),
+               finalizer=o.finalize_two_by_two)
+    np.testing.assert_allclose(d, do, rtol=1e-10)
+    assert tnr.finalize(s) == pytest.approx(1.0, rel=1e-12)

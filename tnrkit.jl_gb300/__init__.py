@@ -39,7 +39,8 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_poll",
            "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes", "tnr_create_impurity_hotrg",
            "tnr_create_impurity_trg", "tnr_finalize_impurity", "tnr_run_impurity", "tnr_create_correlation_hotrg",
-           "tnr_run_correlation", "tnr_correlation_ratio"]
+           "tnr_run_correlation", "tnr_correlation_ratio", "tnr_set_finalizer", "tnr_transfer_eigvals",
+           "tnr_gu_wen_ratio", "tnr_central_charge"]
 
 
 class TNRError(RuntimeError):
@@ -81,6 +82,10 @@ def lib():
         "tnr_create_correlation_hotrg": (I, [C.POINTER(P), pi64, pd, pd, pd, I, C.c_void_p]),
         "tnr_run_correlation": (I, [P, I, I, pd, Z, pz]),
         "tnr_correlation_ratio": (I, [P, pd]),
+        "tnr_set_finalizer": (I, [P, I]),
+        "tnr_transfer_eigvals": (I, [P, I, pd, pd, Z, pz]),
+        "tnr_gu_wen_ratio": (I, [P, pd, pd]),
+        "tnr_central_charge": (I, [P, C.c_double, pd]),
         "tnr_run_impurity": (I, [P, I, I, I, pd, Z, pz]),
         "tnr_free_energy": (D, [pd, Z, D, D, D]),
         "tnr_get_tensor": (I, [P, pd, Z, pi64, C.POINTER(I)]),
@@ -185,14 +190,20 @@ class _Scheme:
         self.symmetry_n = T.N
 
     # --- reference fields -------------------------------------------------
+    def dims(self):
+        """The current tensor's leg dimensions (no data copy)."""
+        dims = (C.c_int64 * 8)()
+        n = C.c_int()
+        _check(lib().tnr_get_tensor(self._h, None, 0, dims, C.byref(n)), self._h)
+        return tuple(dims[i] for i in range(n.value))
+
     @property
     def T(self):
         """Current tensor as a host array indexed like the reference (T[i1, i2, ...])."""
         L = lib()
         dims = (C.c_int64 * 8)()
         n = C.c_int()
-        _check(L.tnr_get_tensor(self._h, None, 0, dims, C.byref(n)), self._h)
-        shape = tuple(dims[i] for i in range(n.value))
+        shape = self.dims()
         out = np.empty(int(np.prod(shape)), dtype=np.float64)
         _check(L.tnr_get_tensor(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), out.size, dims, C.byref(n)),
                self._h)
@@ -375,12 +386,92 @@ def finalize(scheme):
     return n.value
 
 
-def run(scheme, trunc, crit, finalize_beginning=True, verbosity=0):
-    """``run!(scheme, trunc, maxiter(n); finalize_beginning)`` with the default Finalizer.
+class Finalizer:
+    """A finalizer of run! (src/utility/finalize.jl); ``code`` is its C-ABI constant."""
+
+    def __init__(self, name, code):
+        self.name, self.code = name, code
+
+    def __repr__(self):
+        return self.name
+
+
+default_Finalizer = Finalizer("default_Finalizer", 0)          # finalize! (tnrscheme.jl:26)
+two_by_two_Finalizer = Finalizer("two_by_two_Finalizer", 1)    # finalize_two_by_two! (finalize.jl:17-41,151)
+
+
+def set_finalizer(scheme, finalizer):
+    """The finalizer that ``finalize`` and ``run`` use for this scheme."""
+    _check(lib().tnr_set_finalizer(scheme._h, int(finalizer.code)), scheme._h)
+    scheme.finalizer = finalizer
+
+
+def finalize_two_by_two(scheme):
+    """``finalize_two_by_two!(scheme)`` (src/utility/finalize.jl:17-41): the 2 x 2 plaquette norm
+    n, T /= n^(1/4); returns n^(1/4)."""
+    old = getattr(scheme, "finalizer", default_Finalizer)
+    set_finalizer(scheme, two_by_two_Finalizer)
+    try:
+        return finalize(scheme)
+    finally:
+        set_finalizer(scheme, old)
+
+
+def transfer_eigvals(scheme, unitcell=1):
+    """``eig_full`` of the unit-cell column transfer matrix (src/utility/cft.jl:7-16), on the device."""
+    n = int(scheme.dims()[1]) ** unitcell
+    re, im = np.empty(n), np.empty(n)
+    k = C.c_size_t()
+    _check(lib().tnr_transfer_eigvals(scheme._h, int(unitcell), re.ctypes.data_as(C.POINTER(C.c_double)),
+                                      im.ctypes.data_as(C.POINTER(C.c_double)), n, C.byref(k)), scheme._h)
+    return re[:k.value] + 1j * im[:k.value]
+
+
+def cft_data(scheme, v=1, unitcell=1, is_real=True):
+    """``cft_data(scheme; v, unitcell, is_real)`` (src/utility/cft.jl:5-73): the transfer
+    matrix's eigenvalues sorted by magnitude, real part > 0 and magnitude > 1e-12 kept, as
+    unitcell / (2 pi v) log(lambda_1 / lambda)."""
+    lam = transfer_eigvals(scheme, unitcell)
+    lam = lam[np.argsort(-np.abs(lam), kind="stable")]
+    lam = lam[lam.real > 0]
+    lam = lam[np.abs(lam) > 1e-12]
+    if is_real:
+        lam = lam.real
+    return unitcell * (1.0 / (2.0 * np.pi * v)) * np.log(lam[0] / lam)
+
+
+def ground_state_degeneracy(scheme, unitcell=1):
+    """``ground_state_degeneracy(scheme)`` (src/utility/cft.jl:278-340): exp of the Shannon
+    entropy of |lambda / tr D| over the transfer matrix's nonzero eigenvalues."""
+    lam = transfer_eigvals(scheme, unitcell)
+    p = np.abs(lam / lam.sum())
+    p = p[p != 0]
+    return float(np.exp(-np.sum(p * np.log(p))))
+
+
+def gu_wen_ratio(scheme):
+    """``gu_wen_ratio(scheme)`` (src/utility/cft.jl:374-396): (X1, X2), on the device."""
+    x1, x2 = C.c_double(), C.c_double()
+    _check(lib().tnr_gu_wen_ratio(scheme._h, C.byref(x1), C.byref(x2)), scheme._h)
+    return x1.value, x2.value
+
+
+def central_charge(scheme, n):
+    """``central_charge(scheme, n)`` (src/utility/cft.jl:256-269), on the device."""
+    out = C.c_double()
+    _check(lib().tnr_central_charge(scheme._h, float(n), C.byref(out)), scheme._h)
+    return out.value
+
+
+def run(scheme, trunc, crit, finalizer=None, finalize_beginning=True, verbosity=0):
+    """``run!(scheme, trunc, maxiter(n)[, finalizer]; finalize_beginning)``; the default
+    Finalizer unless ``finalizer`` is given (it then stays selected for the scheme).
 
     Returns the list of norms (n + 1 with ``finalize_beginning``)."""
     if not isinstance(crit, maxiter):
         raise TypeError("only maxiter(n) runs on the device path")
+    if finalizer is not None:
+        set_finalizer(scheme, finalizer)
     nsteps = max(crit.n, 1)
     cap = nsteps + 1
     if isinstance(scheme, CorrelationHOTRG):

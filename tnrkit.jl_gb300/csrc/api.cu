@@ -236,6 +236,40 @@ int tnr_correlation_ratio(tnr_handle h, double* out) {
     });
 }
 
+int tnr_set_finalizer(tnr_handle h, int finalizer) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        TNR_REQUIRE(finalizer == TNR_FINALIZER_DEFAULT || finalizer == TNR_FINALIZER_TWO_BY_TWO,
+                    TNR_ERR_INVALID_ARG, "unknown finalizer");
+        TNR_REQUIRE(finalizer == TNR_FINALIZER_DEFAULT || s.kind == TNR_TRG || s.kind == TNR_BTRG || s.kind == TNR_HOTRG,
+                    TNR_ERR_INVALID_ARG, "the 2 x 2 finalizer needs a TRG, BTRG or HOTRG scheme");
+        s.finalizer = finalizer == TNR_FINALIZER_TWO_BY_TWO ? FINALIZER_TWO_BY_TWO : FINALIZER_DEFAULT;
+    });
+}
+
+int tnr_transfer_eigvals(tnr_handle h, int unitcell, double* re, double* im, size_t cap, size_t* n_out) {
+    if (!h || !re || !im) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
+    return guarded(h, [&] {
+        std::vector<double> wr, wi;
+        h->s.transfer_eigvals(unitcell, wr, wi);
+        TNR_REQUIRE(cap >= wr.size(), TNR_ERR_INVALID_ARG, "eigenvalue buffers too small");
+        std::memcpy(re, wr.data(), wr.size() * sizeof(double));
+        std::memcpy(im, wi.data(), wi.size() * sizeof(double));
+        if (n_out) *n_out = wr.size();
+    });
+}
+
+int tnr_gu_wen_ratio(tnr_handle h, double* x1, double* x2) {
+    if (!h || !x1 || !x2) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
+    return guarded(h, [&] { h->s.gu_wen(x1, x2); });
+}
+
+int tnr_central_charge(tnr_handle h, double n, double* c_out) {
+    if (!h || !c_out) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
+    return guarded(h, [&] { *c_out = h->s.central_charge(n); });
+}
+
 int tnr_finalize_impurity(tnr_handle h, double* norms_out) {
     if (!h || !norms_out) return fail(h, TNR_ERR_INVALID_ARG, "NULL argument");
     return guarded(h, [&] {
@@ -442,7 +476,8 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
         std::map<std::string, int> key_to_task;
         for (int i = 0; i < n; ++i) {
             Scheme& sc = hs[i]->s;
-            bool groupable = (sc.kind == TNR_TRG || sc.kind == TNR_BTRG) && sc.steps == 0;
+            bool groupable = (sc.kind == TNR_TRG || sc.kind == TNR_BTRG) && sc.steps == 0 &&
+                             sc.finalizer == FINALIZER_DEFAULT;
             std::string key;
             if (groupable) {
                 uint64_t kbits = 0;                                   // k exactly, not to 6 decimals

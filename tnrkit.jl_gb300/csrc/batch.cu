@@ -11,8 +11,6 @@
 namespace tnr {
 
 namespace {
-enum { La = 0, Lb, Lc, Ld, Le, Lf, Lg, Lh, Li, Lj, Lk, Ll, Lm, Ln, Lo, Lp, Lq, Lr, Ls, Lt, Lu, Lv, Lw, Lx, Ly, Lz };
-
 std::vector<int64_t> per_dims(const DT& t) { return std::vector<int64_t>(t.d, t.d + t.rank - 1); }
 int64_t per_size(const DT& t) {
     int64_t s = 1;

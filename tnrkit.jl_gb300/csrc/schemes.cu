@@ -7,16 +7,12 @@
 
 namespace tnr {
 
-namespace {
-enum { La = 0, Lb, Lc, Ld, Le, Lf, Lg, Lh, Li, Lj, Lk, Ll, Lm, Ln, Lo, Lp, Lq, Lr, Ls, Lt, Lu, Lv, Lw, Lx, Ly, Lz };
-
 std::vector<double> dvec_to_host(Ctx& c, const double* d, int64_t n) {
     std::vector<double> h((size_t)n);
     if (n) TNR_CUDA(cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
     return h;
 }
-}  // namespace
 
 // T[..., i_leg, ...] *= v[i_leg]
 __global__ void k_scale_leg(double* T, int64_t total, int64_t stride, int64_t dim, const double* v) {
@@ -24,7 +20,7 @@ __global__ void k_scale_leg(double* T, int64_t total, int64_t stride, int64_t di
         T[e] *= v[(e / stride) % dim];
 }
 
-static void scale_leg(Ctx& c, DT& T, int leg, const double* v) {
+void scale_leg(Ctx& c, DT& T, int leg, const double* v) {
     int64_t stride = 1;
     for (int i = 0; i < leg; ++i) stride *= T.d[i];
     int64_t total = T.size();
@@ -534,6 +530,10 @@ void Scheme::finalize_async(double* d_norm) {
     Ctx& c = *ctx;
     TNR_REQUIRE(kind != TNR_CORRELATION_HOTRG, TNR_ERR_INVALID_ARG,
                 "CorrelationHOTRG finalizes inside step!: run it with tnr_run_correlation");
+    if (finalizer == FINALIZER_TWO_BY_TWO) {
+        finalize_two_by_two_async(d_norm);
+        return;
+    }
     if (kind == TNR_IMPURITY_HOTRG || kind == TNR_IMPURITY_TRG) {
         // the pure norm; the impurity norms go to scratch (run_impurity reads them all)
         Buf d4(c.pool.get(), 4 * sizeof(double));

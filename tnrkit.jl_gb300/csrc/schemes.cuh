@@ -5,6 +5,16 @@
 
 namespace tnr {
 
+// leg labels of the contraction networks
+enum { La = 0, Lb, Lc, Ld, Le, Lf, Lg, Lh, Li, Lj, Lk, Ll, Lm, Ln, Lo, Lp, Lq, Lr, Ls, Lt, Lu, Lv, Lw, Lx, Ly, Lz };
+
+std::vector<double> dvec_to_host(Ctx& c, const double* d, int64_t n);
+// T[..., i_leg, ...] *= v[i_leg]
+void scale_leg(Ctx& c, DT& T, int leg, const double* v);
+
+// Finalizer selected for finalize!/run! (Finalizer objects of src/utility/finalize.jl)
+enum { FINALIZER_DEFAULT = 0, FINALIZER_TWO_BY_TWO = 1 };
+
 // Split-precision runs compute their first coarse-graining steps in FP64 while the bond
 // dimension is still growing (every input leg below chi): the norm of step i enters the
 // free energy with weight 2^-i (8^-i in 3D), so the first three 2D steps (the first 3D
@@ -40,6 +50,7 @@ struct Scheme {
     DT site[4];                    // ImpurityTRG: impurity tensors on the four plaquette sites
     DT C1, C2, Cf;                 // CorrelationHOTRG: the two first-order impurities, then the merged one
     int corr_dist = 0;             // CorrelationHOTRG: the impurities merge at step corr_dist (2^dist apart)
+    int finalizer = FINALIZER_DEFAULT;
     double btrg_k = -0.5;
     int64_t steps = 0;
     int64_t max_slice_entries = int64_t(1) << 31;   // HOTRG_3D slicing budget (entries)
@@ -63,6 +74,12 @@ struct Scheme {
     void finalize_multi_async(double* d);
     std::vector<double> run_impurity(int chi, int maxiter, bool finalize_beginning);   // norms_per_entry() each
     void record(const TsvdOut& r);
+
+    // finalizers on the fixed-point tensor (src/utility/cft.jl, src/utility/finalize.jl:17-41)
+    void finalize_two_by_two_async(double* d_norm);      // n^(1/4) of the 2 x 2 plaquette; T /= it
+    void transfer_eigvals(int unitcell, std::vector<double>& re, std::vector<double>& im);
+    void gu_wen(double* x1, double* x2);
+    double central_charge(double n);
 };
 
 // run!() of fresh TRG/BTRG schemes with equal kind, dims and k in lockstep on `c`;
