@@ -46,6 +46,7 @@ extern "C" {
 #define TNR_IMPURITY_HOTRG 5 /* impurityhotrg.jl:25-84; created by tnr_create_impurity_hotrg */
 #define TNR_IMPURITY_TRG   6 /* impuritytrg.jl:37-91; created by tnr_create_impurity_trg */
 #define TNR_CORRELATION_HOTRG 7 /* correlationhotrg.jl:29-250; created by tnr_create_correlation_hotrg */
+#define TNR_ATRG           8 /* atrg.jl:26-81; tnr_create with a 4-leg tensor */
 
 /* ---- arithmetic of the bulk contractions -------------------------------- */
 #define TNR_PREC_F64    0  /* plain path: every operation in FP64                      */

@@ -425,6 +425,17 @@ class ImpurityHOTRG:
         self.T_imp_order2 = T_imp_order2.copy()
 
 
+class ATRG:
+    """src/schemes/atrg.jl:26-33: the central tensor; one step is two anisotropic half steps
+    (linear rescaling sqrt(2) each)."""
+    scalefactor = 2.0
+
+    def __init__(self, T: Tensor):
+        assert T.ndim == 4
+        self.T = T.copy()
+        self.svals = []
+
+
 class CorrelationHOTRG:
     """src/schemes/correlationhotrg.jl:29-69: the pure tensor and two first-order impurities
     2^dist sites apart; after dist steps they merge into one impurity (Timp_final)."""
@@ -686,6 +697,48 @@ def step_impurity_hotrg(scheme: ImpurityHOTRG, chi):
                                         (0.25, st(T12, T11))])
 
 
+def _svd_parts(t: Tensor, chi):
+    """svd_trunc of a (2, 2) tensor: U[i1, i2; k], s, V[k; i3, i4] as tensors with charges."""
+    U, s, Vh, _, bq = svd_trunc(t, 2, chi)
+    qu = None if bq is None else [t.q[0], t.q[1], bq[0]]
+    qv = None if bq is None else [bq[1], t.q[2], t.q[3]]
+    return (lambda a: Tensor(a, 2, qu, t.N)), s, (lambda a: Tensor(a, 1, qv, t.N)), U, Vh
+
+
+def _atrg_half(T: Tensor, chi):
+    """_step!(::ATRG) (src/schemes/atrg.jl:47-81): SVD of T as (1,3) x (2,4) into A S D; the
+    swapped pair M = (S D)(A S) is SVD'd into X Y (sqrt(S) on both); Q = A D X Y is SVD'd
+    into H G (sqrt(S) on both) and T[-1 -2; -3 -4] = G[-1; -3 1] H[1 -2; -4]."""
+    Tp = permute(T, (0, 2, 1, 3), 2)
+    mkU, s1, mkV, U, Vh = _svd_parts(Tp, chi)
+    A, D = mkU(U), mkV(Vh)
+    C, B = mkU(U * s1), mkV(s1[:, None, None] * Vh)
+    # M[-1 -2; -3 -4] := B[-3; 1 -4] C[-1 1; -2]
+    a, q, N = _ein('cxd,axb->abcd', B, C)
+    Mp = permute(Tensor(a, 2, q, N), (0, 2, 1, 3), 2)
+    mkU, s2, mkV, U, Vh = _svd_parts(Mp, chi)
+    r = np.sqrt(s2)
+    X, Y = mkU(U * r), mkV(r[:, None, None] * Vh)
+    # Q[-1 -2; -3 -4] := A[3 -3; 2] D[1; -2 4] X[4 2; -4] Y[-1 1; 3]
+    a, q, N = _ein('czb,ayd,dbw,xac->xyzw', A, D, X, Y, path=[(0, 2), (0, 2), (0, 1)])
+    Q = Tensor(a, 2, q, N)
+    mkU, s3, mkV, U, Vh = _svd_parts(Q, chi)
+    r = np.sqrt(s3)
+    H, G = mkU(U * r), mkV(r[:, None, None] * Vh)
+    # T[-1 -2; -3 -4] := G[-1; -3 1] H[1 -2; -4]
+    a, q, N = _ein('acx,xbd->abcd', G, H)
+    return Tensor(a, 2, q, N), [s1, s2, s3]
+
+
+def step_atrg(scheme: ATRG, chi):
+    """step!(::ATRG) (src/schemes/atrg.jl:38-45): a half step, permute ((2,4),(1,3)), a half
+    step, permute ((3,1),(4,2))."""
+    T, sv1 = _atrg_half(scheme.T, chi)
+    T, sv2 = _atrg_half(permute(T, (1, 3, 0, 2), 2), chi)
+    scheme.T = permute(T, (2, 0, 3, 1), 2)
+    scheme.svals += sv1 + sv2
+
+
 def _correlation_phase(scheme: CorrelationHOTRG):
     """src/schemes/correlationhotrg.jl:175-183: 1 for the first dist steps, 2 for the merge, then 3."""
     if scheme.iter < scheme.dist:
@@ -766,6 +819,8 @@ def step(scheme, chi):
         step_hotrg(scheme, chi)
     elif isinstance(scheme, HOTRG_3D):
         step_hotrg3d(scheme, chi)
+    elif isinstance(scheme, ATRG):
+        step_atrg(scheme, chi)
     elif isinstance(scheme, ImpurityHOTRG):
         step_impurity_hotrg(scheme, chi)
     elif isinstance(scheme, ImpurityTRG):
@@ -783,7 +838,7 @@ def finalize(scheme):
     if isinstance(scheme, ImpurityTRG):
         return finalize_impurity_trg(scheme)
     T = scheme.T.a
-    if isinstance(scheme, (TRG, HOTRG)):
+    if isinstance(scheme, (TRG, HOTRG, ATRG)):
         n = abs(np.einsum('abba->', T))                 # T[1 2; 2 1]
     elif isinstance(scheme, BTRG):
         # T[1 2; 4 3] S1[4; 2] S2[3; 1] with diagonal S1, S2

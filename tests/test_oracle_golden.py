@@ -376,3 +376,24 @@ def test_central_charge_ising_trg(oracle):
         o.step(s, 24)
         n = o.finalize(s)
         assert o.central_charge(s, n) == pytest.approx(0.5, abs=1e-2)
+
+
+def test_atrg_ising(oracle):
+    """test/schemes.jl:130-165: ATRG on the Z2 Ising tensor.  truncrank(24), maxiter(25): f to
+    3e-6 (scalefactor 4); maxiter(3): the first two scaling dimensions to 1e-2; truncrank(16),
+    maxiter(20) at beta_c -+ 0.01: GSD, X1, X2 = 1 and 2 to 1e-2."""
+    o = oracle
+    s = o.ATRG(o.classical_ising())
+    data = o.run(s, o.truncrank(24), o.maxiter(25))
+    assert o.free_energy(data, o.ISING_BETA_C, scalefactor=4.0) == pytest.approx(o.F_ONSAGER, rel=3e-6)
+    s = o.ATRG(o.classical_ising())
+    o.run(s, o.truncrank(24), o.maxiter(3))
+    cft = o.cft_data(s)
+    assert cft[1] == pytest.approx(ISING_CFT_EXACT[0], rel=1e-2)
+    assert cft[2] == pytest.approx(ISING_CFT_EXACT[1], rel=1e-2)
+    for db, want in [(-0.01, 1.0), (0.01, 2.0)]:
+        s = o.ATRG(o.classical_ising(o.ISING_BETA_C + db))
+        o.run(s, o.truncrank(16), o.maxiter(20))
+        x1, x2 = o.gu_wen_ratio(s)
+        for v in (o.ground_state_degeneracy(s), x1, x2):
+            assert v == pytest.approx(want, rel=1e-2)

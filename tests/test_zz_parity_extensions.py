@@ -156,3 +156,28 @@ def test_two_by_two_finalizer(tnr, oracle, cls, chi, n):
                finalizer=o.finalize_two_by_two)
     np.testing.assert_allclose(d, do, rtol=1e-10)
     assert tnr.finalize(s) == pytest.approx(1.0, rel=1e-12)
+
+
+def test_atrg(tnr, oracle):
+    """ATRG (src/schemes/atrg.jl:38-81) on the Z2 Ising tensor at beta_c: every norm of
+    truncrank(16), maxiter(6) against the oracle to 1e-10 (ATRG's network pairs the factors of
+    each SVD, so it is basis-free); then the reference's checks (test/schemes.jl:130-165):
+    truncrank(24), maxiter(25): f to 3e-6 with scalefactor 4; maxiter(3): the first two scaling
+    dimensions to 1e-2; and GSD / X1 / X2 at beta_c -+ 0.01 (truncrank(16), 20 steps)."""
+    o = oracle
+    d = np.array(tnr.run(tnr.ATRG(tnr.classical_ising()), tnr.truncrank(16), tnr.maxiter(6)))
+    do = np.array(o.run(o.ATRG(o.classical_ising()), o.truncrank(16), o.maxiter(6)))
+    np.testing.assert_allclose(d, do, rtol=1e-10)
+    d = tnr.run(tnr.ATRG(tnr.classical_ising()), tnr.truncrank(24), tnr.maxiter(25))
+    assert tnr.free_energy(d, tnr.ising_βc, scalefactor=4.0) == pytest.approx(tnr.f_onsager, rel=3e-6)
+    s = tnr.ATRG(tnr.classical_ising())
+    tnr.run(s, tnr.truncrank(24), tnr.maxiter(3))
+    cft = tnr.cft_data(s)
+    assert cft[1] == pytest.approx(ISING_CFT_EXACT[0], rel=1e-2)
+    assert cft[2] == pytest.approx(ISING_CFT_EXACT[1], rel=1e-2)
+    for db, want in [(-0.01, 1.0), (0.01, 2.0)]:
+        s = tnr.ATRG(tnr.classical_ising("Z2", tnr.ising_βc + db))
+        tnr.run(s, tnr.truncrank(16), tnr.maxiter(20))
+        x1, x2 = tnr.gu_wen_ratio(s)
+        for v in (tnr.ground_state_degeneracy(s), x1, x2):
+            assert v == pytest.approx(want, rel=1e-2)

@@ -26,7 +26,7 @@ from .models import (SymTensor, classical_clock, classical_ising, classical_isin
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("TNR_GB300_LIB") or os.path.join(HERE, "libtnr_gb300.so")
 
-TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG, TNR_CORRELATION_HOTRG = range(1, 8)
+TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG, TNR_CORRELATION_HOTRG, TNR_ATRG = range(1, 9)
 PREC_F64, PREC_SPLIT = 0, 1
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "iteration cap reached",
           4: "CUDA error", 5: "admission refused", 6: "non-finite value", 7: "unsupported", 8: "no device"}
@@ -284,6 +284,13 @@ class BTRG(_Scheme):
 class HOTRG(_Scheme):
     """Higher-Order TRG (src/schemes/hotrg.jl:27-160); rescales by 2 (area factor 4)."""
     kind = TNR_HOTRG
+    scalefactor = 4.0
+
+
+class ATRG(_Scheme):
+    """Anisotropic TRG (src/schemes/atrg.jl:26-81): two anisotropic half steps per step, each a
+    linear rescaling by sqrt(2) (area factor 4 per step)."""
+    kind = TNR_ATRG
     scalefactor = 4.0
 
 
@@ -558,7 +565,7 @@ class Server:
     ``submit(T, scheme, chi, maxiter)`` returns a request id; ``result(id)`` blocks and
     returns (norms, latency_ms, queue_ms)."""
 
-    KINDS = {"TRG": TNR_TRG, "BTRG": TNR_BTRG, "HOTRG": TNR_HOTRG, "HOTRG_3D": TNR_HOTRG_3D}
+    KINDS = {"TRG": TNR_TRG, "BTRG": TNR_BTRG, "HOTRG": TNR_HOTRG, "HOTRG_3D": TNR_HOTRG_3D, "ATRG": TNR_ATRG}
 
     def __init__(self, hbm_budget_bytes, max_active=32, precision=PREC_F64):
         h = C.c_void_p()

@@ -84,7 +84,8 @@ int create_common(tnr_handle* out, int kind, int nlegs, const int64_t* dims, con
     if (opts) o = *opts;
     if (!out) return fail(nullptr, TNR_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
-    if (kind < TNR_TRG || kind > TNR_HOTRG_3D) return fail(nullptr, TNR_ERR_INVALID_ARG, "unknown scheme kind");
+    if ((kind < TNR_TRG || kind > TNR_HOTRG_3D) && kind != TNR_ATRG)
+        return fail(nullptr, TNR_ERR_INVALID_ARG, "unknown scheme kind");
     int want = kind == TNR_HOTRG_3D ? 6 : 4;
     if (nlegs != want || !dims || !data)
         return fail(nullptr, TNR_ERR_INVALID_ARG, "scheme needs a " + std::to_string(want) + "-leg tensor");
@@ -242,8 +243,9 @@ int tnr_set_finalizer(tnr_handle h, int finalizer) {
         Scheme& s = h->s;
         TNR_REQUIRE(finalizer == TNR_FINALIZER_DEFAULT || finalizer == TNR_FINALIZER_TWO_BY_TWO,
                     TNR_ERR_INVALID_ARG, "unknown finalizer");
-        TNR_REQUIRE(finalizer == TNR_FINALIZER_DEFAULT || s.kind == TNR_TRG || s.kind == TNR_BTRG || s.kind == TNR_HOTRG,
-                    TNR_ERR_INVALID_ARG, "the 2 x 2 finalizer needs a TRG, BTRG or HOTRG scheme");
+        TNR_REQUIRE(finalizer == TNR_FINALIZER_DEFAULT || s.kind == TNR_TRG || s.kind == TNR_BTRG ||
+                        s.kind == TNR_HOTRG || s.kind == TNR_ATRG,
+                    TNR_ERR_INVALID_ARG, "the 2 x 2 finalizer needs a TRG, BTRG, HOTRG or ATRG scheme");
         s.finalizer = finalizer == TNR_FINALIZER_TWO_BY_TWO ? FINALIZER_TWO_BY_TWO : FINALIZER_DEFAULT;
     });
 }

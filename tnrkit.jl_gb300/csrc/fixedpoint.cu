@@ -114,8 +114,8 @@ static void btrg_weights(const Scheme& s, const double** s1, const double** s2) 
 }
 
 static void require_2d(const Scheme& s, const char* what) {
-    TNR_REQUIRE(s.kind == TNR_TRG || s.kind == TNR_BTRG || s.kind == TNR_HOTRG, TNR_ERR_INVALID_ARG,
-                std::string(what) + " needs a TRG, BTRG or HOTRG scheme");
+    TNR_REQUIRE(s.kind == TNR_TRG || s.kind == TNR_BTRG || s.kind == TNR_HOTRG || s.kind == TNR_ATRG,
+                TNR_ERR_INVALID_ARG, std::string(what) + " needs a TRG, BTRG, HOTRG or ATRG scheme");
     TNR_REQUIRE(s.T.rank == 4 && s.T.d[0] == s.T.d[3] && s.T.d[1] == s.T.d[2], TNR_ERR_INVALID_ARG,
                 std::string(what) + " needs d1 == d4 and d2 == d3");
 }
@@ -125,8 +125,8 @@ static void require_2d(const Scheme& s, const char* what) {
 // S2 on leg 4, T2 S1 on leg 2, T4 S2 on leg 4.  d_norm = n^(1/4), T /= n^(1/4).
 void Scheme::finalize_two_by_two_async(double* d_norm) {
     Ctx& c = *ctx;
-    TNR_REQUIRE(kind == TNR_TRG || kind == TNR_BTRG || kind == TNR_HOTRG, TNR_ERR_INVALID_ARG,
-                "the 2 x 2 finalizer needs a TRG, BTRG or HOTRG scheme");
+    TNR_REQUIRE(kind == TNR_TRG || kind == TNR_BTRG || kind == TNR_HOTRG || kind == TNR_ATRG, TNR_ERR_INVALID_ARG,
+                "the 2 x 2 finalizer needs a TRG, BTRG, HOTRG or ATRG scheme");
     const DT* t1 = &T;
     const DT* t2 = &T;
     const DT* t4 = &T;

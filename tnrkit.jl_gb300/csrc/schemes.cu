@@ -73,6 +73,74 @@ static void step_trg(Scheme& s, int chi) {
     s.T = trg_contract(c, D, B, C, A);
 }
 
+// svd_trunc of a (2, 2) tensor, unscaled: U[i1, i2; k], sv (k, device), Vt[k; i3, i4]
+static void svd22(Scheme& s, const DT& M4, int chi, DT& U, Buf& sv, DT& Vt) {
+    Ctx& c = *s.ctx;
+    const int64_t m = M4.d[0] * M4.d[1], n = M4.d[2] * M4.d[3];
+    const int k = (int)std::min<int64_t>(chi, std::min(m, n));
+    U = make_dt(c.pool.get(), {M4.d[0], M4.d[1], (int64_t)k});
+    Vt = make_dt(c.pool.get(), {(int64_t)k, M4.d[2], M4.d[3]});
+    sv = Buf(c.pool.get(), (size_t)k * sizeof(double));
+    TsvdOut r = tsvd(c, M4.p(), m, n, k, U.p(), sv.d(), Vt.p());
+    s.record(r);
+}
+
+static DT copy_of(Ctx& c, const DT& t) {
+    DT o = make_dt(c.pool.get(), t.dims());
+    copy_f64(c, o.p(), t.p(), t.size());
+    return o;
+}
+
+// _step!(::ATRG) (src/schemes/atrg.jl:47-81): SVD of T as (1,3) x (2,4) into A S D; the
+// swapped pair M = (S D)(A S) is SVD'd into X Y (sqrt(S) on both); Q = A D X Y is SVD'd into
+// H G (sqrt(S) on both) and T[-1 -2; -3 -4] = G[-1; -3 1] H[1 -2; -4]
+static DT atrg_half(Scheme& s, const DT& T, int chi) {
+    Ctx& c = *s.ctx;
+    DT A, D, X, Y, H, G;
+    Buf s1, s2, s3;
+    {
+        DT Tp = permuted(c, T, {0, 2, 1, 3});
+        svd22(s, Tp, chi, A, s1, D);
+    }
+    {
+        const int64_t k1 = A.d[2], mA = A.d[0] * A.d[1], nD = D.d[1] * D.d[2];
+        DT C = copy_of(c, A), B = copy_of(c, D);
+        col_scale(c, C.p(), mA, k1, mA, s1.d(), 0);      // C = A S
+        row_scale(c, B.p(), k1, nD, k1, s1.d(), 0);      // B = S D
+        // M[-1 -2; -3 -4] := B[-3; 1 -4] C[-1 1; -2]:  B[c,x,d] C[a,x,b] -> M[a,b,c,d]
+        DT M = contract(c, B, {Lc, Lx, Ld}, C, {La, Lx, Lb}, {La, Lb, Lc, Ld});
+        DT Mp = permuted(c, M, {0, 2, 1, 3});
+        svd22(s, Mp, chi, X, s2, Y);
+    }
+    {
+        const int64_t k2 = X.d[2], mX = X.d[0] * X.d[1], nY = Y.d[1] * Y.d[2];
+        col_scale(c, X.p(), mX, k2, mX, s2.d(), 1);
+        row_scale(c, Y.p(), k2, nY, k2, s2.d(), 1);
+        // Q[-1 -2; -3 -4] := A[3 -3; 2] D[1; -2 4] X[4 2; -4] Y[-1 1; 3]
+        //   A[c,z,b] X[d,b,w] -> AX[c,z,d,w];  Y[x,a,c] D[a,y,d] -> YD[x,c,y,d];  YD AX -> Q[x,y,z,w]
+        DT AX = contract(c, A, {Lc, Lz, Lb}, X, {Ld, Lb, Lw}, {Lc, Lz, Ld, Lw});
+        DT YD = contract(c, Y, {Lx, La, Lc}, D, {La, Ly, Ld}, {Lx, Lc, Ly, Ld});
+        A = DT(); D = DT(); X = DT(); Y = DT();
+        DT Q = contract(c, YD, {Lx, Lc, Ly, Ld}, AX, {Lc, Lz, Ld, Lw}, {Lx, Ly, Lz, Lw});
+        svd22(s, Q, chi, H, s3, G);
+    }
+    const int64_t k3 = H.d[2], mH = H.d[0] * H.d[1], nG = G.d[1] * G.d[2];
+    col_scale(c, H.p(), mH, k3, mH, s3.d(), 1);
+    row_scale(c, G.p(), k3, nG, k3, s3.d(), 1);
+    // T[-1 -2; -3 -4] := G[-1; -3 1] H[1 -2; -4]:  G[a,c,x] H[x,b,d] -> T[a,b,c,d]
+    return contract(c, G, {La, Lc, Lx}, H, {Lx, Lb, Ld}, {La, Lb, Lc, Ld});
+}
+
+// step!(::ATRG) (src/schemes/atrg.jl:38-45): a half step, permute ((2,4),(1,3)), a half step,
+// permute ((3,1),(4,2))
+static void step_atrg(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    TNR_REQUIRE(s.T.d[0] == s.T.d[3] && s.T.d[1] == s.T.d[2], TNR_ERR_INVALID_ARG, "ATRG needs d1 == d4 and d2 == d3");
+    DT T = atrg_half(s, s.T, chi);
+    T = atrg_half(s, permuted(c, T, {1, 3, 0, 2}), chi);
+    s.T = permuted(c, T, {2, 0, 3, 1});
+}
+
 // step!(::ImpurityTRG) (src/schemes/impuritytrg.jl:63-91): SVD12 of sites 1 and 3 and of the
 // pure tensor, and of sites 2 and 4 and the pure tensor transposed ((2,4),(1,3)); the new
 // pure and site tensors are five TRG contractions of those factors.  The contractions pair
@@ -513,6 +581,7 @@ void Scheme::step(int chi, double* d_corr) {
         case TNR_BTRG: step_btrg(*this, chi); break;
         case TNR_HOTRG: step_hotrg(*this, chi); break;
         case TNR_HOTRG_3D: step_hotrg3d(*this, chi); break;
+        case TNR_ATRG: step_atrg(*this, chi); break;
         case TNR_IMPURITY_HOTRG: step_impurity_hotrg(*this, chi); break;
         case TNR_IMPURITY_TRG: step_impurity_trg(*this, chi); break;
         case TNR_CORRELATION_HOTRG: {
@@ -543,7 +612,8 @@ void Scheme::finalize_async(double* d_norm) {
     }
     switch (kind) {
         case TNR_TRG:
-        case TNR_HOTRG: trace2d(c, T.p(), T.d, d_norm); break;
+        case TNR_HOTRG:
+        case TNR_ATRG: trace2d(c, T.p(), T.d, d_norm); break;
         case TNR_BTRG: trace_btrg(c, T.p(), T.d, S1.p(), S2.p(), d_norm); break;
         case TNR_HOTRG_3D: trace3d(c, T.p(), T.d, d_norm); break;
         default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
