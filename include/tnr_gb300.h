@@ -39,12 +39,12 @@ extern "C" {
 #define TNR_ERR_NO_DEVICE      8  /* no usable sm_103 GPU                                    */
 
 /* ---- scheme kinds (reference: src/schemes/{trg,btrg,hotrg,hotrg3d}.jl) --- */
-#define TNR_TRG       1   /* trg.jl:85-100     */
-#define TNR_BTRG      2   /* btrg.jl:132-200   */
+#define TNR_TRG       1   /* trg.jl:26-41     */
+#define TNR_BTRG      2   /* btrg.jl:26-94   */
 #define TNR_HOTRG     3   /* hotrg.jl:27-160   */
 #define TNR_HOTRG_3D  4   /* hotrg3d.jl:27-135 */
-#define TNR_IMPURITY_HOTRG 5 /* impurityhotrg.jl:25-84; created by tnr_create_impurity_hotrg */
-#define TNR_IMPURITY_TRG   6 /* impuritytrg.jl:37-91; created by tnr_create_impurity_trg */
+#define TNR_IMPURITY_HOTRG 5 /* impurityhotrg.jl:26-84; created by tnr_create_impurity_hotrg */
+#define TNR_IMPURITY_TRG   6 /* impuritytrg.jl:38-91; created by tnr_create_impurity_trg */
 #define TNR_CORRELATION_HOTRG 7 /* correlationhotrg.jl:29-250; created by tnr_create_correlation_hotrg */
 #define TNR_ATRG           8 /* atrg.jl:26-81; tnr_create with a 4-leg tensor */
 
@@ -57,7 +57,7 @@ typedef struct tnr_handle_s* tnr_handle;
 
 typedef struct tnr_options {
     int    precision;      /* TNR_PREC_F64 or TNR_PREC_SPLIT                          */
-    double btrg_k;         /* BTRG bond-weight exponent k (btrg.jl:154 default -0.5)   */
+    double btrg_k;         /* BTRG bond-weight exponent k (btrg.jl:48 default -0.5)   */
     int    symmetry_n;     /* 1 = Trivial, N = Z_N charges given in leg_charges         */
     const int32_t* leg_charges; /* sum(dims) ints: charge of each basis index per leg,
                                    or NULL.  Used to validate charge conservation.     */
@@ -71,7 +71,7 @@ void tnr_default_options(tnr_options* opts);
 /* Create a scheme from a host tensor.
  *   kind  : TNR_TRG | TNR_BTRG | TNR_HOTRG (nlegs = 4) or TNR_HOTRG_3D (nlegs = 6)
  *   dims  : leg dimensions; data: prod(dims) doubles, column-major.
- * Replaces the constructors TRG(T) (trg.jl:89), BTRG(T, k) (btrg.jl:145-154),
+ * Replaces the constructors TRG(T) (trg.jl:30), BTRG(T, k) (btrg.jl:39-48),
  * HOTRG(T) (hotrg.jl:31), HOTRG_3D(T) (hotrg3d.jl:31). */
 int tnr_create(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
                const double* data, const tnr_options* opts);
@@ -81,20 +81,20 @@ int tnr_create_device(tnr_handle* out, int kind, int nlegs, const int64_t* dims,
                       const double* device_data, const tnr_options* opts);
 
 /* ImpurityHOTRG(T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)
- * (impurityhotrg.jl:25-44): four host tensors of the same dims (4 legs, column-major).
- * tnr_step steps all four (impurityhotrg.jl:46-84); tnr_finalize returns the pure norm and
+ * (impurityhotrg.jl:26-46): four host tensors of the same dims (4 legs, column-major).
+ * tnr_step steps all four (impurityhotrg.jl:48-84); tnr_finalize returns the pure norm and
  * tnr_finalize_impurity the four norms of finalize!(::ImpurityHOTRG) (finalize.jl:91-101). */
 int tnr_create_impurity_hotrg(tnr_handle* out, const int64_t* dims, const double* T,
                               const double* T_imp_order1_1, const double* T_imp_order1_2,
                               const double* T_imp_order2, const tnr_options* opts);
-/* ImpurityTRG(T, T_imp1, T_imp2, T_imp3, T_imp4) (impuritytrg.jl:37-59): five host tensors
+/* ImpurityTRG(T, T_imp1, T_imp2, T_imp3, T_imp4) (impuritytrg.jl:38-61): five host tensors
  * of the same dims; tnr_step steps all five (impuritytrg.jl:63-91). */
 int tnr_create_impurity_trg(tnr_handle* out, const int64_t* dims, const double* T, const double* T_imp1,
                             const double* T_imp2, const double* T_imp3, const double* T_imp4,
                             const tnr_options* opts);
 /* CorrelationHOTRG(Tpure, Timp1, Timp2, dist) (correlationhotrg.jl:51-68): two first-order
  * impurities 2^dist sites apart, merged into one at step dist (dist >= 0).  tnr_step runs
- * step! with its phase finalizer (correlationhotrg.jl:92-135); tnr_finalize and tnr_run do not
+ * step! with its phase finalizer (correlationhotrg.jl:94-135); tnr_finalize and tnr_run do not
  * apply to it. */
 int tnr_create_correlation_hotrg(tnr_handle* out, const int64_t* dims, const double* Tpure, const double* Timp1,
                                  const double* Timp2, int dist, const tnr_options* opts);
@@ -131,7 +131,7 @@ int tnr_run_impurity(tnr_handle h, int chi, int maxiter, int finalize_beginning,
                      double* norms_out, size_t cap, size_t* n_out);
 
 /* One coarse-graining step with truncrank(chi).
- * Replaces step!(scheme, trunc) (tnrscheme.jl:2; trg.jl:94, btrg.jl:166,
+ * Replaces step!(scheme, trunc) (tnrscheme.jl:2; trg.jl:35, btrg.jl:60,
  * hotrg.jl:154, hotrg3d.jl:127). */
 int tnr_step(tnr_handle h, int chi);
 

@@ -118,7 +118,7 @@ def permute(t: Tensor, perm, nout):
 
 # ---------------------------------------------------------------------------
 # truncated decompositions (MatrixAlgebraKit 0.6.1, called at
-# src/utility/projectors.jl:215, src/schemes/btrg.jl:167,178,
+# src/utility/projectors.jl:215, src/schemes/btrg.jl:61,72,
 # src/schemes/hotrg.jl:103,110,139,146, src/schemes/hotrg3d.jl:93,96)
 # ---------------------------------------------------------------------------
 def _row_col_keys(t: Tensor, nrow):
@@ -368,7 +368,7 @@ def random_hotrg_tensor(chi, seed, decay=6.0):
 # schemes
 # ---------------------------------------------------------------------------
 class TRG:
-    """src/schemes/trg.jl:85-92"""
+    """src/schemes/trg.jl:26-33"""
     scalefactor = 2.0
 
     def __init__(self, T: Tensor):
@@ -378,7 +378,7 @@ class TRG:
 
 
 class BTRG:
-    """src/schemes/btrg.jl:132-154: S1 = id(space(T,2)), S2 = id(space(T,1)), k = -1/2."""
+    """src/schemes/btrg.jl:26-48: S1 = id(space(T,2)), S2 = id(space(T,1)), k = -1/2."""
     scalefactor = 2.0
 
     def __init__(self, T: Tensor, k=-0.5):
@@ -413,7 +413,7 @@ class HOTRG_3D:
 
 
 class ImpurityHOTRG:
-    """src/schemes/impurityhotrg.jl:25-44: the pure tensor, the two first-order impurity
+    """src/schemes/impurityhotrg.jl:26-46: the pure tensor, the two first-order impurity
     tensors and the second-order one, all of the same spaces."""
 
     def __init__(self, T: Tensor, T_imp_order1_1: Tensor, T_imp_order1_2: Tensor, T_imp_order2: Tensor):
@@ -437,7 +437,7 @@ class ATRG:
 
 
 class CorrelationHOTRG:
-    """src/schemes/correlationhotrg.jl:29-69: the pure tensor and two first-order impurities
+    """src/schemes/correlationhotrg.jl:29-71: the pure tensor and two first-order impurities
     2^dist sites apart; after dist steps they merge into one impurity (Timp_final)."""
 
     def __init__(self, Tpure: Tensor, Timp1: Tensor, Timp2: Tensor, dist: int):
@@ -453,7 +453,7 @@ class CorrelationHOTRG:
 
 
 class ImpurityTRG:
-    """src/schemes/impuritytrg.jl:37-59: the pure tensor and impurity tensors on the four
+    """src/schemes/impuritytrg.jl:38-61: the pure tensor and impurity tensors on the four
     sites of a plaquette, all of the same spaces."""
 
     def __init__(self, T: Tensor, T_imp1: Tensor, T_imp2: Tensor, T_imp3: Tensor, T_imp4: Tensor):
@@ -473,7 +473,7 @@ def SVD12(T: Tensor, chi):
 
 
 def step_trg(scheme: TRG, chi):
-    """src/schemes/trg.jl:94-100"""
+    """src/schemes/trg.jl:35-41"""
     T = scheme.T
     A, B, s1 = SVD12(T, chi)
     Tp = permute(T, (1, 3, 0, 2), 2)                       # transpose(T, ((2,4),(1,3)))
@@ -485,7 +485,7 @@ def step_trg(scheme: TRG, chi):
 
 
 def _trg_contract(D, B, C, A):
-    """T[-1 -2; -3 -4] := D[-2; 1 2] B[-1; 4 1] C[4 3; -3] A[3 2; -4] (src/schemes/trg.jl:98-99)"""
+    """T[-1 -2; -3 -4] := D[-2; 1 2] B[-1; 4 1] C[4 3; -3] A[3 2; -4] (src/schemes/trg.jl:39)"""
     a, q, N = _ein('bpq,arp,rsc,sqd->abcd', D, B, C, A, path=[(0, 1), (0, 1), (0, 1)])
     return Tensor(a, 2, q, N)
 
@@ -522,7 +522,7 @@ def finalize_impurity_trg(scheme: ImpurityTRG):
 
 
 def pseudopow(s, a, tol=EPS ** 0.75):
-    """src/schemes/btrg.jl:156-164"""
+    """src/schemes/btrg.jl:50-58"""
     out = s.copy()
     m = s >= tol
     out[m] = s[m] ** a
@@ -530,7 +530,7 @@ def pseudopow(s, a, tol=EPS ** 0.75):
 
 
 def step_btrg(scheme: BTRG, chi):
-    """src/schemes/btrg.jl:166-200"""
+    """src/schemes/btrg.jl:60-94"""
     T = scheme.T
     k = scheme.k
     U, s, Vh, _, bq = svd_trunc(T, 2, chi)
@@ -684,7 +684,7 @@ def _combine(terms):
 
 
 def step_impurity_hotrg(scheme: ImpurityHOTRG, chi):
-    """src/schemes/impurityhotrg.jl:46-84: the y projector of the pure tensor, x-steps of the
+    """src/schemes/impurityhotrg.jl:48-84: the y projector of the pure tensor, x-steps of the
     pure / impurity pairs; then the x projector and y-steps, with the symmetrised averages."""
     for proj, stepf in ((_hotrg_yproj, _hotrg_step_x), (_hotrg_xproj, _hotrg_step_y)):
         T, T11, T12, T2 = scheme.T, scheme.T_imp_order1_1, scheme.T_imp_order1_2, scheme.T_imp_order2
@@ -740,14 +740,14 @@ def step_atrg(scheme: ATRG, chi):
 
 
 def _correlation_phase(scheme: CorrelationHOTRG):
-    """src/schemes/correlationhotrg.jl:175-183: 1 for the first dist steps, 2 for the merge, then 3."""
+    """src/schemes/correlationhotrg.jl:177-185: 1 for the first dist steps, 2 for the merge, then 3."""
     if scheme.iter < scheme.dist:
         return 1
     return 2 if scheme.iter == scheme.dist else 3
 
 
 def step_correlation_hotrg(scheme: CorrelationHOTRG, chi):
-    """src/schemes/correlationhotrg.jl:92-135,185-250: the y projector of the pure tensor and
+    """src/schemes/correlationhotrg.jl:94-135,177-250: the y projector of the pure tensor and
     x-steps, then the x projector and y-steps (the order of ImpurityHOTRG); an impurity step is
     the average of the (impurity, pure) and (pure, impurity) steps.  Phase 2's x-step merges the
     two impurities (their average, both orders); finalize! follows (src/utility/finalize.jl:104-124):

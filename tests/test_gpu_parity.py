@@ -127,7 +127,7 @@ def test_hotrg_random_single_step(tnr, oracle, chi, seed):
 
 
 def test_impurity_hotrg(tnr, oracle):
-    """ImpurityHOTRG (src/schemes/impurityhotrg.jl:46-84, finalize.jl:91-101) on the Ising
+    """ImpurityHOTRG (src/schemes/impurityhotrg.jl:48-84, finalize.jl:91-101) on the Ising
     model at beta_c with the magnetisation impurity, truncrank(16), 4 steps: the four norms
     of every step (pure, +1, -1, second order) against the oracle to 1e-10.  The first-order
     impurity is Z2-odd, so its trace vanishes up to rounding: an absolute floor of 1e-12 of

@@ -84,7 +84,7 @@ def test_free_energy_formula(oracle):
 
 
 def test_pseudopow(oracle):
-    # src/schemes/btrg.jl:156-164: values below eps^(3/4) are left unchanged
+    # src/schemes/btrg.jl:50-58: values below eps^(3/4) are left unchanged
     o = oracle
     s = np.array([4.0, 1e-13, 0.25])
     np.testing.assert_allclose(o.pseudopow(s, -0.5), [0.5, 1e-13, 2.0])

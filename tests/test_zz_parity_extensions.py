@@ -59,7 +59,7 @@ def test_impurity_trg_high_temperature(tnr):
 
 
 def test_correlation_hotrg(tnr, oracle):
-    """CorrelationHOTRG (src/schemes/correlationhotrg.jl:92-250, finalize.jl:104-124) with the
+    """CorrelationHOTRG (src/schemes/correlationhotrg.jl:94-250, finalize.jl:104-124) with the
     magnetisation impurity at both ends.  At beta_c, dist 2, truncrank(16), 6 steps, every
     step's three norms against the oracle to 1e-10 (the phase-1 traces of the Z2-odd
     impurities vanish up to rounding: an absolute floor of 1e-12 of the largest norm); then

@@ -251,12 +251,12 @@ class _Scheme:
 
 
 class TRG(_Scheme):
-    """Tensor Renormalization Group (src/schemes/trg.jl:85-100); rescales by sqrt(2)."""
+    """Tensor Renormalization Group (src/schemes/trg.jl:26-41); rescales by sqrt(2)."""
     kind = TNR_TRG
 
 
 class BTRG(_Scheme):
-    """Bond-weighted TRG (src/schemes/btrg.jl:132-200); ``BTRG(T, k=-0.5)``."""
+    """Bond-weighted TRG (src/schemes/btrg.jl:26-94); ``BTRG(T, k=-0.5)``."""
     kind = TNR_BTRG
 
     def __init__(self, T, k=-0.5, **kw):
@@ -328,7 +328,7 @@ class _ImpurityScheme(_Scheme):
 
 class ImpurityHOTRG(_ImpurityScheme):
     """``ImpurityHOTRG(T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)``
-    (src/schemes/impurityhotrg.jl:25-84): four tensors of the same spaces; ``run`` returns
+    (src/schemes/impurityhotrg.jl:26-84): four tensors of the same spaces; ``run`` returns
     the (pure, +1, -1, second-order) norm tuples of finalize!(::ImpurityHOTRG)."""
     kind = TNR_IMPURITY_HOTRG
     scalefactor = 4.0
@@ -340,7 +340,7 @@ class ImpurityHOTRG(_ImpurityScheme):
 
 
 class ImpurityTRG(_ImpurityScheme):
-    """``ImpurityTRG(T, T_imp1, T_imp2, T_imp3, T_imp4)`` (src/schemes/impuritytrg.jl:37-59):
+    """``ImpurityTRG(T, T_imp1, T_imp2, T_imp3, T_imp4)`` (src/schemes/impuritytrg.jl:38-61):
     the pure tensor and the four sites of an impurity plaquette; ``run`` returns the
     (pure, plaquette) norm tuples of finalize!(::ImpurityTRG) (src/utility/finalize.jl:75-88)."""
     kind = TNR_IMPURITY_TRG
@@ -353,7 +353,7 @@ class ImpurityTRG(_ImpurityScheme):
 
 
 class CorrelationHOTRG(_ImpurityScheme):
-    """``CorrelationHOTRG(Tpure, Timp1, Timp2, dist)`` (src/schemes/correlationhotrg.jl:29-68): two
+    """``CorrelationHOTRG(Tpure, Timp1, Timp2, dist)`` (src/schemes/correlationhotrg.jl:29-71): two
     first-order impurities 2^dist sites apart, merged into one at step dist.  ``run`` returns the
     (n, n_1, n_2) / (n, n_imp, n_imp) tuple of every step (correlationhotrg.jl:138-162); ``step``
     runs step! with its phase finalizer; ``correlation()`` is |tr Timp_final| / |tr Tpure|."""

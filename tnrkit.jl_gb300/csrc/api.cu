@@ -112,7 +112,7 @@ int create_common(tnr_handle* out, int kind, int nlegs, const int64_t* dims, con
         TNR_CUDA(cudaMemcpyAsync(s.T.p(), data, s.T.size() * sizeof(double),
                                  device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s.ctx->stream));
         if (kind == TNR_BTRG) {
-            // S1 = id(space(T, 2)), S2 = id(space(T, 1))  (btrg.jl:145-150)
+            // S1 = id(space(T, 2)), S2 = id(space(T, 1))  (btrg.jl:39-44)
             s.S1 = make_dt(s.ctx->pool.get(), {dims[1]});
             s.S2 = make_dt(s.ctx->pool.get(), {dims[0]});
             std::vector<double> ones((size_t)std::max(dims[0], dims[1]), 1.0);

@@ -40,7 +40,7 @@ static void svd12_b(Ctx& c, const DT& M4, int chi, int B, DT& A, DT& Bv) {
     row_scale_batched(c, Bv.p(), k, n * B, sv.d(), 1, n);
 }
 
-// step!(::TRG) for a batch (src/schemes/trg.jl:94-100)
+// step!(::TRG) for a batch (src/schemes/trg.jl:35-41)
 static void step_trg_b(Ctx& c, BatchState& s, int chi) {
     const int B = s.B;
     DT A, Bv, C, D;
@@ -55,7 +55,7 @@ static void step_trg_b(Ctx& c, BatchState& s, int chi) {
                    true, B);
 }
 
-// step!(::BTRG) for a batch (src/schemes/btrg.jl:166-200)
+// step!(::BTRG) for a batch (src/schemes/btrg.jl:60-94)
 static void step_btrg_b(Ctx& c, BatchState& s, int chi) {
     const int B = s.B;
     const double kexp = s.k;

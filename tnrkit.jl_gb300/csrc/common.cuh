@@ -287,7 +287,7 @@ void lincomb2(Ctx& c, double* out, int64_t n, double a, const double* x, double 
 void trace2d(Ctx& c, const double* T, const int64_t* d, double* out);
 void trace_btrg(Ctx& c, const double* T, const int64_t* d, const double* S1, const double* S2, double* out);
 void trace3d(Ctx& c, const double* T, const int64_t* d, double* out);
-// pseudopow of a diagonal (btrg.jl:156-164): out = s >= tol ? s^a : s
+// pseudopow of a diagonal (btrg.jl:50-58): out = s >= tol ? s^a : s
 void pseudopow(Ctx& c, const double* s, int n, double a, double* out);
 void check_finite(Ctx& c, const double* x, int64_t n);
 

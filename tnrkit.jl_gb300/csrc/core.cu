@@ -698,7 +698,7 @@ void trace3d(Ctx& c, const double* T, const int64_t* d, double* out) {
     check_launch("trace3d");
 }
 
-// pseudopow (src/schemes/btrg.jl:156-164), tol = eps(Float64)^(3/4)
+// pseudopow (src/schemes/btrg.jl:50-58), tol = eps(Float64)^(3/4)
 __global__ void k_pseudopow(const double* s, int n, double a, double tol, double* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = s[i] < tol ? s[i] : pow(s[i], a);

@@ -52,7 +52,7 @@ static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B, bool canonical
     s.record(r);
 }
 
-// T[-1 -2;-3 -4] = D[-2;1 2] B[-1;4 1] C[4 3;-3] A[3 2;-4]  (src/schemes/trg.jl:98-99)
+// T[-1 -2;-3 -4] = D[-2;1 2] B[-1;4 1] C[4 3;-3] A[3 2;-4]  (src/schemes/trg.jl:39)
 //   D[b,p,q] B[a,r,p] C[r,s,c] A[s,q,d]
 static DT trg_contract(Ctx& c, const DT& D, const DT& B, const DT& C, const DT& A) {
     DT X = contract(c, D, {Lb, Lp, Lq}, B, {La, Lr, Lp}, {La, Lb, Lq, Lr});
@@ -60,7 +60,7 @@ static DT trg_contract(Ctx& c, const DT& D, const DT& B, const DT& C, const DT& 
     return contract(c, X, {La, Lb, Lq, Lr}, Y, {Lq, Lr, Lc, Ld}, {La, Lb, Lc, Ld});
 }
 
-// step!(::TRG) (src/schemes/trg.jl:94-100)
+// step!(::TRG) (src/schemes/trg.jl:35-41)
 static void step_trg(Scheme& s, int chi) {
     Ctx& c = *s.ctx;
     DT& T = s.T;
@@ -174,7 +174,7 @@ static void step_impurity_trg(Scheme& s, int chi) {
     s.site[3] = std::move(S4);
 }
 
-// step!(::BTRG) (src/schemes/btrg.jl:166-200)
+// step!(::BTRG) (src/schemes/btrg.jl:60-94)
 static void step_btrg(Scheme& s, int chi) {
     Ctx& c = *s.ctx;
     DT& T = s.T;
@@ -383,7 +383,7 @@ static void step_hotrg(Scheme& s, int chi) {
     hotrg_step_x(s, Uy);
 }
 
-// step!(::ImpurityHOTRG) (src/schemes/impurityhotrg.jl:46-84): the y projector of the pure
+// step!(::ImpurityHOTRG) (src/schemes/impurityhotrg.jl:48-84): the y projector of the pure
 // tensor with x-steps of the pure / impurity pairs, then the x projector with y-steps;
 // first-order impurities average the two placements, the second order the four
 static void step_impurity_hotrg(Scheme& s, int chi) {
@@ -511,7 +511,7 @@ bool split_step_in_fp64(int kind, int64_t step, const int64_t* dims, int nlegs, 
     return true;
 }
 
-// step!(::CorrelationHOTRG) with its finalizer (src/schemes/correlationhotrg.jl:92-135,175-250;
+// step!(::CorrelationHOTRG) with its finalizer (src/schemes/correlationhotrg.jl:94-135,177-250;
 // src/utility/finalize.jl:104-124).  Phase 1 (the first dist steps) carries both impurities, phase
 // 2 merges them in its x-step, phase 3 carries the merged one; each half step is the y projector
 // of the pure tensor and x-steps, then the x projector and y-steps, an impurity step being the
