@@ -47,6 +47,7 @@ extern "C" {
 #define TNR_IMPURITY_TRG   6 /* impuritytrg.jl:38-91; created by tnr_create_impurity_trg */
 #define TNR_CORRELATION_HOTRG 7 /* correlationhotrg.jl:29-250; created by tnr_create_correlation_hotrg */
 #define TNR_ATRG           8 /* atrg.jl:26-81; tnr_create with a 4-leg tensor */
+#define TNR_ATRG_3D        9 /* atrg3d.jl:26-90; tnr_create with a 6-leg tensor */
 
 /* ---- arithmetic of the bulk contractions -------------------------------- */
 #define TNR_PREC_F64    0  /* plain path: every operation in FP64                      */

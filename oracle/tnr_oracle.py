@@ -436,6 +436,17 @@ class ATRG:
         self.svals = []
 
 
+class ATRG_3D:
+    """src/schemes/atrg3d.jl:26-33: the central 6-leg tensor T[1 2; 3 4 5 6]; one step is three
+    half steps, one along each axis (volume factor 8).  Dense (Trivial) arrays only."""
+    scalefactor = 8.0
+
+    def __init__(self, T: Tensor):
+        assert T.ndim == 6
+        self.T = Tensor(np.array(T.a), 2, None, 1)
+        self.svals = []
+
+
 class CorrelationHOTRG:
     """src/schemes/correlationhotrg.jl:29-71: the pure tensor and two first-order impurities
     2^dist sites apart; after dist steps they merge into one impurity (Timp_final)."""
@@ -739,6 +750,79 @@ def step_atrg(scheme: ATRG, chi):
     scheme.svals += sv1 + sv2
 
 
+def _svd_dense(M, chi):
+    """truncated SVD of a dense matrix (rank chi): U, s, Vh"""
+    U, s, Vh = np.linalg.svd(M, full_matrices=False)
+    k = min(chi, len(s))
+    return U[:, :k], s[:k], Vh[:k]
+
+
+def _atrg3d_half(T, chi):
+    """_step!(::ATRG_3D) (src/schemes/atrg3d.jl:35-78) on a dense T[t1..t6]: SVD of (2,5,6) x
+    (3,4,1) into A S D; M = (S D)(A S) SVD'd into X Y (sqrt(S) on both); AX and YD; the R factors
+    of left_orth / right_orth of YD and AX on two leg pairs give the oblique projectors
+    (R2 V1^T s1^-1/2, s1^-1/2 U1^T R1 with pseudopow), and T = G H."""
+    d = T.shape
+    U, s, Vh = _svd_dense(T.transpose(1, 4, 5, 2, 3, 0).reshape(d[1] * d[4] * d[5], -1), chi)
+    k = len(s)
+    U4 = U.reshape(d[1], d[4], d[5], k)                 # U[t2, t5, t6; k]
+    V4 = Vh.reshape(k, d[2], d[3], d[0])                # V[k; t3, t4, t1]
+    A = U4.transpose(3, 0, 1, 2)                        # A[k, t2; t5, t6]
+    D = V4.transpose(3, 0, 1, 2)                        # D[t1, k; t3, t4]
+    C = (U4 * s).transpose(3, 0, 1, 2)
+    B = (s[:, None, None, None] * V4).transpose(3, 0, 1, 2)
+    # M[-1 -2; -3 -4 -5 -6] := B[1 -2; -3 -4] C[-1 1; -5 -6]
+    M = np.einsum('xbcd,axef->abcdef', B, C, optimize=True)
+    m = M.shape
+    U, s2, Vh = _svd_dense(M.transpose(1, 4, 5, 2, 3, 0).reshape(m[1] * m[4] * m[5], -1), chi)
+    k2, r = len(s2), np.sqrt(s2)
+    X = (U * r).reshape(m[1], m[4], m[5], k2).transpose(3, 0, 1, 2)                  # X[k2, m2; m5, m6]
+    Y = (r[:, None] * Vh).reshape(k2, m[2], m[3], m[0]).transpose(3, 0, 1, 2)      # Y[m1, k2; m3, m4]
+    # AX[-1 -2; -3 -4 -5 -6] := A[1 -2; -3 -5] X[-1 1; -4 -6];  YD likewise with Y, D
+    AX = np.einsum('xbce,axdf->abcdef', A, X, optimize=True)
+    YD = np.einsum('xbce,axdf->abcdef', Y, D, optimize=True)
+    ax, yd = AX.shape, YD.shape
+
+    def r_left(Mat):                                    # left_orth: Mat = Q R, the R factor
+        return np.linalg.qr(Mat, mode='r')
+
+    def r_right(Mat):                                   # right_orth: Mat = L Q, the L factor
+        return np.linalg.qr(Mat.T, mode='r').T
+
+    R1 = r_left(YD.reshape(-1, yd[4] * yd[5]))                                          # [r; y5 y6]
+    R2 = r_right(AX.transpose(4, 5, 0, 1, 2, 3).reshape(ax[4] * ax[5], -1))            # [a5 a6; r]
+    R3 = r_left(YD.transpose(0, 1, 4, 5, 2, 3).reshape(-1, yd[2] * yd[3]))              # [r; y3 y4]
+    R4 = r_right(AX.transpose(2, 3, 0, 1, 4, 5).reshape(ax[2] * ax[3], -1))            # [a3 a4; r]
+
+    def projectors(Rl, Rr):
+        U1, s1, V1h = _svd_dense(Rl @ Rr, chi)
+        inv = pseudopow(s1, -0.5)
+        return Rr @ V1h.T * inv, (inv[:, None] * U1.T) @ Rl      # Proj_a [pq; k], Proj_b [k; pq]
+
+    P1, P2 = projectors(R1, R2)
+    P3, P4 = projectors(R3, R4)
+    # H[-1 -2; -3 -4] := YD[-1 -2; 1 2 3 4] Proj_3[1 2; -3] Proj_1[3 4; -4]
+    YDm = YD.reshape(yd[0] * yd[1], yd[2] * yd[3], yd[4] * yd[5])
+    H = np.einsum('xpq,pc,qd->xcd', YDm, P3, P1, optimize=True).reshape(yd[0], yd[1], P3.shape[1], P1.shape[1])
+    # G[-1 -2; -3 -4] := AX[-1 -2; 1 2 3 4] Proj_4[-3; 1 2] Proj_2[-4; 3 4]
+    AXm = AX.reshape(ax[0] * ax[1], ax[2] * ax[3], ax[4] * ax[5])
+    G = np.einsum('xpq,cp,dq->xcd', AXm, P4, P2, optimize=True).reshape(ax[0], ax[1], P4.shape[0], P2.shape[0])
+    # T[-1 -2; -3 -4 -5 -6] := G[1 -2; -5 -6] H[-1 1; -3 -4]
+    Tn = np.einsum('xbef,axcd->abcdef', G, H, optimize=True)
+    return Tn, [s, s2]
+
+
+def step_atrg3d(scheme: ATRG_3D, chi):
+    """step!(::ATRG_3D) (src/schemes/atrg3d.jl:80-90): three half steps, each followed by
+    permute(T, ((4, 6), (2, 5, 1, 3)))."""
+    T = scheme.T.a
+    for _ in range(3):
+        T, sv = _atrg3d_half(T, chi)
+        T = T.transpose(3, 5, 1, 4, 0, 2)
+        scheme.svals += sv
+    scheme.T = Tensor(np.ascontiguousarray(T), 2, None, 1)
+
+
 def _correlation_phase(scheme: CorrelationHOTRG):
     """src/schemes/correlationhotrg.jl:177-185: 1 for the first dist steps, 2 for the merge, then 3."""
     if scheme.iter < scheme.dist:
@@ -821,6 +905,8 @@ def step(scheme, chi):
         step_hotrg3d(scheme, chi)
     elif isinstance(scheme, ATRG):
         step_atrg(scheme, chi)
+    elif isinstance(scheme, ATRG_3D):
+        step_atrg3d(scheme, chi)
     elif isinstance(scheme, ImpurityHOTRG):
         step_impurity_hotrg(scheme, chi)
     elif isinstance(scheme, ImpurityTRG):
@@ -843,8 +929,8 @@ def finalize(scheme):
     elif isinstance(scheme, BTRG):
         # T[1 2; 4 3] S1[4; 2] S2[3; 1] with diagonal S1, S2
         n = abs(_btrg_trace(T, scheme.S1, scheme.S2))
-    elif isinstance(scheme, HOTRG_3D):
-        n = abs(np.einsum('aabcbc->', T))               # T[1 1; 2 3 2 3]
+    elif isinstance(scheme, (HOTRG_3D, ATRG_3D)):
+        n = abs(np.einsum('aabcbc->', T))               # T[1 1; 2 3 2 3] (finalize.jl:56-66)
     else:
         raise TypeError(type(scheme))
     scheme.T.a = T / n

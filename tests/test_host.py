@@ -113,8 +113,8 @@ def test_python_constants_match_header(tnr):
     d = header_defines()
     assert (tnr.TNR_TRG, tnr.TNR_BTRG, tnr.TNR_HOTRG, tnr.TNR_HOTRG_3D) == (
         d["TNR_TRG"], d["TNR_BTRG"], d["TNR_HOTRG"], d["TNR_HOTRG_3D"])
-    assert (tnr.TNR_IMPURITY_HOTRG, tnr.TNR_IMPURITY_TRG, tnr.TNR_CORRELATION_HOTRG, tnr.TNR_ATRG) == (
-        d["TNR_IMPURITY_HOTRG"], d["TNR_IMPURITY_TRG"], d["TNR_CORRELATION_HOTRG"], d["TNR_ATRG"])
+    assert (tnr.TNR_IMPURITY_HOTRG, tnr.TNR_IMPURITY_TRG, tnr.TNR_CORRELATION_HOTRG, tnr.TNR_ATRG, tnr.TNR_ATRG_3D) == (
+        d["TNR_IMPURITY_HOTRG"], d["TNR_IMPURITY_TRG"], d["TNR_CORRELATION_HOTRG"], d["TNR_ATRG"], d["TNR_ATRG_3D"])
     assert (tnr.default_Finalizer.code, tnr.two_by_two_Finalizer.code) == (
         d["TNR_FINALIZER_DEFAULT"], d["TNR_FINALIZER_TWO_BY_TWO"])
     assert (tnr.PREC_F64, tnr.PREC_SPLIT) == (d["TNR_PREC_F64"], d["TNR_PREC_SPLIT"])

@@ -397,3 +397,13 @@ def test_atrg_ising(oracle):
         x1, x2 = o.gu_wen_ratio(s)
         for v in (o.ground_state_degeneracy(s), x1, x2):
             assert v == pytest.approx(want, rel=1e-2)
+
+
+@pytest.mark.slow
+def test_atrg3d_ising(oracle):
+    """test/schemes.jl:365-373: ATRG_3D on the 3D Ising tensor, truncrank(12), scalefactor 8:
+    f = -3.507 (Phys. Rev. B 102, 054432, Fig. 5) to 5e-3.  Ten steps instead of 25: step i
+    enters f with weight 8^(1-i), so steps 11..25 move it by < 1e-8."""
+    o = oracle
+    data = o.run(o.ATRG_3D(o.classical_ising_3D()), o.truncrank(12), o.maxiter(10))
+    assert o.free_energy(data, o.ISING_BETA_C_3D, scalefactor=8.0) == pytest.approx(-3.507, rel=5e-3)

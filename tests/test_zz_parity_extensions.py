@@ -181,3 +181,16 @@ def test_atrg(tnr, oracle):
         x1, x2 = tnr.gu_wen_ratio(s)
         for v in (tnr.ground_state_degeneracy(s), x1, x2):
             assert v == pytest.approx(want, rel=1e-2)
+
+
+def test_atrg3d(tnr, oracle):
+    """ATRG_3D (src/schemes/atrg3d.jl:35-90) on the 3D Ising tensor: every norm of
+    truncrank(6), maxiter(5) against the oracle to 1e-10 (the engine's QR factors differ from
+    LAPACK's by an orthogonal factor, which the oblique projectors do not see); and the
+    reference's check (test/schemes.jl:365-373): truncrank(12), maxiter(25), f = -3.507 to 5e-3."""
+    o = oracle
+    d = np.array(tnr.run(tnr.ATRG_3D(tnr.classical_ising_3D()), tnr.truncrank(6), tnr.maxiter(5)))
+    do = np.array(o.run(o.ATRG_3D(o.classical_ising_3D()), o.truncrank(6), o.maxiter(5)))
+    np.testing.assert_allclose(d, do, rtol=1e-10)
+    d = tnr.run(tnr.ATRG_3D(tnr.classical_ising_3D()), tnr.truncrank(12), tnr.maxiter(25))
+    assert tnr.free_energy(d, tnr.ising_βc_3D, scalefactor=8.0) == pytest.approx(-3.507, rel=5e-3)

@@ -26,7 +26,8 @@ from .models import (SymTensor, classical_clock, classical_ising, classical_isin
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("TNR_GB300_LIB") or os.path.join(HERE, "libtnr_gb300.so")
 
-TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG, TNR_CORRELATION_HOTRG, TNR_ATRG = range(1, 9)
+(TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D, TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG, TNR_CORRELATION_HOTRG, TNR_ATRG,
+ TNR_ATRG_3D) = range(1, 10)
 PREC_F64, PREC_SPLIT = 0, 1
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "iteration cap reached",
           4: "CUDA error", 5: "admission refused", 6: "non-finite value", 7: "unsupported", 8: "no device"}
@@ -292,6 +293,14 @@ class ATRG(_Scheme):
     linear rescaling by sqrt(2) (area factor 4 per step)."""
     kind = TNR_ATRG
     scalefactor = 4.0
+
+
+class ATRG_3D(_Scheme):
+    """3D anisotropic TRG (src/schemes/atrg3d.jl:26-90): three half steps per step (volume
+    factor 8); on the device up to truncrank(12) (its QR factors have at most chi^2 columns)."""
+    kind = TNR_ATRG_3D
+    nlegs = 6
+    scalefactor = 8.0
 
 
 class HOTRG_3D(_Scheme):
@@ -565,7 +574,8 @@ class Server:
     ``submit(T, scheme, chi, maxiter)`` returns a request id; ``result(id)`` blocks and
     returns (norms, latency_ms, queue_ms)."""
 
-    KINDS = {"TRG": TNR_TRG, "BTRG": TNR_BTRG, "HOTRG": TNR_HOTRG, "HOTRG_3D": TNR_HOTRG_3D, "ATRG": TNR_ATRG}
+    KINDS = {"TRG": TNR_TRG, "BTRG": TNR_BTRG, "HOTRG": TNR_HOTRG, "HOTRG_3D": TNR_HOTRG_3D, "ATRG": TNR_ATRG,
+             "ATRG_3D": TNR_ATRG_3D}
 
     def __init__(self, hbm_budget_bytes, max_active=32, precision=PREC_F64):
         h = C.c_void_p()

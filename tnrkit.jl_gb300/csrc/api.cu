@@ -84,9 +84,9 @@ int create_common(tnr_handle* out, int kind, int nlegs, const int64_t* dims, con
     if (opts) o = *opts;
     if (!out) return fail(nullptr, TNR_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
-    if ((kind < TNR_TRG || kind > TNR_HOTRG_3D) && kind != TNR_ATRG)
+    if ((kind < TNR_TRG || kind > TNR_HOTRG_3D) && kind != TNR_ATRG && kind != TNR_ATRG_3D)
         return fail(nullptr, TNR_ERR_INVALID_ARG, "unknown scheme kind");
-    int want = kind == TNR_HOTRG_3D ? 6 : 4;
+    int want = kind == TNR_HOTRG_3D || kind == TNR_ATRG_3D ? 6 : 4;
     if (nlegs != want || !dims || !data)
         return fail(nullptr, TNR_ERR_INVALID_ARG, "scheme needs a " + std::to_string(want) + "-leg tensor");
     for (int l = 0; l < nlegs; ++l)

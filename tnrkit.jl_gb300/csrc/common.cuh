@@ -278,6 +278,8 @@ void copy_f64(Ctx& c, double* dst, const double* src, int64_t n);
 // solver's size (160) is refused.
 #define TNR_DEGENERATE_REL 1e-11
 void degenerate_basis(Ctx& c, const std::vector<double>& vals, double* U, int64_t m, double* Vt, int64_t n);
+// Q (m x r, orthonormal columns spanning those of Y) by shifted CholeskyQR3; Y is overwritten
+void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q);
 // dst[0] = |src[0]|
 void abs_copy(Ctx& c, double* dst, const double* src);
 // out[i] = a x[i] + b y[i] (out may alias x or y)

@@ -141,6 +141,129 @@ static void step_atrg(Scheme& s, int chi) {
     s.T = permuted(c, T, {2, 0, 3, 1});
 }
 
+// R of a QR decomposition Mat = Q R of a column-major m x n matrix (m >= n), up to an orthogonal
+// factor on its rows: Q by CholeskyQR3, R = Q^T Mat (n x n).  The oblique projectors of ATRG_3D
+// use R only through R and R^T R, which that factor leaves unchanged.
+static Buf qr_r(Ctx& c, const double* Mat, int64_t m, int64_t n) {
+    TNR_REQUIRE(m >= n && n <= 160, TNR_ERR_UNSUPPORTED, "ATRG_3D: QR of a wide matrix or above 160 columns");
+    Buf Y(c.pool.get(), (size_t)m * n * sizeof(double)), Q(c.pool.get(), (size_t)m * n * sizeof(double));
+    copy_f64(c, Y.d(), Mat, m * n);
+    orth_scaled(c, Y.d(), m, (int)n, Q.d());
+    Buf R(c.pool.get(), (size_t)n * n * sizeof(double));
+    gemm_f64(c, true, false, n, n, m, 1.0, Q.d(), m, 0, Mat, m, 0, 0.0, R.d(), n, 0);
+    return R;
+}
+
+// the oblique projector pair of atrg3d.jl:60-68 from Rl (left_orth R, r x n) and Rrt (the
+// transpose of right_orth's L, r' x n): temp = Rl Rrt^T = U s V^T truncated to chi,
+// Pa[pq; k] = Rrt^T V s^-1/2 (n x k), Pb[k; pq] = s^-1/2 U^T Rl (k x n), pseudopow for s^-1/2
+static void oblique_projectors(Scheme& s, const Buf& Rl, const Buf& Rrt, int64_t n, int chi, Buf& Pa, Buf& Pb, int& k) {
+    Ctx& c = *s.ctx;
+    Buf tmp(c.pool.get(), (size_t)n * n * sizeof(double));
+    gemm_f64(c, false, true, n, n, n, 1.0, Rl.d(), n, 0, Rrt.d(), n, 0, 0.0, tmp.d(), n, 0);
+    k = (int)std::min<int64_t>(chi, n);
+    Buf U(c.pool.get(), (size_t)n * k * sizeof(double)), sv(c.pool.get(), (size_t)k * sizeof(double));
+    Buf Vt(c.pool.get(), (size_t)k * n * sizeof(double)), inv(c.pool.get(), (size_t)k * sizeof(double));
+    TsvdOut r = tsvd(c, tmp.d(), n, n, k, U.d(), sv.d(), Vt.d());
+    s.record(r);
+    pseudopow(c, sv.d(), k, -0.5, inv.d());
+    Pa = Buf(c.pool.get(), (size_t)n * k * sizeof(double));
+    Pb = Buf(c.pool.get(), (size_t)k * n * sizeof(double));
+    gemm_f64(c, true, true, n, k, n, 1.0, Rrt.d(), n, 0, Vt.d(), k, 0, 0.0, Pa.d(), n, 0);
+    col_scale(c, Pa.d(), n, k, n, inv.d(), 0);
+    gemm_f64(c, true, false, k, n, n, 1.0, U.d(), n, 0, Rl.d(), n, 0, 0.0, Pb.d(), k, 0);
+    row_scale(c, Pb.d(), k, n, k, inv.d(), 0);
+}
+
+// _step!(::ATRG_3D) (src/schemes/atrg3d.jl:35-78) on T[t0..t5] (column-major, first leg fastest)
+static DT atrg3d_half(Scheme& s, const DT& T, int chi) {
+    Ctx& c = *s.ctx;
+    DT A, B, C, D, X, Y;
+    {
+        // U, S, V = svd_trunc(permute(T, ((2,5,6), (3,4,1))))
+        DT Tp = permuted(c, T, {1, 4, 5, 2, 3, 0});
+        const int64_t m = Tp.d[0] * Tp.d[1] * Tp.d[2], n = Tp.d[3] * Tp.d[4] * Tp.d[5];
+        const int k = (int)std::min<int64_t>(chi, std::min(m, n));
+        DT U = make_dt(c.pool.get(), {Tp.d[0], Tp.d[1], Tp.d[2], (int64_t)k});
+        DT V = make_dt(c.pool.get(), {(int64_t)k, Tp.d[3], Tp.d[4], Tp.d[5]});
+        Buf sv(c.pool.get(), (size_t)k * sizeof(double));
+        TsvdOut r = tsvd(c, Tp.p(), m, n, k, U.p(), sv.d(), V.p());
+        s.record(r);
+        A = permuted(c, U, {3, 0, 1, 2});            // A[k, t2; t5, t6]
+        D = permuted(c, V, {3, 0, 1, 2});            // D[t1, k; t3, t4]
+        C = copy_of(c, A);
+        B = copy_of(c, D);
+        scale_leg(c, C, 0, sv.d());                  // permute(U S)
+        scale_leg(c, B, 1, sv.d());                  // permute(S V)
+    }
+    {
+        // M[-1 -2; -3 -4 -5 -6] := B[1 -2; -3 -4] C[-1 1; -5 -6]
+        DT M = contract(c, B, {Lx, Lb, Lc, Ld}, C, {La, Lx, Le, Lf}, {La, Lb, Lc, Ld, Le, Lf});
+        B = DT();
+        C = DT();
+        DT Mp = permuted(c, M, {1, 4, 5, 2, 3, 0});
+        M = DT();
+        const int64_t m = Mp.d[0] * Mp.d[1] * Mp.d[2], n = Mp.d[3] * Mp.d[4] * Mp.d[5];
+        const int k = (int)std::min<int64_t>(chi, std::min(m, n));
+        DT U = make_dt(c.pool.get(), {Mp.d[0], Mp.d[1], Mp.d[2], (int64_t)k});
+        DT V = make_dt(c.pool.get(), {(int64_t)k, Mp.d[3], Mp.d[4], Mp.d[5]});
+        Buf sv(c.pool.get(), (size_t)k * sizeof(double));
+        TsvdOut r = tsvd(c, Mp.p(), m, n, k, U.p(), sv.d(), V.p());
+        s.record(r);
+        col_scale(c, U.p(), m, k, m, sv.d(), 1);
+        row_scale(c, V.p(), k, n, k, sv.d(), 1);
+        X = permuted(c, U, {3, 0, 1, 2});            // X[k2, m2; m5, m6]
+        Y = permuted(c, V, {3, 0, 1, 2});            // Y[m1, k2; m3, m4]
+    }
+    // AX[-1 -2; -3 -4 -5 -6] := A[1 -2; -3 -5] X[-1 1; -4 -6], YD likewise from Y and D
+    DT AX = contract(c, A, {Lx, Lb, Lc, Le}, X, {La, Lx, Ld, Lf}, {La, Lb, Lc, Ld, Le, Lf});
+    DT YD = contract(c, Y, {Lx, Lb, Lc, Le}, D, {La, Lx, Ld, Lf}, {La, Lb, Lc, Ld, Le, Lf});
+    A = DT(); D = DT(); X = DT(); Y = DT();
+    const int64_t y0 = YD.d[0], y1 = YD.d[1], x0 = AX.d[0], x1 = AX.d[1];
+    const int64_t ab_y = y0 * y1, ab_x = x0 * x1;
+    const int64_t n1 = YD.d[4] * YD.d[5], n3 = YD.d[2] * YD.d[3];
+    TNR_REQUIRE(n1 == AX.d[4] * AX.d[5] && n3 == AX.d[2] * AX.d[3], TNR_ERR_INVALID_ARG, "ATRG_3D: leg mismatch");
+    Buf P1, P2, P3, P4;
+    int k1 = 0, k3 = 0;
+    {
+        // R1 = left_orth R of YD as (1,2,3,4) x (5,6); R2 = right_orth L of AX as (5,6) x (1,2,3,4),
+        // whose transpose is the R of AX's natural (1,2,3,4) x (5,6) layout
+        Buf R1 = qr_r(c, YD.p(), ab_y * n3, n1);
+        Buf R2t = qr_r(c, AX.p(), ab_x * n3, n1);
+        oblique_projectors(s, R1, R2t, n1, chi, P1, P2, k1);
+    }
+    {
+        // R3 of YD as (1,2,5,6) x (3,4); R4 = right_orth L of AX as (3,4) x (1,2,5,6)
+        DT YDp = permuted(c, YD, {0, 1, 4, 5, 2, 3});
+        DT AXp = permuted(c, AX, {0, 1, 4, 5, 2, 3});
+        Buf R3 = qr_r(c, YDp.p(), ab_y * n1, n3);
+        Buf R4t = qr_r(c, AXp.p(), ab_x * n1, n3);
+        oblique_projectors(s, R3, R4t, n3, chi, P3, P4, k3);
+    }
+    // H[-1 -2; -3 -4] := YD[-1 -2; 1 2 3 4] Proj_3[1 2; -3] Proj_1[3 4; -4]
+    DT Z = contract(c, YD.p(), {ab_y, n3, n1}, {La, Lp, Lq}, P1.d(), {n1, (int64_t)k1}, {Lq, Lb}, {La, Lp, Lb});
+    DT H = contract(c, Z.p(), Z.dims(), {La, Lp, Lb}, P3.d(), {n3, (int64_t)k3}, {Lp, Lc}, {La, Lc, Lb});
+    YD = DT();
+    // G[-1 -2; -3 -4] := AX[-1 -2; 1 2 3 4] Proj_4[-3; 1 2] Proj_2[-4; 3 4]
+    Z = contract(c, AX.p(), {ab_x, n3, n1}, {La, Lp, Lq}, P2.d(), {(int64_t)k1, n1}, {Lb, Lq}, {La, Lp, Lb});
+    DT G = contract(c, Z.p(), Z.dims(), {La, Lp, Lb}, P4.d(), {(int64_t)k3, n3}, {Lc, Lp}, {La, Lc, Lb});
+    Z = DT();
+    // (ab, k3, k1) read as the 4-leg H[y1, y2; k3, k1] and G[x1, x2; k3, k1]
+    H.rank = 4;
+    H.d[0] = y0; H.d[1] = y1; H.d[2] = k3; H.d[3] = k1;
+    G.rank = 4;
+    G.d[0] = x0; G.d[1] = x1; G.d[2] = k3; G.d[3] = k1;
+    // T[-1 -2; -3 -4 -5 -6] := G[1 -2; -5 -6] H[-1 1; -3 -4]
+    return contract(c, G, {Lx, Lb, Le, Lf}, H, {La, Lx, Lc, Ld}, {La, Lb, Lc, Ld, Le, Lf});
+}
+
+// step!(::ATRG_3D) (src/schemes/atrg3d.jl:80-90): three half steps, each followed by
+// permute(T, ((4, 6), (2, 5, 1, 3)))
+static void step_atrg3d(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    for (int i = 0; i < 3; ++i) s.T = permuted(c, atrg3d_half(s, s.T, chi), {3, 5, 1, 4, 0, 2});
+}
+
 // step!(::ImpurityTRG) (src/schemes/impuritytrg.jl:63-91): SVD12 of sites 1 and 3 and of the
 // pure tensor, and of sites 2 and 4 and the pure tensor transposed ((2,4),(1,3)); the new
 // pure and site tensors are five TRG contractions of those factors.  The contractions pair
@@ -502,7 +625,9 @@ static void step_hotrg3d(Scheme& s, int chi) {
     }
 }
 
-int split_fp64_steps(int kind) { return kind == TNR_HOTRG_3D ? TNR_SPLIT_FP64_STEPS_3D : TNR_SPLIT_FP64_STEPS_2D; }
+int split_fp64_steps(int kind) {
+    return kind == TNR_HOTRG_3D || kind == TNR_ATRG_3D ? TNR_SPLIT_FP64_STEPS_3D : TNR_SPLIT_FP64_STEPS_2D;
+}
 
 bool split_step_in_fp64(int kind, int64_t step, const int64_t* dims, int nlegs, int chi) {
     if (step >= split_fp64_steps(kind)) return false;
@@ -582,6 +707,7 @@ void Scheme::step(int chi, double* d_corr) {
         case TNR_HOTRG: step_hotrg(*this, chi); break;
         case TNR_HOTRG_3D: step_hotrg3d(*this, chi); break;
         case TNR_ATRG: step_atrg(*this, chi); break;
+        case TNR_ATRG_3D: step_atrg3d(*this, chi); break;
         case TNR_IMPURITY_HOTRG: step_impurity_hotrg(*this, chi); break;
         case TNR_IMPURITY_TRG: step_impurity_trg(*this, chi); break;
         case TNR_CORRELATION_HOTRG: {
@@ -615,7 +741,8 @@ void Scheme::finalize_async(double* d_norm) {
         case TNR_HOTRG:
         case TNR_ATRG: trace2d(c, T.p(), T.d, d_norm); break;
         case TNR_BTRG: trace_btrg(c, T.p(), T.d, S1.p(), S2.p(), d_norm); break;
-        case TNR_HOTRG_3D: trace3d(c, T.p(), T.d, d_norm); break;
+        case TNR_HOTRG_3D:
+        case TNR_ATRG_3D: trace3d(c, T.p(), T.d, d_norm); break;
         default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
     }
     scale_inplace(c, T.p(), T.size(), d_norm);

@@ -47,6 +47,7 @@ size_t footprint_bytes(int kind, int chi, const std::vector<int64_t>& dims) {
         case TNR_BTRG: entries = 12.0 * c * c * c * c + 4.0 * 128 * c * c; break;
         case TNR_HOTRG: entries = 2.2 * c * c * c * c * c + 12.0 * c * c * c * c; break;
         case TNR_ATRG: entries = 16.0 * c * c * c * c + 4.0 * 128 * c * c; break;
+        case TNR_ATRG_3D: entries = 14.0 * c * c * c * c * c * c; break;
         default: {
             double c6 = c * c * c * c * c * c;
             entries = 10.0 * c6 + 3.0 * std::min(c6 * c * c, 2147483648.0);
@@ -158,8 +159,8 @@ int tnr_server_create(tnr_server* out, size_t hbm_budget_bytes, int max_active, 
 int tnr_server_submit(tnr_server s, int kind, int nlegs, const int64_t* dims, const double* data, int chi,
                       int maxiter, double btrg_k, uint64_t* id_out) {
     if (!s || !dims || !data || !id_out || chi < 1) return TNR_ERR_INVALID_ARG;
-    if ((kind < TNR_TRG || kind > TNR_HOTRG_3D) && kind != TNR_ATRG) return TNR_ERR_INVALID_ARG;
-    if (nlegs != (kind == TNR_HOTRG_3D ? 6 : 4)) return TNR_ERR_INVALID_ARG;
+    if ((kind < TNR_TRG || kind > TNR_HOTRG_3D) && kind != TNR_ATRG && kind != TNR_ATRG_3D) return TNR_ERR_INVALID_ARG;
+    if (nlegs != (kind == TNR_HOTRG_3D || kind == TNR_ATRG_3D ? 6 : 4)) return TNR_ERR_INVALID_ARG;
     Request* r = new (std::nothrow) Request();
     if (!r) return TNR_ERR_OOM;
     r->kind = kind;

@@ -48,7 +48,7 @@ static std::vector<double> to_host(Ctx& c, const double* d, int n) {
 // FP64 precision: FP64 Gram and Cholesky, first shift 11 (m r + r (r + 1)) eps, then none.
 // Split precision: Grams on the split kernel (FP32-level), FP32 Cholesky, shifts
 // 1e-6 max(1, r/16) then 1e-7.
-static void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q) {
+void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q) {
     const bool f64 = c.precision == TNR_PREC_F64;
     const int passes = 3;
     Buf G(c.pool.get(), (size_t)r * r * sizeof(double));
