@@ -10,9 +10,12 @@ Julia binding of the GB300 coarse-graining engine (`libtnr_gb300.so`, C ABI in
     data = run!(scheme, truncrank(16), maxiter(25))
     f = free_energy(data, ising_βc)
 
-`GPU(scheme)` wraps a TNRKit `TRG`, `BTRG`, `HOTRG` or `HOTRG_3D` whose tensor is a
-dense or abelian (Z_N) TensorMap; `run!`, `step!` and `finalize!` on the wrapper
-call the library, which keeps the tensor resident on the device.  `run_batch!` runs
+`GPU(scheme)` wraps a TNRKit `TRG`, `BTRG`, `HOTRG`, `HOTRG_3D`, `ATRG`, `ATRG_3D`,
+`ImpurityHOTRG`, `ImpurityTRG` or `CorrelationHOTRG` whose tensors are dense or abelian
+(Z_N) TensorMaps; `run!`, `step!` and `finalize!` on the wrapper call the library, which
+keeps the tensors resident on the device.  `run!(g, trunc, crit, two_by_two_Finalizer)`
+selects the 2 x 2 finalizer; `cft_data`, `ground_state_degeneracy`, `gu_wen_ratio` and
+`central_charge` read the fixed-point tensor on the device.  `run_batch!` runs
 many wrapped schemes at once, and `Server` is the request loop that admits `run!`
 requests by their HBM footprint:
 
@@ -24,13 +27,16 @@ module TNRKitGB300
 
 using TensorKit
 import TNRKit
-import TNRKit: run!, step!, finalize!, free_energy, maxiter, TNRScheme
+import TNRKit: run!, step!, finalize!, free_energy, maxiter, TNRScheme, cft_data, ground_state_degeneracy,
+    gu_wen_ratio, central_charge
 
 export GPU, run_batch!, Server, submit!, result, TNR_PREC_F64, TNR_PREC_SPLIT
 
 const libtnr = get(ENV, "TNR_GB300_LIB", joinpath(@__DIR__, "..", "libtnr_gb300.so"))
 
 const TNR_TRG, TNR_BTRG, TNR_HOTRG, TNR_HOTRG_3D = 1, 2, 3, 4
+const TNR_IMPURITY_HOTRG, TNR_IMPURITY_TRG, TNR_CORRELATION_HOTRG, TNR_ATRG, TNR_ATRG_3D = 5, 6, 7, 8, 9
+const TNR_FINALIZER_DEFAULT, TNR_FINALIZER_TWO_BY_TWO = 0, 1
 const TNR_PREC_F64, TNR_PREC_SPLIT = 0, 1
 
 # mirrors `tnr_options` (include/tnr_gb300.h)
@@ -58,31 +64,60 @@ check(st, h = C_NULL) = st == 0 || throw(TNRError(st, lasterror(h)))
 
 scheme_kind(scheme) = scheme isa TNRKit.TRG ? TNR_TRG : scheme isa TNRKit.BTRG ? TNR_BTRG :
     scheme isa TNRKit.HOTRG ? TNR_HOTRG : scheme isa TNRKit.HOTRG_3D ? TNR_HOTRG_3D :
+    scheme isa TNRKit.ATRG ? TNR_ATRG : scheme isa TNRKit.ATRG_3D ? TNR_ATRG_3D :
+    scheme isa TNRKit.ImpurityHOTRG ? TNR_IMPURITY_HOTRG : scheme isa TNRKit.ImpurityTRG ? TNR_IMPURITY_TRG :
+    scheme isa TNRKit.CorrelationHOTRG ? TNR_CORRELATION_HOTRG :
     throw(ArgumentError("scheme $(typeof(scheme)) has no GPU path"))
 
-function dense_tensor(scheme)
-    arr = convert(Array, scheme.T)                     # dense column-major T[i1, i2, ...]
+function dense_array(t)
+    arr = convert(Array, t)                            # dense column-major t[i1, i2, ...]
     eltype(arr) <: Real || throw(ArgumentError("the GPU path takes real tensors"))
     return Array{Float64}(arr)
 end
+dense_tensor(scheme) = dense_array(scheme isa TNRKit.CorrelationHOTRG ? scheme.Tpure : scheme.T)
+
+# the impurity tensors in the order of the library's create call
+impurity_tensors(s) = s isa TNRKit.ImpurityHOTRG ? (s.T_imp_order1_1, s.T_imp_order1_2, s.T_imp_order2) :
+    s isa TNRKit.ImpurityTRG ? (s.T_imp1, s.T_imp2, s.T_imp3, s.T_imp4) : (s.Timp1, s.Timp2)
+norms_per_entry(g) = g.kind == TNR_IMPURITY_HOTRG ? 4 : g.kind == TNR_IMPURITY_TRG ? 2 :
+    g.kind == TNR_CORRELATION_HOTRG ? 3 : 1
 
 btrg_k(scheme) = scheme isa TNRKit.BTRG ? scheme.k : -0.5
 
-mutable struct GPU{S <: TNRScheme} <: TNRScheme{Float64, Any}
+mutable struct GPU{S} <: TNRScheme{Float64, Any}
     scheme::S
     handle::Ptr{Cvoid}
-    function GPU(scheme::S; precision = TNR_PREC_F64, seed = 0) where {S <: TNRScheme}
+    kind::Int
+    function GPU(scheme::S; precision = TNR_PREC_F64, seed = 0) where {S}
         kind = scheme_kind(scheme)
         arr = dense_tensor(scheme)
         dims = Int64[size(arr)...]
         k = btrg_k(scheme)
         opts = Ref(Options(precision, k, 1, Ptr{Int32}(C_NULL), UInt64(seed), C_NULL))
         h = Ref{Ptr{Cvoid}}(C_NULL)
-        st = ccall((:tnr_create, libtnr), Cint,
-            (Ptr{Ptr{Cvoid}}, Cint, Cint, Ptr{Int64}, Ptr{Float64}, Ref{Options}),
-            h, kind, length(dims), dims, arr, opts)
+        if kind <= TNR_HOTRG_3D || kind >= TNR_ATRG
+            st = ccall((:tnr_create, libtnr), Cint,
+                (Ptr{Ptr{Cvoid}}, Cint, Cint, Ptr{Int64}, Ptr{Float64}, Ref{Options}),
+                h, kind, length(dims), dims, arr, opts)
+        else
+            imps = map(dense_array, impurity_tensors(scheme))
+            if kind == TNR_IMPURITY_HOTRG
+                st = ccall((:tnr_create_impurity_hotrg, libtnr), Cint,
+                    (Ptr{Ptr{Cvoid}}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{Options}),
+                    h, dims, arr, imps..., opts)
+            elseif kind == TNR_IMPURITY_TRG
+                st = ccall((:tnr_create_impurity_trg, libtnr), Cint,
+                    (Ptr{Ptr{Cvoid}}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                     Ptr{Float64}, Ref{Options}),
+                    h, dims, arr, imps..., opts)
+            else
+                st = ccall((:tnr_create_correlation_hotrg, libtnr), Cint,
+                    (Ptr{Ptr{Cvoid}}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Cint, Ref{Options}),
+                    h, dims, arr, imps..., scheme.dist, opts)
+            end
+        end
         check(st)
-        g = new{S}(scheme, h[])
+        g = new{S}(scheme, h[], kind)
         finalizer(x -> ccall((:tnr_destroy, libtnr), Cint, (Ptr{Cvoid},), x.handle), g)
         return g
     end
@@ -94,20 +129,87 @@ function step!(g::GPU, trunc::TensorKit.MatrixAlgebraKit.TruncationByOrder)
 end
 
 function finalize!(g::GPU)
+    np = norms_per_entry(g)
+    if np > 1
+        out = Vector{Float64}(undef, 4)
+        check(ccall((:tnr_finalize_impurity, libtnr), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.handle, out), g.handle)
+        return Tuple(out[1:np])
+    end
     n = Ref{Float64}(0)
     check(ccall((:tnr_finalize, libtnr), Cint, (Ptr{Cvoid}, Ref{Float64}), g.handle, n), g.handle)
     return n[]
 end
 
-# run!(scheme, truncrank(chi), maxiter(n); finalize_beginning) with the default Finalizer
+# run!(scheme, truncrank(chi), maxiter(n); finalize_beginning) with the scheme's Finalizer;
+# impurity schemes return tuples, CorrelationHOTRG its own run! (no finalize at the beginning)
 function run!(g::GPU, trunc, crit::maxiter; finalize_beginning = true, verbosity = 1)
-    cap = max(crit.n, 1) + 1
-    out = Vector{Float64}(undef, cap)
+    np = norms_per_entry(g)
     n = Ref{Csize_t}(0)
-    check(ccall((:tnr_run, libtnr), Cint,
-        (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Float64}, Csize_t, Ref{Csize_t}),
-        g.handle, trunc.howmany, crit.n, finalize_beginning, out, cap, n), g.handle)
-    return out[1:n[]]
+    if g.kind == TNR_CORRELATION_HOTRG
+        out = Vector{Float64}(undef, 3 * crit.n)
+        check(ccall((:tnr_run_correlation, libtnr), Cint,
+            (Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Csize_t, Ref{Csize_t}),
+            g.handle, trunc.howmany, crit.n, out, length(out), n), g.handle)
+        return [Tuple(out[3i - 2:3i]) for i in 1:n[]]
+    end
+    cap = max(crit.n, 1) + 1
+    out = Vector{Float64}(undef, np * cap)
+    if np > 1
+        st = ccall((:tnr_run_impurity, libtnr), Cint,
+            (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Float64}, Csize_t, Ref{Csize_t}),
+            g.handle, trunc.howmany, crit.n, finalize_beginning, out, length(out), n)
+    else
+        st = ccall((:tnr_run, libtnr), Cint,
+            (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Float64}, Csize_t, Ref{Csize_t}),
+            g.handle, trunc.howmany, crit.n, finalize_beginning, out, length(out), n)
+    end
+    check(st, g.handle)
+    return np == 1 ? out[1:n[]] : [Tuple(out[np * (i - 1) + 1:np * i]) for i in 1:n[]]
+end
+
+# run! with a Finalizer object: the 2 x 2 finalizer (finalize.jl:151) or the default one
+function run!(g::GPU, trunc, crit::maxiter, fin; finalize_beginning = true, verbosity = 1)
+    code = fin === TNRKit.two_by_two_Finalizer ? TNR_FINALIZER_TWO_BY_TWO : TNR_FINALIZER_DEFAULT
+    check(ccall((:tnr_set_finalizer, libtnr), Cint, (Ptr{Cvoid}, Cint), g.handle, code), g.handle)
+    return run!(g, trunc, crit; finalize_beginning, verbosity)
+end
+
+# the fixed-point finalizers (cft.jl): eigenvalues of the transfer matrix on the device, the
+# sorting and filtering of cft.jl:17-36 and 296-309 on the host
+function transfer_eigvals(g::GPU; unitcell = 1)
+    n = size(dense_tensor(g.scheme), 2)^unitcell
+    re, im = Vector{Float64}(undef, n), Vector{Float64}(undef, n)
+    k = Ref{Csize_t}(0)
+    check(ccall((:tnr_transfer_eigvals, libtnr), Cint,
+        (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Csize_t, Ref{Csize_t}), g.handle, unitcell, re, im, n, k),
+        g.handle)
+    return complex.(re[1:k[]], im[1:k[]])
+end
+
+function cft_data(g::GPU; v = 1, unitcell = 1, is_real = true)
+    data = sort(transfer_eigvals(g; unitcell); by = x -> abs(x), rev = true)
+    data = filter(x -> real(x) > 0 && abs(x) > 1.0e-12, data)
+    is_real && (data = real(data))
+    return unitcell * (1 / (2π * v)) * log.(data[1] ./ data)
+end
+
+function ground_state_degeneracy(g::GPU; unitcell = 1)
+    D = transfer_eigvals(g; unitcell)
+    p = filter(!iszero, abs.(D ./ sum(D)))
+    return exp(-sum(p .* log.(p)))
+end
+
+function gu_wen_ratio(g::GPU)
+    x1, x2 = Ref{Float64}(0), Ref{Float64}(0)
+    check(ccall((:tnr_gu_wen_ratio, libtnr), Cint, (Ptr{Cvoid}, Ref{Float64}, Ref{Float64}), g.handle, x1, x2),
+        g.handle)
+    return x1[], x2[]
+end
+
+function central_charge(g::GPU, n::Number)
+    c = Ref{Float64}(0)
+    check(ccall((:tnr_central_charge, libtnr), Cint, (Ptr{Cvoid}, Cdouble, Ref{Float64}), g.handle, n, c), g.handle)
+    return c[]
 end
 
 """
