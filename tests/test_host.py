@@ -253,3 +253,17 @@ def test_transfer_eigvals_routine_on_the_host(tmp_path):
     M = o.transfer_matrix(s)
     ref = np.linalg.eigvals(M)
     assert _match(eig(M), ref) <= 1e-13 * np.abs(ref).max()
+
+
+def test_cft_and_gsd_host_postprocessing(tnr, oracle, monkeypatch):
+    """cft_data and ground_state_degeneracy sort and filter the device's transfer-matrix
+    eigenvalues on the host (src/utility/cft.jl:17-36, 296-309); fed the oracle's eigenvalues,
+    in a scrambled order, they return the oracle's values."""
+    o = oracle
+    s = o.TRG(o.classical_ising())
+    o.run(s, o.truncrank(16), o.maxiter(8))
+    lam = np.linalg.eigvals(o.transfer_matrix(s))
+    rng = np.random.default_rng(1)
+    monkeypatch.setattr(tnr, "transfer_eigvals", lambda scheme, unitcell=1: lam[rng.permutation(len(lam))])
+    np.testing.assert_allclose(tnr.cft_data(None), o.cft_data(s), rtol=1e-12, atol=1e-14)
+    assert tnr.ground_state_degeneracy(None) == pytest.approx(o.ground_state_degeneracy(s), rel=1e-12)

@@ -286,15 +286,15 @@ static void step_impurity_trg(Scheme& s, int chi) {
     svd12(s, s.T, chi, Ap, Bp, true);
     svd_t(s.T, Cp, Dp);
     DT T = trg_contract(c, Dp, Bp, Cp, Ap);
-    DT S1 = trg_contract(c, Dp, B1, C2, Ap);
-    DT S2 = trg_contract(c, D2, B3, Cp, Ap);
-    DT S3 = trg_contract(c, D4, Bp, Cp, A3);
-    DT S4 = trg_contract(c, Dp, Bp, C4, A1);
+    DT N1 = trg_contract(c, Dp, B1, C2, Ap);
+    DT N2 = trg_contract(c, D2, B3, Cp, Ap);
+    DT N3 = trg_contract(c, D4, Bp, Cp, A3);
+    DT N4 = trg_contract(c, Dp, Bp, C4, A1);
     s.T = std::move(T);
-    s.site[0] = std::move(S1);
-    s.site[1] = std::move(S2);
-    s.site[2] = std::move(S3);
-    s.site[3] = std::move(S4);
+    s.site[0] = std::move(N1);
+    s.site[1] = std::move(N2);
+    s.site[2] = std::move(N3);
+    s.site[3] = std::move(N4);
 }
 
 // step!(::BTRG) (src/schemes/btrg.jl:60-94)
