@@ -267,3 +267,17 @@ def test_cft_and_gsd_host_postprocessing(tnr, oracle, monkeypatch):
     monkeypatch.setattr(tnr, "transfer_eigvals", lambda scheme, unitcell=1: lam[rng.permutation(len(lam))])
     np.testing.assert_allclose(tnr.cft_data(None), o.cft_data(s), rtol=1e-12, atol=1e-14)
     assert tnr.ground_state_degeneracy(None) == pytest.approx(o.ground_state_degeneracy(s), rel=1e-12)
+
+
+def test_stopping_criteria(tnr, oracle):
+    """maxiter, convcrit, trivial_convcrit, ``&`` (MultipleCrit) and ATRG_3D_convcrit follow
+    src/utility/stopping.jl and src/schemes/atrg3d.jl:98 (evaluated on host data, as run! does)."""
+    data = [1.0, 0.5, 0.25]
+    assert tnr.maxiter(3)(2, data) and not tnr.maxiter(3)(3, data)
+    assert tnr.trivial_convcrit(0.1)(1, data) and not tnr.trivial_convcrit(0.3)(1, data)
+    both = tnr.maxiter(10) & tnr.convcrit(0.2, lambda steps, d: d[-1])
+    assert isinstance(both, tnr.MultipleCrit) and both(3, data) and not both(10, data)
+    assert not (tnr.maxiter(10) & tnr.convcrit(0.3, lambda steps, d: d[-1]))(3, data)
+    assert tnr.ATRG_3D_convcrit(3, [2.0]) == pytest.approx(abs(np.log(2.0)) / 64.0)
+    with pytest.raises(TypeError):
+        tnr.run(None, tnr.truncrank(4), 5)

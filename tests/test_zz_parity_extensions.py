@@ -194,3 +194,16 @@ def test_atrg3d(tnr, oracle):
     np.testing.assert_allclose(d, do, rtol=1e-10)
     d = tnr.run(tnr.ATRG_3D(tnr.classical_ising_3D()), tnr.truncrank(12), tnr.maxiter(25))
     assert tnr.free_energy(d, tnr.ising_βc_3D, scalefactor=8.0) == pytest.approx(-3.507, rel=5e-3)
+
+
+def test_convcrit_run(tnr, oracle):
+    """run! with maxiter(30) & convcrit (src/utility/stopping.jl:7-22, evaluated on the host
+    after every device step): TRG on the Ising model at beta = 0.40, truncrank(16), stopping
+    once successive norms agree to 1e-8 (step 18 in the oracle, well before maxiter); the norms
+    equal the oracle's maxiter run of as many steps."""
+    o = oracle
+    crit = tnr.maxiter(30) & tnr.convcrit(1e-8, lambda steps, d: abs(d[-1] / d[-2] - 1))
+    d = tnr.run(tnr.TRG(tnr.classical_ising("Trivial", 0.40)), tnr.truncrank(16), crit)
+    assert 2 < len(d) < 31
+    do = o.run(o.TRG(o.classical_ising(0.40, "Trivial")), o.truncrank(16), o.maxiter(len(d) - 1))
+    np.testing.assert_allclose(d, do, rtol=1e-10)

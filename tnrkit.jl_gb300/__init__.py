@@ -143,13 +143,50 @@ class truncrank:
     howmany: int
 
 
+class stopcrit:
+    """A stopping criterion of run! (src/utility/stopping.jl): called with (steps, data), it
+    returns whether to continue; ``a & b`` continues while both do (MultipleCrit)."""
+
+    def __and__(self, other):
+        return MultipleCrit([self, other])
+
+
 @dataclass
-class maxiter:
+class maxiter(stopcrit):
     """``maxiter(n)`` (src/utility/stopping.jl:3-5,18): continue while steps < n."""
     n: int
 
     def __call__(self, steps, data):
         return steps < self.n
+
+
+@dataclass
+class convcrit(stopcrit):
+    """``convcrit(Δ, f)`` (src/utility/stopping.jl:7-10,19): continue while Δ < f(steps, data)."""
+    delta: float
+    f: object
+
+    def __call__(self, steps, data):
+        return self.delta < self.f(steps, data)
+
+
+@dataclass
+class MultipleCrit(stopcrit):
+    """``MultipleCrit(crits)`` (src/utility/stopping.jl:12-22): continue while every criterion does."""
+    crits: list
+
+    def __call__(self, steps, data):
+        return all(c(steps, data) for c in self.crits)
+
+
+def trivial_convcrit(delta):
+    """``trivial_convcrit(Δ)`` (src/utility/stopping.jl:42): continue while Δ < data[end]."""
+    return convcrit(delta, lambda steps, data: data[-1])
+
+
+def ATRG_3D_convcrit(steps, data):
+    """``ATRG_3D_convcrit`` (src/schemes/atrg3d.jl:98): |log(data[end]) 8^(1 - steps)|."""
+    return abs(np.log(data[-1]) * 8.0 ** (1 - steps))
 
 
 def _as_sym(T):
@@ -483,11 +520,25 @@ def run(scheme, trunc, crit, finalizer=None, finalize_beginning=True, verbosity=
     """``run!(scheme, trunc, maxiter(n)[, finalizer]; finalize_beginning)``; the default
     Finalizer unless ``finalizer`` is given (it then stays selected for the scheme).
 
-    Returns the list of norms (n + 1 with ``finalize_beginning``)."""
-    if not isinstance(crit, maxiter):
-        raise TypeError("only maxiter(n) runs on the device path")
+    Returns the list of norms (n + 1 with ``finalize_beginning``).  With maxiter(n) the whole
+    loop runs in the library and the norms come back once; any other criterion (convcrit,
+    MultipleCrit) is evaluated on the host after every step, as run! does
+    (src/schemes/tnrscheme.jl:44-55), from the norm that step's finalize! returns."""
+    if not isinstance(crit, stopcrit):
+        raise TypeError("crit must be a stopping criterion (maxiter, convcrit, a & b)")
     if finalizer is not None:
         set_finalizer(scheme, finalizer)
+    if not isinstance(crit, maxiter):
+        if isinstance(scheme, CorrelationHOTRG):
+            raise TypeError("CorrelationHOTRG's run! takes maxiter(n)")
+        data = [finalize(scheme)] if finalize_beginning else []
+        steps = 0
+        while True:
+            step(scheme, trunc)
+            data.append(finalize(scheme))
+            steps += 1
+            if not crit(steps, data):
+                return data
     nsteps = max(crit.n, 1)
     cap = nsteps + 1
     if isinstance(scheme, CorrelationHOTRG):

@@ -167,6 +167,21 @@ function run!(g::GPU, trunc, crit::maxiter; finalize_beginning = true, verbosity
     return np == 1 ? out[1:n[]] : [Tuple(out[np * (i - 1) + 1:np * i]) for i in 1:n[]]
 end
 
+# run! with any other stopping criterion (convcrit, a & b): the loop of tnrscheme.jl:44-55 on
+# the host, each step and finalize! on the device
+function run!(g::GPU, trunc, crit; finalize_beginning = true, verbosity = 1)
+    g.kind == TNR_CORRELATION_HOTRG && throw(ArgumentError("CorrelationHOTRG's run! takes maxiter(n)"))
+    data = finalize_beginning ? Any[finalize!(g)] : Any[]
+    steps = 0
+    while true
+        step!(g, trunc)
+        push!(data, finalize!(g))
+        steps += 1
+        crit(steps, data) || break
+    end
+    return [d for d in data]
+end
+
 # run! with a Finalizer object: the 2 x 2 finalizer (finalize.jl:151) or the default one
 function run!(g::GPU, trunc, crit::maxiter, fin; finalize_beginning = true, verbosity = 1)
     code = fin === TNRKit.two_by_two_Finalizer ? TNR_FINALIZER_TWO_BY_TWO : TNR_FINALIZER_DEFAULT
