@@ -757,6 +757,16 @@ def _svd_dense(M, chi):
     return U[:, :k], s[:k], Vh[:k]
 
 
+def _left_orth_r(Mat):
+    """left_orth (MatrixAlgebraKit QR): Mat = Q R, the R factor"""
+    return np.linalg.qr(Mat, mode='r')
+
+
+def _right_orth_l(Mat):
+    """right_orth (MatrixAlgebraKit LQ): Mat = L Q, the L factor"""
+    return np.linalg.qr(Mat.T, mode='r').T
+
+
 def _atrg3d_half(T, chi):
     """_step!(::ATRG_3D) (src/schemes/atrg3d.jl:35-78) on a dense T[t1..t6]: SVD of (2,5,6) x
     (3,4,1) into A S D; M = (S D)(A S) SVD'd into X Y (sqrt(S) on both); AX and YD; the R factors
@@ -783,12 +793,7 @@ def _atrg3d_half(T, chi):
     YD = np.einsum('xbce,axdf->abcdef', Y, D, optimize=True)
     ax, yd = AX.shape, YD.shape
 
-    def r_left(Mat):                                    # left_orth: Mat = Q R, the R factor
-        return np.linalg.qr(Mat, mode='r')
-
-    def r_right(Mat):                                   # right_orth: Mat = L Q, the L factor
-        return np.linalg.qr(Mat.T, mode='r').T
-
+    r_left, r_right = _left_orth_r, _right_orth_l
     R1 = r_left(YD.reshape(-1, yd[4] * yd[5]))                                          # [r; y5 y6]
     R2 = r_right(AX.transpose(4, 5, 0, 1, 2, 3).reshape(ax[4] * ax[5], -1))            # [a5 a6; r]
     R3 = r_left(YD.transpose(0, 1, 4, 5, 2, 3).reshape(-1, yd[2] * yd[3]))              # [r; y3 y4]

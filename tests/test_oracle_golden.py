@@ -407,3 +407,22 @@ def test_atrg3d_ising(oracle):
     o = oracle
     data = o.run(o.ATRG_3D(o.classical_ising_3D()), o.truncrank(12), o.maxiter(10))
     assert o.free_energy(data, o.ISING_BETA_C_3D, scalefactor=8.0) == pytest.approx(-3.507, rel=5e-3)
+
+
+def test_atrg3d_projectors_ignore_the_orthogonal_factor(oracle, monkeypatch):
+    """ATRG_3D's oblique projectors (src/schemes/atrg3d.jl:54-68) use the R / L factors of
+    left_orth / right_orth only through R1 R2 and its SVD, so R -> O R and L -> L O' with any
+    orthogonal O, O' leave every norm unchanged: the engine's R = Q^T M from CholeskyQR3 is as
+    good as LAPACK's."""
+    o = oracle
+    rng = np.random.default_rng(4)
+    ref = np.array(o.run(o.ATRG_3D(o.classical_ising_3D()), o.truncrank(6), o.maxiter(4)))
+    left, right = o._left_orth_r, o._right_orth_l
+
+    def orth(n):
+        return np.linalg.qr(rng.standard_normal((n, n)))[0]
+
+    monkeypatch.setattr(o, "_left_orth_r", lambda M: (lambda R: orth(R.shape[0]) @ R)(left(M)))
+    monkeypatch.setattr(o, "_right_orth_l", lambda M: (lambda L: L @ orth(L.shape[1]))(right(M)))
+    got = np.array(o.run(o.ATRG_3D(o.classical_ising_3D()), o.truncrank(6), o.maxiter(4)))
+    np.testing.assert_allclose(got, ref, rtol=1e-11)
