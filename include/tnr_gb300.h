@@ -116,7 +116,7 @@ int tnr_set_finalizer(tnr_handle h, int finalizer);
 /* eig_full of the column transfer matrix M[b, c] = sum_a T_unit[a, b, c, a] of a 2D scheme
  * (TRG, BTRG with its bond weights, HOTRG; cft.jl:5-73, 278-340): the eigenvalues, re + i im, in
  * no particular order (the caller sorts and filters as cft_data / ground_state_degeneracy do).
- * unitcell must be 1; M above 256 x 256 is refused. */
+ * unitcell 1..4 copies of T_unit on the ring (cft.jl:7-15); M above 256 x 256 is refused. */
 int tnr_transfer_eigvals(tnr_handle h, int unitcell, double* re, double* im, size_t cap, size_t* n_out);
 /* gu_wen_ratio (cft.jl:374-396): X1 = |T[1 2;2 1]|^2 / |T[1 2;2 3] T[3 4;4 1]|,
  * X2 = |T[1 2;2 1]|^2 / |T[1 2;3 4] T[4 3;2 1]| of T_unit. */

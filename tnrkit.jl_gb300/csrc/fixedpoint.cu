@@ -101,6 +101,15 @@ __global__ void k_gu_wen_sums(const double* __restrict__ T, int64_t d0, int64_t 
     }
 }
 
+// out[i] = sum_a P[a, i, a] for P of dims (da, inner, da): closes the ring of transfer tensors
+__global__ void k_ring_close(const double* __restrict__ P, int64_t da, int64_t inner, double* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= inner) return;
+    double acc = 0.0;
+    for (int64_t a = 0; a < da; ++a) acc += P[a + da * (i + inner * a)];
+    out[i] = acc;
+}
+
 // dst[0] = |src[0]|^(1/4)
 __global__ void k_root4_abs(double* dst, const double* src) { dst[0] = pow(fabs(src[0]), 0.25); }
 
@@ -111,6 +120,12 @@ static void btrg_weights(const Scheme& s, const double** s1, const double** s2) 
     const bool btrg = s.kind == TNR_BTRG;
     *s1 = btrg ? s.S1.p() : nullptr;
     *s2 = btrg ? s.S2.p() : nullptr;
+}
+
+static DT copy_of_dt(Ctx& c, const DT& t) {
+    DT o = make_dt(c.pool.get(), t.dims());
+    copy_f64(c, o.p(), t.p(), t.size());
+    return o;
 }
 
 static void require_2d(const Scheme& s, const char* what) {
@@ -159,19 +174,62 @@ void Scheme::finalize_two_by_two_async(double* d_norm) {
 
 // eig_full of the unit-cell-1 column transfer matrix (src/utility/cft.jl:7-16, 41-50, 280-296):
 // M[b, c] = sum_a T_unit[a, b, c, a], T_unit = T with BTRG's S1 on leg 2 and S2 on leg 1
+// unitcell u > 1: u copies of T_unit on a ring, indices [i, -i, -(i+u), i+1] with the last leg
+// closing on the first (cft.jl:7-15): the chain T_unit[a1, b1, c1, a2] T_unit[a2, b2, c2, a3] ... is
+// contracted leg by leg, the ring closed by tracing a1 against a_{u+1}, and the (b, c) legs
+// ordered as rows (b1..bu), columns (c1..cu)
+static DT ring_transfer(Scheme& s, int unitcell) {
+    Ctx& c = *s.ctx;
+    DT Tu = copy_of_dt(c, s.T);
+    if (s.kind == TNR_BTRG) {
+        scale_leg(c, Tu, 1, s.S1.p());
+        scale_leg(c, Tu, 0, s.S2.p());
+    }
+    const int64_t da = Tu.d[0], db = Tu.d[1], dc = Tu.d[2];
+    // chain[a1, (b1 c1) ... (bi ci), a_{i+1}]
+    DT chain = copy_of_dt(c, Tu);
+    for (int i = 1; i < unitcell; ++i) {
+        const int64_t inner = chain.size() / (da * da);
+        DT next = contract(c, chain.p(), {da, inner, da}, {La, Lb, Lx}, Tu.p(), {da, db, dc, da}, {Lx, Lc, Ld, Le},
+                           {La, Lb, Lc, Ld, Le});
+        chain = std::move(next);
+    }
+    const int64_t inner = chain.size() / (da * da);
+    DT ring = make_dt(c.pool.get(), {inner});
+    k_ring_close<<<(unsigned)((inner + 255) / 256), 256, 0, c.stream>>>(chain.p(), da, inner, ring.p());
+    check_launch("ring_close");
+    // ring legs (b1, c1, b2, c2, ...) -> (b1, ..., bu, c1, ..., cu)
+    std::vector<int64_t> dims;
+    std::vector<int> perm;
+    for (int i = 0; i < unitcell; ++i) {
+        dims.push_back(db);
+        dims.push_back(dc);
+    }
+    for (int i = 0; i < unitcell; ++i) perm.push_back(2 * i);
+    for (int i = 0; i < unitcell; ++i) perm.push_back(2 * i + 1);
+    ring.rank = (int)dims.size();
+    for (int i = 0; i < ring.rank; ++i) ring.d[i] = dims[i];
+    return permuted(c, ring, perm);
+}
+
 void Scheme::transfer_eigvals(int unitcell, std::vector<double>& re, std::vector<double>& im) {
     Ctx& c = *ctx;
     require_2d(*this, "the transfer matrix");
-    TNR_REQUIRE(unitcell == 1, TNR_ERR_UNSUPPORTED, "the transfer matrix is built for unitcell 1 only");
-    const int64_t n = T.d[1];
+    TNR_REQUIRE(unitcell >= 1 && unitcell <= 4, TNR_ERR_INVALID_ARG, "unitcell must be 1..4");
+    int64_t n = 1;
+    for (int i = 0; i < unitcell; ++i) n *= T.d[1];
     TNR_REQUIRE(n <= 256, TNR_ERR_UNSUPPORTED, "transfer matrix above 256 x 256");
     const double *s1, *s2;
     btrg_weights(*this, &s1, &s2);
     Buf M(c.pool.get(), (size_t)n * n * sizeof(double)), w(c.pool.get(), (size_t)(3 * n + 1) * sizeof(double));
-    const int64_t cells = n * n;
-    k_transfer<<<(unsigned)((cells + 255) / 256), 256, 0, c.stream>>>(T.p(), T.d[0], T.d[1], T.d[2], s2, s1, nullptr,
-                                                                     1.0, M.d());
-    check_launch("transfer");
+    if (unitcell == 1) {
+        k_transfer<<<(unsigned)((n * n + 255) / 256), 256, 0, c.stream>>>(T.p(), T.d[0], T.d[1], T.d[2], s2, s1,
+                                                                          nullptr, 1.0, M.d());
+        check_launch("transfer");
+    } else {
+        DT R = ring_transfer(*this, unitcell);
+        copy_f64(c, M.d(), R.p(), n * n);
+    }
     double* wr = w.d();
     double* wi = wr + n;
     double* work = wi + n;
