@@ -7,6 +7,11 @@ Mirrors the reference's user-facing interface for the hot path:
     data = run(scheme, truncrank(16), maxiter(25))      # run! (tnrscheme.jl:33-59)
     f = free_energy(data, ising_βc)       # src/utility/free_energy.jl
 
+Schemes: TRG, BTRG, HOTRG, HOTRG_3D (the hot path), ATRG, ATRG_3D, ImpurityHOTRG,
+ImpurityTRG and CorrelationHOTRG.  Stopping criteria: maxiter, convcrit, trivial_convcrit
+and ``a & b``.  Finalizers: the default one, two_by_two_Finalizer, and the fixed-point
+functions cft_data, ground_state_degeneracy, gu_wen_ratio and central_charge.
+
 Every step runs as sm_103a CUDA inside ``libtnr_gb300.so`` behind the C ABI of
 ``include/tnr_gb300.h``; the tensor stays resident in GPU memory between calls.
 There is no CPU fallback: without the library or a GPU the calls raise.
