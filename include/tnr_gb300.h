@@ -152,6 +152,11 @@ double tnr_free_energy(const double* norms, size_t n, double beta,
 
 /* Copy the current tensor to host (column-major); dims_out gets nlegs entries. */
 int tnr_get_tensor(tnr_handle h, double* host_out, size_t cap, int64_t* dims_out, int* nlegs_out);
+/* The impurity tensors of an impurity scheme, as tnr_get_tensor copies T: ImpurityHOTRG which =
+ * 0, 1, 2 -> T_imp_order1_1, T_imp_order1_2, T_imp_order2 (impurityhotrg.jl:26-46); ImpurityTRG
+ * 0..3 -> T_imp1..T_imp4 (impuritytrg.jl:38-61); CorrelationHOTRG 0, 1, 2 -> Timp1, Timp2 (before
+ * the merge), Timp_final (from it on; correlationhotrg.jl:29-71). */
+int tnr_get_impurity_tensor(tnr_handle h, int which, double* host_out, size_t cap, int64_t* dims_out, int* nlegs_out);
 
 /* Kept singular values (TRG/BTRG) or kept eigenvalues of the chosen Gram
  * matrices (HOTRG/HOTRG_3D) of the most recent step, concatenated in the order

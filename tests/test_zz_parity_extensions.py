@@ -80,6 +80,9 @@ def test_correlation_hotrg(tnr, oracle):
         assert len(d) == 25
         got = s.correlation()
         assert got == pytest.approx(want, rel=rtol)
+        # the reference's own expression over the scheme's fields (test/schemes.jl:506)
+        tr = lambda t: abs(np.einsum('abba->', t))        # noqa: E731
+        assert tr(s.Timp_final) / tr(s.Tpure) == pytest.approx(got, rel=1e-12)
         if beta == tnr.ising_βc:
             f = tnr.free_energy([x[0] for x in d], beta, scalefactor=4.0, initial_size=4.0)
             assert f == pytest.approx(tnr.f_onsager, rel=1e-4)

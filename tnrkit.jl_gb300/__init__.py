@@ -46,7 +46,7 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes", "tnr_create_impurity_hotrg",
            "tnr_create_impurity_trg", "tnr_finalize_impurity", "tnr_run_impurity", "tnr_create_correlation_hotrg",
            "tnr_run_correlation", "tnr_correlation_ratio", "tnr_set_finalizer", "tnr_transfer_eigvals",
-           "tnr_gu_wen_ratio", "tnr_central_charge"]
+           "tnr_gu_wen_ratio", "tnr_central_charge", "tnr_get_impurity_tensor"]
 
 
 class TNRError(RuntimeError):
@@ -92,6 +92,7 @@ def lib():
         "tnr_transfer_eigvals": (I, [P, I, pd, pd, Z, pz]),
         "tnr_gu_wen_ratio": (I, [P, pd, pd]),
         "tnr_central_charge": (I, [P, C.c_double, pd]),
+        "tnr_get_impurity_tensor": (I, [P, I, pd, Z, pi64, C.POINTER(I)]),
         "tnr_run_impurity": (I, [P, I, I, I, pd, Z, pz]),
         "tnr_free_energy": (D, [pd, Z, D, D, D]),
         "tnr_get_tensor": (I, [P, pd, Z, pi64, C.POINTER(I)]),
@@ -377,6 +378,19 @@ class _ImpurityScheme(_Scheme):
         self.symmetry_n = 1
 
 
+def _impurity_tensor(scheme, which):
+    """Impurity tensor ``which`` of an impurity scheme as a host array (tnr_get_impurity_tensor)."""
+    L = lib()
+    dims = (C.c_int64 * 8)()
+    n = C.c_int()
+    _check(L.tnr_get_impurity_tensor(scheme._h, int(which), None, 0, dims, C.byref(n)), scheme._h)
+    shape = tuple(dims[i] for i in range(n.value))
+    out = np.empty(int(np.prod(shape)), dtype=np.float64)
+    _check(L.tnr_get_impurity_tensor(scheme._h, int(which), out.ctypes.data_as(C.POINTER(C.c_double)), out.size,
+                                     dims, C.byref(n)), scheme._h)
+    return out.reshape(shape, order="F")
+
+
 class ImpurityHOTRG(_ImpurityScheme):
     """``ImpurityHOTRG(T, T_imp_order1_1, T_imp_order1_2, T_imp_order2)``
     (src/schemes/impurityhotrg.jl:26-84): four tensors of the same spaces; ``run`` returns
@@ -388,6 +402,10 @@ class ImpurityHOTRG(_ImpurityScheme):
 
     def __init__(self, T, T_imp_order1_1, T_imp_order1_2, T_imp_order2, precision=PREC_F64, seed=0, stream=None):
         self._make((T, T_imp_order1_1, T_imp_order1_2, T_imp_order2), precision, seed, stream)
+
+    T_imp_order1_1 = property(lambda self: _impurity_tensor(self, 0))
+    T_imp_order1_2 = property(lambda self: _impurity_tensor(self, 1))
+    T_imp_order2 = property(lambda self: _impurity_tensor(self, 2))
 
 
 class ImpurityTRG(_ImpurityScheme):
@@ -401,6 +419,11 @@ class ImpurityTRG(_ImpurityScheme):
 
     def __init__(self, T, T_imp1, T_imp2, T_imp3, T_imp4, precision=PREC_F64, seed=0, stream=None):
         self._make((T, T_imp1, T_imp2, T_imp3, T_imp4), precision, seed, stream)
+
+    T_imp1 = property(lambda self: _impurity_tensor(self, 0))
+    T_imp2 = property(lambda self: _impurity_tensor(self, 1))
+    T_imp3 = property(lambda self: _impurity_tensor(self, 2))
+    T_imp4 = property(lambda self: _impurity_tensor(self, 3))
 
 
 class CorrelationHOTRG(_ImpurityScheme):
@@ -418,6 +441,11 @@ class CorrelationHOTRG(_ImpurityScheme):
             raise ValueError("Distance must be non-negative")
         self.dist = int(dist)
         self._make((Tpure, Timp1, Timp2), precision, seed, stream, self.dist)
+
+    Tpure = property(lambda self: self.T)
+    Timp1 = property(lambda self: _impurity_tensor(self, 0))
+    Timp2 = property(lambda self: _impurity_tensor(self, 1))
+    Timp_final = property(lambda self: _impurity_tensor(self, 2))
 
     def correlation(self):
         out = C.c_double()

@@ -349,6 +349,27 @@ int tnr_get_tensor(tnr_handle h, double* host_out, size_t cap, int64_t* dims_out
     });
 }
 
+int tnr_get_impurity_tensor(tnr_handle h, int which, double* host_out, size_t cap, int64_t* dims_out, int* nlegs_out) {
+    if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
+    return guarded(h, [&] {
+        Scheme& s = h->s;
+        const DT* t = nullptr;
+        if (s.kind == TNR_IMPURITY_HOTRG && which >= 0 && which < 3) t = which == 0 ? &s.I11 : which == 1 ? &s.I12 : &s.I2;
+        if (s.kind == TNR_IMPURITY_TRG && which >= 0 && which < 4) t = &s.site[which];
+        if (s.kind == TNR_CORRELATION_HOTRG && which >= 0 && which < 3) t = which == 0 ? &s.C1 : which == 1 ? &s.C2 : &s.Cf;
+        TNR_REQUIRE(t != nullptr, TNR_ERR_INVALID_ARG, "no impurity tensor with that index in this scheme");
+        TNR_REQUIRE(t->rank > 0, TNR_ERR_INVALID_ARG, "that impurity tensor is not present at this step");
+        if (nlegs_out) *nlegs_out = t->rank;
+        if (dims_out)
+            for (int i = 0; i < t->rank; ++i) dims_out[i] = t->d[i];
+        if (host_out) {
+            TNR_REQUIRE(cap >= (size_t)t->size(), TNR_ERR_INVALID_ARG, "host_out too small");
+            TNR_CUDA(cudaMemcpyAsync(host_out, t->p(), t->size() * sizeof(double), cudaMemcpyDeviceToHost, s.ctx->stream));
+            s.ctx->sync();
+        }
+    });
+}
+
 int tnr_singular_values(tnr_handle h, double* out, size_t cap, size_t* n_out, int32_t* counts, size_t counts_cap,
                         size_t* ndec_out) {
     if (!h) return fail(nullptr, TNR_ERR_INVALID_ARG, "NULL handle");
