@@ -104,16 +104,16 @@ mutable struct GPU{S} <: TNRScheme{Float64, Any}
             if kind == TNR_IMPURITY_HOTRG
                 st = ccall((:tnr_create_impurity_hotrg, libtnr), Cint,
                     (Ptr{Ptr{Cvoid}}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{Options}),
-                    h, dims, arr, imps..., opts)
+                    h, dims, arr, imps[1], imps[2], imps[3], opts)
             elseif kind == TNR_IMPURITY_TRG
                 st = ccall((:tnr_create_impurity_trg, libtnr), Cint,
                     (Ptr{Ptr{Cvoid}}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
                      Ptr{Float64}, Ref{Options}),
-                    h, dims, arr, imps..., opts)
+                    h, dims, arr, imps[1], imps[2], imps[3], imps[4], opts)
             else
                 st = ccall((:tnr_create_correlation_hotrg, libtnr), Cint,
                     (Ptr{Ptr{Cvoid}}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Cint, Ref{Options}),
-                    h, dims, arr, imps..., scheme.dist, opts)
+                    h, dims, arr, imps[1], imps[2], scheme.dist, opts)
             end
         end
         check(st)
