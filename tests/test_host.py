@@ -281,3 +281,27 @@ def test_stopping_criteria(tnr, oracle):
     assert tnr.ATRG_3D_convcrit(3, [2.0]) == pytest.approx(abs(np.log(2.0)) / 64.0)
     with pytest.raises(TypeError):
         tnr.run(None, tnr.truncrank(4), 5)
+
+
+def test_new_entry_points_refuse_null_handles(tnr):
+    """Every entry point added for the schemes around the hot path returns TNR_ERR_INVALID_ARG
+    on a NULL handle or NULL outputs instead of crashing (no device needed)."""
+    L = tnr.lib()
+    bad = header_defines()["TNR_ERR_INVALID_ARG"]
+    d = ctypes.c_double()
+    n = ctypes.c_size_t()
+    buf = (ctypes.c_double * 8)()
+    dims = (ctypes.c_int64 * 8)()
+    nl = ctypes.c_int()
+    assert L.tnr_set_finalizer(None, 1) == bad
+    assert L.tnr_transfer_eigvals(None, 1, buf, buf, 8, ctypes.byref(n)) == bad
+    assert L.tnr_gu_wen_ratio(None, ctypes.byref(d), ctypes.byref(d)) == bad
+    assert L.tnr_central_charge(None, 1.0, ctypes.byref(d)) == bad
+    assert L.tnr_run_correlation(None, 8, 4, buf, 8, ctypes.byref(n)) == bad
+    assert L.tnr_correlation_ratio(None, ctypes.byref(d)) == bad
+    assert L.tnr_get_impurity_tensor(None, 0, buf, 8, dims, ctypes.byref(nl)) == bad
+    assert L.tnr_finalize_impurity(None, buf) == bad
+    assert L.tnr_run_impurity(None, 8, 4, 1, buf, 8, ctypes.byref(n)) == bad
+    h = ctypes.c_void_p()
+    assert L.tnr_create(ctypes.byref(h), 10, 4, dims, buf, None) == bad       # unknown kind
+    assert L.tnr_create(ctypes.byref(h), header_defines()["TNR_ATRG_3D"], 4, dims, buf, None) == bad   # 6 legs
