@@ -214,10 +214,10 @@ def test_convcrit_run(tnr, oracle):
 
 def test_cft_data_unitcell2(tnr, oracle):
     """cft_data and ground_state_degeneracy with unitcell = 2 (src/utility/cft.jl:7-15: two
-    tensors on the ring, a 256 x 256 transfer matrix at truncrank(16)) against the oracle."""
+    tensors on the ring, a 144 x 144 transfer matrix at truncrank(12)) against the oracle."""
     o = oracle
     s, so = tnr.TRG(tnr.classical_ising()), o.TRG(o.classical_ising())
-    tnr.run(s, tnr.truncrank(16), tnr.maxiter(8))
-    o.run(so, o.truncrank(16), o.maxiter(8))
+    tnr.run(s, tnr.truncrank(12), tnr.maxiter(8))
+    o.run(so, o.truncrank(12), o.maxiter(8))
     np.testing.assert_allclose(tnr.cft_data(s, unitcell=2)[:8], o.cft_data(so, unitcell=2)[:8], rtol=0, atol=1e-9)
     assert tnr.ground_state_degeneracy(s, 2) == pytest.approx(o.ground_state_degeneracy(so, 2), rel=1e-9)
