@@ -305,3 +305,24 @@ def test_new_entry_points_refuse_null_handles(tnr):
     h = ctypes.c_void_p()
     assert L.tnr_create(ctypes.byref(h), 10, 4, dims, buf, None) == bad       # unknown kind
     assert L.tnr_create(ctypes.byref(h), header_defines()["TNR_ATRG_3D"], 4, dims, buf, None) == bad   # 6 legs
+
+
+def test_impurity_constructors_check_arguments(tnr):
+    """The impurity constructors refuse mismatched tensors in the host layer and NULL tensors
+    or non-square legs in the C ABI, before any device work."""
+    T = tnr.classical_ising("Trivial")
+    with pytest.raises(ValueError):
+        tnr.ImpurityTRG(T, np.ones((2, 2, 2, 3)), T, T, T)
+    with pytest.raises(ValueError):
+        tnr.ImpurityHOTRG(T, T, np.ones((2, 2, 2)), T)
+    L = tnr.lib()
+    bad = header_defines()["TNR_ERR_INVALID_ARG"]
+    a = np.asfortranarray(T.array)
+    p = a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    dims = (ctypes.c_int64 * 4)(*a.shape)
+    h = ctypes.c_void_p()
+    assert L.tnr_create_impurity_trg(ctypes.byref(h), dims, p, p, p, None, p, None) == bad
+    assert L.tnr_create_impurity_hotrg(ctypes.byref(h), dims, p, None, p, p, None) == bad
+    ragged = (ctypes.c_int64 * 4)(2, 2, 3, 2)
+    assert L.tnr_create_impurity_trg(ctypes.byref(h), ragged, p, p, p, p, p, None) == bad
+    assert not h.value
