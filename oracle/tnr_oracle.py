@@ -46,7 +46,7 @@ EPS = np.finfo(np.float64).eps
 
 
 def potts_beta_c(q):
-    """src/models/potts.jl:204"""
+    """src/models/potts.jl:39"""
     return math.log(1.0 + math.sqrt(q))
 
 
@@ -301,7 +301,7 @@ def classical_ising_3D(beta=ISING_BETA_C_3D, symmetry="Z2", J=1.0):
 
 
 def _fourier_real_zn(A, q, conj_first_two=True):
-    """(P'(x)P') A (P(x)P) with P[k,c] = w^{kc}/sqrt(q); real part (potts.jl:236-246, clock.jl:322-339)."""
+    """(P'(x)P') A (P(x)P) with P[k,c] = w^{kc}/sqrt(q); real part (potts.jl:71-81, clock.jl:32-49)."""
     w = np.exp(2j * np.pi / q)
     P = np.array([[w ** (k * c) for c in range(q)] for k in range(q)]) / math.sqrt(q)
     U = np.einsum('ijkl,ia,jb,kc,ld->abcd', A.astype(complex), P.conj(), P.conj(), P, P)
@@ -309,7 +309,7 @@ def _fourier_real_zn(A, q, conj_first_two=True):
 
 
 def classical_potts(q=3, beta=None, symmetry="ZN"):
-    """src/models/potts.jl:187-195,228-246."""
+    """src/models/potts.jl:22-30,68-81."""
     if beta is None:
         beta = potts_beta_c(q)
     A = np.zeros((q, q, q, q))
@@ -324,7 +324,7 @@ def classical_potts(q=3, beta=None, symmetry="ZN"):
 
 
 def classical_clock(q=6, beta=1.0, symmetry="ZN"):
-    """src/models/clock.jl:1-12,316-339 (Trivial and Z_q branches)."""
+    """src/models/clock.jl:1-12,29-49 (Trivial and Z_q branches)."""
     A = np.zeros((q, q, q, q))
 
     def clock(i, j):

@@ -20,7 +20,7 @@ ising_βc_3D = ising_beta_c_3D = 1.0 / 4.51152469                               
 
 
 def potts_βc(q):
-    """potts.jl:204"""
+    """potts.jl:39"""
     return math.log(1.0 + math.sqrt(q))
 
 
@@ -102,7 +102,7 @@ def _zn_fourier(A, q):
 
 
 def classical_potts(q=3, beta=None, symmetry="ZN"):
-    """``classical_potts(S, q, β)`` (potts.jl:187-195,228-246)."""
+    """``classical_potts(S, q, β)`` (potts.jl:22-30,68-81)."""
     beta = potts_βc(q) if beta is None else beta
     i = np.arange(q)
     d = (i[:, None] == i[None, :]).astype(float)
@@ -114,7 +114,7 @@ def classical_potts(q=3, beta=None, symmetry="ZN"):
 
 
 def classical_clock(q=6, beta=1.0, symmetry="ZN"):
-    """``classical_clock(S, q, β)`` (clock.jl:1-12,316-339), Trivial and Z_q."""
+    """``classical_clock(S, q, β)`` (clock.jl:1-12,29-49), Trivial and Z_q."""
     i = np.arange(q)
     cl = -np.cos(2 * np.pi / q * (i[:, None] - i[None, :]))
     E = cl[:, :, None, None] + cl[None, :, None, :] + cl.T[None, None, :, :] + cl.T[:, None, :, None]
