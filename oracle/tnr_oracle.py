@@ -339,6 +339,63 @@ def classical_clock(q=6, beta=1.0, symmetry="ZN"):
     return _project_symmetric(t)
 
 
+def sixvertex(a=1.0, b=1.0, c=1.0):
+    """src/models/sixvertex.jl:29-37 (Trivial): the 4 x 4 vertex weights (a on the two
+    all-equal configurations, c and b on the two mixed ones) as T[i1, i2; i3, i4]."""
+    W = np.array([[a, 0, 0, 0], [0, c, b, 0], [0, b, c, 0], [0, 0, 0, a]], dtype=np.float64)
+    return Tensor(W.reshape(2, 2, 2, 2, order='F'), 2, None, 1)
+
+
+def _phi4_real_site(K, mu0, lam, h, power):
+    """src/models/phi4_real.jl:5-23,88-111,186-209,241-264 (Trivial): Gauss-Hermite nodes y_p and
+    weights w_p, the link matrix F[i, j] = exp(-(y_i - y_j)^2/2 - mu0 (y_i^2 + y_j^2)/8
+    - lam (y_i^4 + y_j^4)/16 + h (y_i + y_j)/4) = U S V, and
+    T[i,j,k,l] = sum_p sqrt(S_i S_j S_k S_l) y_p^power w_p exp(y_p^2) U[p,i] U[p,j] V[k,p] V[l,p]."""
+    y, w = np.polynomial.hermite.hermgauss(K)
+    Y1, Y2 = np.meshgrid(y, y, indexing='ij')
+    F = np.exp(-0.5 * (Y1 - Y2) ** 2 - mu0 / 8 * (Y1 ** 2 + Y2 ** 2) - lam / 16 * (Y1 ** 4 + Y2 ** 4) + h / 4 * (Y1 + Y2))
+    U, S, Vh = np.linalg.svd(F)
+    r = np.sqrt(S)
+    site = w * np.exp(y ** 2) * y ** power
+    Uw, Vw = U * r, (r[:, None] * Vh)
+    return np.einsum('p,pi,pj,kp,lp->ijkl', site, Uw, Uw, Vw, Vw)
+
+
+def phi4_real(K, mu0, lam, h=0.0, symmetry="Z2"):
+    """src/models/phi4_real.jl:85-154: the real phi^4 site tensor, Trivial (Gauss-Hermite, bond
+    dimension K) or Z2 (Taylor expansion of the link term to order K-1: t[s1..s4] =
+    M_{s1+s2+s3+s4} / sqrt(s1! s2! s3! s4!) for an even order sum, M_n = int exp(-a phi^2 - b phi^4)
+    phi^n, a = (4 + mu0)/2, b = lam/4; even orders first, then odd, as the two charge sectors)."""
+    if symmetry == "Trivial":
+        return Tensor(_phi4_real_site(K, mu0, lam, h, 0), 2, None, 1)
+    assert h == 0.0 and K % 2 == 0
+    from scipy.integrate import quad
+    a, b = (4 + mu0) / 2, lam / 4
+    M = np.zeros(4 * (K - 1) + 1)
+    for n in range(0, 4 * (K - 1) + 1, 2):
+        M[n] = quad(lambda x, n=n: math.exp(-a * x * x - b * x ** 4) * x ** n, -np.inf, np.inf)[0]
+    lf = np.array([math.lgamma(s + 1) for s in range(K)])
+    t = np.zeros((K, K, K, K))
+    for s1, s2, s3, s4 in np.ndindex(K, K, K, K):
+        n = s1 + s2 + s3 + s4
+        if n % 2 == 0:
+            t[s1, s2, s3, s4] = M[n] / math.exp((lf[s1] + lf[s2] + lf[s3] + lf[s4]) / 2)
+    perm = list(range(0, K, 2)) + list(range(1, K, 2))
+    t = t[np.ix_(perm, perm, perm, perm)]
+    qv = np.array([0] * (K // 2) + [1] * (K // 2), dtype=np.int64)
+    return Tensor(t, 2, [qv.copy(), qv.copy(), (-qv) % 2, (-qv) % 2], 2)
+
+
+def phi4_real_imp1(K, mu0, lam, h=0.0):
+    """src/models/phi4_real.jl:186-209: the site tensor with a phi insertion (Trivial)."""
+    return Tensor(_phi4_real_site(K, mu0, lam, h, 1), 2, None, 1)
+
+
+def phi4_real_imp2(K, mu0, lam, h=0.0):
+    """src/models/phi4_real.jl:241-264: the site tensor with a phi^2 insertion (Trivial)."""
+    return Tensor(_phi4_real_site(K, mu0, lam, h, 2), 2, None, 1)
+
+
 def _project_symmetric(t: Tensor):
     """Zero the entries that break charge conservation (TensorKit keeps only symmetric blocks)."""
     if t.q is None:

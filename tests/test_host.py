@@ -71,7 +71,8 @@ def test_no_device_is_an_error_not_a_crash(tnr):
     assert e.value.status in (8, 4)
 
 
-@pytest.mark.parametrize("name", ["ising", "ising_triv", "ising_impurity", "potts3", "clock6", "clock3", "ising3d"])
+@pytest.mark.parametrize("name", ["ising", "ising_triv", "ising_impurity", "potts3", "clock6", "clock3", "ising3d",
+                                  "sixvertex", "phi4_triv", "phi4_z2", "phi4_imp1", "phi4_imp2"])
 def test_models_match_oracle(tnr, oracle, name):
     o = oracle
     if name == "ising":
@@ -86,9 +87,19 @@ def test_models_match_oracle(tnr, oracle, name):
         a, b = tnr.classical_clock(6, 0.9), o.classical_clock(6, 0.9)
     elif name == "clock3":
         a, b = tnr.classical_clock(3, 0.9, "Trivial"), o.classical_clock(3, 0.9, "Trivial")
+    elif name == "sixvertex":
+        a, b = tnr.sixvertex("Trivial", 1.0, 2.0, 3.0), o.sixvertex(1.0, 2.0, 3.0)
+    elif name == "phi4_triv":
+        a, b = tnr.phi4_real(8, -1.0, 1.0, 0.1, symmetry="Trivial"), o.phi4_real(8, -1.0, 1.0, 0.1, symmetry="Trivial")
+    elif name == "phi4_z2":
+        a, b = tnr.phi4_real(8, -1.0, 1.0), o.phi4_real(8, -1.0, 1.0)
+    elif name == "phi4_imp1":
+        a, b = tnr.phi4_real_imp1(8, -2.0, 1.0), o.phi4_real_imp1(8, -2.0, 1.0)
+    elif name == "phi4_imp2":
+        a, b = tnr.phi4_real_imp2(8, -2.0, 1.0), o.phi4_real_imp2(8, -2.0, 1.0)
     else:
         a, b = tnr.classical_ising_3D(), o.classical_ising_3D()
-    np.testing.assert_allclose(a.array, b.a, rtol=1e-13, atol=1e-14)
+    np.testing.assert_allclose(a.array, b.a, rtol=1e-13, atol=1e-14 * max(1.0, np.abs(b.a).max()))
     if b.q is not None:
         for qa, qb, l in zip(a.charges, b.q, range(b.a.ndim)):
             # the package stores plain charges; the oracle stores signed ones (domain legs negated)

@@ -426,3 +426,39 @@ def test_atrg3d_projectors_ignore_the_orthogonal_factor(oracle, monkeypatch):
     monkeypatch.setattr(o, "_right_orth_l", lambda M: (lambda L: L @ orth(L.shape[1]))(right(M)))
     got = np.array(o.run(o.ATRG_3D(o.classical_ising_3D()), o.truncrank(6), o.maxiter(4)))
     np.testing.assert_allclose(got, ref, rtol=1e-11)
+
+
+@pytest.mark.parametrize("model,temp,answer,rtol", [
+    ("sixvertex", 1.0, 1.5 * math.log(0.75), 1e-3),
+    ("phi4_trivial", -1.0, 0.4241912271276211, 1e-12),
+    ("phi4_z2", -1.0, 0.4232381701937374, 1e-10),
+])
+def test_models_trg16_sixvertex_phi4(oracle, model, temp, answer, rtol):
+    """test/models.jl:17-23,37-41: TRG, truncrank(16), maxiter(25) on the six-vertex model (Trivial;
+    the reference's bar is rtol 1e-3 against 3/2 log(3/4)) and the real phi^4 model K = 10, mu0 = -1,
+    lam = 1 (Trivial and Z2).  The phi^4 answers are the reference's printed results to 16 digits;
+    the oracle reproduces them to 6e-16 (Trivial) and 4e-13 (Z2), so they are held far tighter
+    than the reference's 1e-3."""
+    o = oracle
+    T = {"sixvertex": lambda: o.sixvertex(), "phi4_trivial": lambda: o.phi4_real(10, -1.0, 1.0, symmetry="Trivial"),
+         "phi4_z2": lambda: o.phi4_real(10, -1.0, 1.0)}[model]()
+    data = o.run(o.TRG(T), o.truncrank(16), o.maxiter(25))
+    assert o.free_energy(data, temp) == pytest.approx(answer, rel=rtol)
+
+
+def test_impurity_hotrg_phi4_order_parameter(oracle):
+    """test/models.jl:89-121: ImpurityHOTRG(Tpure, T_imp1, T_imp1, T_imp2) of the real phi^4
+    model (Trivial, K = 10, lam = 1), truncrank(16), maxiter(25): <phi^2>-like ratio
+    data[end][4] / data[end][1] is 0 in the disordered phase (mu0 = 0, atol 1e-3) and
+    1.5317112652447245 in the ordered one (mu0 = -2); the oracle reproduces the latter to 7e-15,
+    held here at 1e-12."""
+    o = oracle
+    for mu0, want in [(0.0, 0.0), (-2.0, 1.5317112652447245)]:
+        args = (10, mu0, 1.0)
+        Tp, i1, i2 = o.phi4_real(*args, symmetry="Trivial"), o.phi4_real_imp1(*args), o.phi4_real_imp2(*args)
+        data = o.run(o.ImpurityHOTRG(Tp, i1, i1, i2), o.truncrank(16), o.maxiter(25))
+        got = data[-1][3] / data[-1][0]
+        if want == 0.0:
+            assert abs(got) <= 1e-3
+        else:
+            assert got == pytest.approx(want, rel=1e-12)

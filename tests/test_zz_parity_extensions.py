@@ -221,3 +221,23 @@ def test_cft_data_unitcell2(tnr, oracle):
     o.run(so, o.truncrank(12), o.maxiter(8))
     np.testing.assert_allclose(tnr.cft_data(s, unitcell=2)[:8], o.cft_data(so, unitcell=2)[:8], rtol=0, atol=1e-9)
     assert tnr.ground_state_degeneracy(s, 2) == pytest.approx(o.ground_state_degeneracy(so, 2), rel=1e-9)
+
+
+def test_phi4_and_sixvertex_models(tnr, oracle):
+    """Models of test/models.jl:17-23,89-121 through the tested TRG and ImpurityHOTRG paths.
+    Their late-step norms sit near ties at the cut (the oracle's own move by 3e-7 to 2e-2 under a
+    1e-14 perturbation), while f and the order parameter move by < 1e-13: those are held.  TRG,
+    truncrank(16), maxiter(25): the real phi^4 f (Trivial, K = 10, mu0 = -1) against the reference's
+    printed 0.4241912271276211 to 1e-10, the six-vertex f against the oracle's to 1e-10; the phi^4
+    ImpurityHOTRG order parameter at mu0 = -2 against the reference's 1.5317112652447245 to 1e-10."""
+    o = oracle
+    d = tnr.run(tnr.TRG(tnr.phi4_real(10, -1.0, 1.0, symmetry="Trivial")), tnr.truncrank(16), tnr.maxiter(25))
+    assert tnr.free_energy(d, -1.0) == pytest.approx(0.4241912271276211, rel=1e-10)
+    d = tnr.run(tnr.TRG(tnr.sixvertex()), tnr.truncrank(16), tnr.maxiter(25))
+    do = o.run(o.TRG(o.sixvertex()), o.truncrank(16), o.maxiter(25))
+    assert tnr.free_energy(d, 1.0) == pytest.approx(o.free_energy(do, 1.0), rel=1e-10)
+    args = (10, -2.0, 1.0)
+    s = tnr.ImpurityHOTRG(tnr.phi4_real(*args, symmetry="Trivial"), tnr.phi4_real_imp1(*args), tnr.phi4_real_imp1(*args),
+                          tnr.phi4_real_imp2(*args))
+    d = tnr.run(s, tnr.truncrank(16), tnr.maxiter(25))
+    assert d[-1][3] / d[-1][0] == pytest.approx(1.5317112652447245, rel=1e-10)

@@ -124,6 +124,66 @@ def classical_clock(q=6, beta=1.0, symmetry="ZN"):
     return SymTensor(_zn_fourier(A, q), _charges(q, 4, q), q)
 
 
+def sixvertex(symmetry="Trivial", a=1.0, b=1.0, c=1.0):
+    """``sixvertex(Trivial; a, b, c)`` (sixvertex.jl:29-37): the vertex weights as T[i1, i2; i3, i4],
+    a on the two all-equal configurations, c and b on the mixed ones.  The U(1)/CU(1) forms
+    carry non-abelian or continuous sectors and are not built here."""
+    if symmetry != "Trivial":
+        raise ValueError("sixvertex: only the Trivial form runs on this engine")
+    W = np.array([[a, 0, 0, 0], [0, c, b, 0], [0, b, c, 0], [0, 0, 0, a]], dtype=np.float64)
+    return SymTensor(np.ascontiguousarray(W.reshape(2, 2, 2, 2, order="F")), None, 1)
+
+
+def _phi4_gauss_hermite(K, mu0, lam, h, power):
+    """Gauss-Hermite form of the real phi^4 site (phi4_real.jl:5-23,88-111): link matrix F = U S V
+    on the quadrature nodes, T = sum_p sqrt(S)^4 y_p^power w_p e^{y_p^2} U U V V."""
+    y, w = np.polynomial.hermite.hermgauss(K)
+    yi, yj = y[:, None], y[None, :]
+    F = np.exp(-0.5 * (yi - yj) ** 2 - mu0 / 8.0 * (yi ** 2 + yj ** 2) - lam / 16.0 * (yi ** 4 + yj ** 4) + h / 4.0 * (yi + yj))
+    U, S, V = np.linalg.svd(F)
+    left = U * np.sqrt(S)                      # [p, i]
+    right = np.sqrt(S)[:, None] * V            # [k, p]
+    weight = w * np.exp(y ** 2) * y ** power
+    return np.ascontiguousarray(np.einsum("p,pi,pj,kp,lp->ijkl", weight, left, left, right, right))
+
+
+def phi4_real(K, mu0, lam, h=0.0, symmetry="Z2"):
+    """``phi4_real([S,] K, μ0, λ[, h])`` (phi4_real.jl:85-154).  Trivial: Gauss-Hermite quadrature
+    with K nodes (bond dimension K).  Z2: the link term Taylor-expanded to order K-1, entries
+    M_n / sqrt(s1! s2! s3! s4!) for even n = s1+s2+s3+s4 with M_n = ∫ exp(-(4+μ0)/2 φ² - λ/4 φ⁴) φⁿ dφ,
+    even orders then odd orders as the two sectors (no field)."""
+    if symmetry == "Trivial":
+        return SymTensor(_phi4_gauss_hermite(K, mu0, lam, h, 0), None, 1)
+    if symmetry != "Z2":
+        raise ValueError("symmetry must be 'Trivial' or 'Z2'")
+    if h != 0.0 or K % 2:
+        raise ValueError("the Z2 form needs h = 0 and an even K")
+    from scipy.integrate import quad
+    a, b = (4.0 + mu0) / 2.0, lam / 4.0
+    moments = {n: quad(lambda x, n=n: math.exp(-a * x * x - b * x ** 4) * x ** n, -math.inf, math.inf)[0]
+               for n in range(0, 4 * (K - 1) + 1, 2)}
+    half_log_fact = np.array([math.lgamma(k + 1) / 2.0 for k in range(K)])
+    order = np.arange(K)
+    n_tot = order[:, None, None, None] + order[None, :, None, None] + order[None, None, :, None] + order[None, None, None, :]
+    scale = np.exp(-(half_log_fact[:, None, None, None] + half_log_fact[None, :, None, None]
+                     + half_log_fact[None, None, :, None] + half_log_fact[None, None, None, :]))
+    t = np.where(n_tot % 2 == 0, np.vectorize(lambda n: moments.get(int(n), 0.0))(n_tot), 0.0) * scale
+    perm = np.r_[0:K:2, 1:K:2]                 # even orders (charge 0), then odd (charge 1)
+    t = t[np.ix_(perm, perm, perm, perm)]
+    q = np.r_[np.zeros(K // 2, dtype=np.int32), np.ones(K // 2, dtype=np.int32)]
+    return SymTensor(np.ascontiguousarray(t), [q.copy() for _ in range(4)], 2)
+
+
+def phi4_real_imp1(K, mu0, lam, h=0.0):
+    """``phi4_real_imp1(Trivial, K, μ0, λ[, h])`` (phi4_real.jl:186-209): a φ insertion on the site."""
+    return SymTensor(_phi4_gauss_hermite(K, mu0, lam, h, 1), None, 1)
+
+
+def phi4_real_imp2(K, mu0, lam, h=0.0):
+    """``phi4_real_imp2(Trivial, K, μ0, λ[, h])`` (phi4_real.jl:241-264): a φ² insertion on the site."""
+    return SymTensor(_phi4_gauss_hermite(K, mu0, lam, h, 2), None, 1)
+
+
 def random_hotrg_tensor(chi, seed, decay=6.0):
     """Seeded dense 4-leg tensor for the single-step HOTRG workload: N(0,1) entries times
     exp(-k/decay) per leg index k, normalised to Frobenius norm 1 (numpy PCG64)."""
