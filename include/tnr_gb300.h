@@ -179,7 +179,8 @@ int  tnr_destroy(tnr_handle h);
 int  tnr_last_error(tnr_handle h, char* buf, size_t cap); /* h may be NULL: global */
 const char* tnr_status_string(int status);
 
-/* Device-time measurement on the handle's stream (CUDA events). */
+/* Device-time measurement on the handle's stream (CUDA events).  No reference counterpart
+ * (the reference times run!() with @elapsed on the host, tnrscheme.jl:44). */
 int tnr_timer_start(tnr_handle h);
 int tnr_timer_stop(tnr_handle h, double* ms_out);
 
@@ -218,9 +219,12 @@ int tnr_server_poll(tnr_server s, uint64_t id, int wait, int* done, double* norm
                     size_t* n_out, double* latency_ms, double* queue_ms);
 int tnr_server_stats(tnr_server s, int* active, int* queued, size_t* bytes_in_use);
 int tnr_server_destroy(tnr_server s);
+/* Device bytes a run!() of this kind, chi and initial legs needs (the admission estimate). */
 size_t tnr_footprint_bytes(int kind, int chi, int nlegs, const int64_t* dims);
 
 /* ---- profiling: CUDA events around every launch of a kernel class -------- */
+/* No reference counterpart: per-class launch counts, device time and algorithmic work
+ * for the roofline of the benchmark. */
 #define TNR_PROF_GEMM_BULK 0  /* bulk contraction / projection GEMMs run in FP64; work = flops */
 #define TNR_PROF_GEMM_F64  1  /* FP64 GEMMs inside the decompositions; work = flops */
 #define TNR_PROF_JACOBI    2  /* Jacobi eigensolver; work = r^3                     */
@@ -275,7 +279,7 @@ int tnr_gemm_split_noalloc(int ta, int tb, int64_t m, int64_t n, int64_t k, doub
                            double beta, double* C, int64_t ldc, void* stream,
                            char* err, size_t err_cap);
 
-/* ---- library info ------------------------------------------------------- */
+/* ---- library info (no reference counterpart) ----------------------------- */
 int tnr_device_info(int* sm_count, int* cc_major, int* cc_minor, size_t* hbm_bytes);
 const char* tnr_version(void);
 
