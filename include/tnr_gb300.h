@@ -180,7 +180,7 @@ int  tnr_last_error(tnr_handle h, char* buf, size_t cap); /* h may be NULL: glob
 const char* tnr_status_string(int status);
 
 /* Device-time measurement on the handle's stream (CUDA events).  No reference counterpart
- * (the reference times run!() with @elapsed on the host, tnrscheme.jl:44). */
+ * (the reference times run!() with @elapsed on the host, tnrscheme.jl:46). */
 int tnr_timer_start(tnr_handle h);
 int tnr_timer_stop(tnr_handle h, double* ms_out);
 
