@@ -556,7 +556,7 @@ def run(scheme, trunc, crit, finalizer=None, finalize_beginning=True, verbosity=
     Returns the list of norms (n + 1 with ``finalize_beginning``).  With maxiter(n) the whole
     loop runs in the library and the norms come back once; any other criterion (convcrit,
     MultipleCrit) is evaluated on the host after every step, as run! does
-    (src/schemes/tnrscheme.jl:44-55), from the norm that step's finalize! returns."""
+    (src/schemes/tnrscheme.jl:39-52), from the norm that step's finalize! returns."""
     if not isinstance(crit, stopcrit):
         raise TypeError("crit must be a stopping criterion (maxiter, convcrit, a & b)")
     if finalizer is not None:

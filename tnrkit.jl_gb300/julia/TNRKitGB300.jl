@@ -167,7 +167,7 @@ function run!(g::GPU, trunc, crit::maxiter; finalize_beginning = true, verbosity
     return np == 1 ? out[1:n[]] : [Tuple(out[np * (i - 1) + 1:np * i]) for i in 1:n[]]
 end
 
-# run! with any other stopping criterion (convcrit, a & b): the loop of tnrscheme.jl:44-55 on
+# run! with any other stopping criterion (convcrit, a & b): the loop of tnrscheme.jl:39-52 on
 # the host, each step and finalize! on the device
 function run!(g::GPU, trunc, crit; finalize_beginning = true, verbosity = 1)
     g.kind == TNR_CORRELATION_HOTRG && throw(ArgumentError("CorrelationHOTRG's run! takes maxiter(n)"))
