@@ -410,7 +410,7 @@ def test_atrg3d_ising(oracle):
 
 
 def test_atrg3d_projectors_ignore_the_orthogonal_factor(oracle, monkeypatch):
-    """ATRG_3D's oblique projectors (src/schemes/atrg3d.jl:54-68) use the R / L factors of
+    """ATRG_3D's oblique projectors (src/schemes/atrg3d.jl:54-69) use the R / L factors of
     left_orth / right_orth only through R1 R2 and its SVD, so R -> O R and L -> L O' with any
     orthogonal O, O' leave every norm unchanged: the engine's R = Q^T M from CholeskyQR3 is as
     good as LAPACK's."""

@@ -154,7 +154,7 @@ static Buf qr_r(Ctx& c, const double* Mat, int64_t m, int64_t n) {
     return R;
 }
 
-// the oblique projector pair of atrg3d.jl:60-68 from Rl (left_orth R, r x n) and Rrt (the
+// the oblique projector pair of atrg3d.jl:59-69 from Rl (left_orth R, r x n) and Rrt (the
 // transpose of right_orth's L, r' x n): temp = Rl Rrt^T = U s V^T truncated to chi,
 // Pa[pq; k] = Rrt^T V s^-1/2 (n x k), Pb[k; pq] = s^-1/2 U^T Rl (k x n), pseudopow for s^-1/2
 static void oblique_projectors(Scheme& s, const Buf& Rl, const Buf& Rrt, int64_t n, int chi, Buf& Pa, Buf& Pb, int& k) {
