@@ -386,6 +386,25 @@ def phi4_real(K, mu0, lam, h=0.0, symmetry="Z2"):
     return Tensor(t, 2, [qv.copy(), qv.copy(), (-qv) % 2, (-qv) % 2], 2)
 
 
+def phi4_complex(K, mu0, lam):
+    """src/models/phi4_complex.jl:6-36,108-138,194-206 (Trivial, real entries): Gauss-Hermite
+    nodes for the real and imaginary parts, link matrix F[(a,b),(c,d)] = exp(-((y_a - y_c)^2
+    + (y_b - y_d)^2)/2 - mu0 (|phi_1|^2 + |phi_2|^2)/8 - lam (|phi_1|^4 + |phi_2|^4)/16) = U S V on the
+    K^2 pairs (pair index a K + b), site weights w_a w_b exp(y_a^2 + y_b^2), and
+    T[i,j,k,l] = sum_p sqrt(S_i S_j S_k S_l) W_p U[p,i] U[p,j] V[k,p] V[l,p] (bond dimension K^2).
+    F is symmetric positive definite, so U = V^T and T is fully symmetric, as the reference's
+    sorted-index fill assumes."""
+    y, w = np.polynomial.hermite.hermgauss(K)
+    R1, I1, R2, I2 = np.meshgrid(y, y, y, y, indexing='ij')
+    F = np.exp(-0.5 * ((R1 - R2) ** 2 + (I1 - I2) ** 2) - mu0 / 8 * (R1 ** 2 + I1 ** 2 + R2 ** 2 + I2 ** 2)
+               - lam / 16 * ((R1 ** 2 + I1 ** 2) ** 2 + (R2 ** 2 + I2 ** 2) ** 2)).reshape(K * K, K * K)
+    U, S, Vh = np.linalg.svd(F)
+    Wt = (w[:, None] * w[None, :] * np.exp(y[:, None] ** 2 + y[None, :] ** 2)).reshape(-1)
+    r = np.sqrt(S)
+    Ul, Vr = U * r, r[:, None] * Vh
+    return Tensor(np.einsum('p,pi,pj,kp,lp->ijkl', Wt, Ul, Ul, Vr, Vr, optimize=True), 2, None, 1)
+
+
 def phi4_real_imp1(K, mu0, lam, h=0.0):
     """src/models/phi4_real.jl:186-209: the site tensor with a phi insertion (Trivial)."""
     return Tensor(_phi4_real_site(K, mu0, lam, h, 1), 2, None, 1)

@@ -72,7 +72,7 @@ def test_no_device_is_an_error_not_a_crash(tnr):
 
 
 @pytest.mark.parametrize("name", ["ising", "ising_triv", "ising_impurity", "potts3", "clock6", "clock3", "ising3d",
-                                  "sixvertex", "phi4_triv", "phi4_z2", "phi4_imp1", "phi4_imp2"])
+                                  "sixvertex", "phi4_triv", "phi4_z2", "phi4_imp1", "phi4_imp2", "phi4_complex"])
 def test_models_match_oracle(tnr, oracle, name):
     o = oracle
     if name == "ising":
@@ -95,6 +95,8 @@ def test_models_match_oracle(tnr, oracle, name):
         a, b = tnr.phi4_real(8, -1.0, 1.0), o.phi4_real(8, -1.0, 1.0)
     elif name == "phi4_imp1":
         a, b = tnr.phi4_real_imp1(8, -2.0, 1.0), o.phi4_real_imp1(8, -2.0, 1.0)
+    elif name == "phi4_complex":
+        a, b = tnr.phi4_complex("Trivial", 4, -1.0, 1.0), o.phi4_complex(4, -1.0, 1.0)
     elif name == "phi4_imp2":
         a, b = tnr.phi4_real_imp2(8, -2.0, 1.0), o.phi4_real_imp2(8, -2.0, 1.0)
     else:

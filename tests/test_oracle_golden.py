@@ -432,16 +432,19 @@ def test_atrg3d_projectors_ignore_the_orthogonal_factor(oracle, monkeypatch):
     ("sixvertex", 1.0, 1.5 * math.log(0.75), 1e-3),
     ("phi4_trivial", -1.0, 0.4241912271276211, 1e-12),
     ("phi4_z2", -1.0, 0.4232381701937374, 1e-10),
+    ("phi4_complex", -1.0, 0.7583605364656325, 1e-9),
 ])
 def test_models_trg16_sixvertex_phi4(oracle, model, temp, answer, rtol):
     """test/models.jl:17-23,37-41: TRG, truncrank(16), maxiter(25) on the six-vertex model (Trivial;
     the reference's bar is rtol 1e-3 against 3/2 log(3/4)) and the real phi^4 model K = 10, mu0 = -1,
-    lam = 1 (Trivial and Z2).  The phi^4 answers are the reference's printed results to 16 digits;
-    the oracle reproduces them to 6e-16 (Trivial) and 4e-13 (Z2), so they are held far tighter
-    than the reference's 1e-3."""
+    lam = 1 (Trivial and Z2), and the complex phi^4 model (Trivial, K = 6, bond dimension 36).  The
+    phi^4 answers are the reference's printed results to 16 digits; the oracle reproduces them to
+    6e-16 (real, Trivial), 4e-13 (real, Z2) and 4e-10 (complex), so they are held far tighter than the
+    reference's 1e-3."""
     o = oracle
     T = {"sixvertex": lambda: o.sixvertex(), "phi4_trivial": lambda: o.phi4_real(10, -1.0, 1.0, symmetry="Trivial"),
-         "phi4_z2": lambda: o.phi4_real(10, -1.0, 1.0)}[model]()
+         "phi4_z2": lambda: o.phi4_real(10, -1.0, 1.0),
+         "phi4_complex": lambda: o.phi4_complex(6, -1.0, 1.0)}[model]()
     data = o.run(o.TRG(T), o.truncrank(16), o.maxiter(25))
     assert o.free_energy(data, temp) == pytest.approx(answer, rel=rtol)
 

@@ -233,6 +233,9 @@ def test_phi4_and_sixvertex_models(tnr, oracle):
     o = oracle
     d = tnr.run(tnr.TRG(tnr.phi4_real(10, -1.0, 1.0, symmetry="Trivial")), tnr.truncrank(16), tnr.maxiter(25))
     assert tnr.free_energy(d, -1.0) == pytest.approx(0.4241912271276211, rel=1e-10)
+    d = tnr.run(tnr.TRG(tnr.phi4_complex("Trivial", 6, -1.0, 1.0)), tnr.truncrank(16), tnr.maxiter(25))
+    do = o.run(o.TRG(o.phi4_complex(6, -1.0, 1.0)), o.truncrank(16), o.maxiter(25))
+    assert tnr.free_energy(d, -1.0) == pytest.approx(o.free_energy(do, -1.0), rel=1e-9)
     d = tnr.run(tnr.TRG(tnr.sixvertex()), tnr.truncrank(16), tnr.maxiter(25))
     do = o.run(o.TRG(o.sixvertex()), o.truncrank(16), o.maxiter(25))
     assert tnr.free_energy(d, 1.0) == pytest.approx(o.free_energy(do, 1.0), rel=1e-10)

@@ -25,7 +25,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from .models import (SymTensor, classical_clock, classical_ising, classical_ising_3D, classical_ising_impurity,  # noqa: F401
-                     classical_potts, f_onsager, ising_beta_c, ising_beta_c_3D, ising_βc, ising_βc_3D, phi4_real,
+                     classical_potts, f_onsager, ising_beta_c, ising_beta_c_3D, ising_βc, ising_βc_3D, phi4_complex, phi4_real,
                      phi4_real_imp1, phi4_real_imp2, potts_beta_c, potts_βc, random_hotrg_tensor, sixvertex)
 
 HERE = os.path.dirname(os.path.abspath(__file__))

@@ -174,6 +174,24 @@ def phi4_real(K, mu0, lam, h=0.0, symmetry="Z2"):
     return SymTensor(np.ascontiguousarray(t), [q.copy() for _ in range(4)], 2)
 
 
+def phi4_complex(symmetry, K, mu0, lam):
+    """``phi4_complex(Trivial, K, μ0, λ)`` (phi4_complex.jl:6-36,108-138,194-206): Gauss-Hermite
+    quadrature over the real and imaginary parts (K nodes each), bond dimension K²; the entries
+    are real.  The U(1) and Z2×Z2 forms are not built here."""
+    if symmetry != "Trivial":
+        raise ValueError("phi4_complex: only the Trivial form runs on this engine")
+    y, w = np.polynomial.hermite.hermgauss(K)
+    re1, im1, re2, im2 = np.meshgrid(y, y, y, y, indexing="ij")
+    F = np.exp(-0.5 * ((re1 - re2) ** 2 + (im1 - im2) ** 2) - mu0 / 8.0 * (re1 ** 2 + im1 ** 2 + re2 ** 2 + im2 ** 2)
+               - lam / 16.0 * ((re1 ** 2 + im1 ** 2) ** 2 + (re2 ** 2 + im2 ** 2) ** 2)).reshape(K * K, K * K)
+    U, S, V = np.linalg.svd(F)
+    left = U * np.sqrt(S)
+    right = np.sqrt(S)[:, None] * V
+    weight = (w[:, None] * w[None, :] * np.exp(y[:, None] ** 2 + y[None, :] ** 2)).reshape(-1)
+    return SymTensor(np.ascontiguousarray(np.einsum("p,pi,pj,kp,lp->ijkl", weight, left, left, right, right,
+                                                    optimize=True)), None, 1)
+
+
 def phi4_real_imp1(K, mu0, lam, h=0.0):
     """``phi4_real_imp1(Trivial, K, μ0, λ[, h])`` (phi4_real.jl:186-209): a φ insertion on the site."""
     return SymTensor(_phi4_gauss_hermite(K, mu0, lam, h, 1), None, 1)
