@@ -40,12 +40,20 @@ def parse():
     p.add_argument("--instances", type=int, default=256)
     p.add_argument("--maxiter", type=int, default=30)
     p.add_argument("--seed", type=int, default=2026)
-    p.add_argument("--plain-sample", type=int, default=64,
-                   help="instances of the batch also solved on the plain FP64 path (solves/s and |df/f|)")
+    p.add_argument("--plain-sample", type=int, default=-1,
+                   help="instances of the batch also solved on the plain FP64 path (solves/s and per-instance "
+                        "|df/f|); -1 = all of them")
     p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="beta_sweep", choices=["beta_sweep", "hotrg_step", "serving", "hotrg3d"],
-                   help="beta_sweep is the headline metric; the others measure the remaining configurations")
+    p.add_argument("--workload", default="beta_sweep",
+                   choices=["beta_sweep", "hotrg_step", "serving", "hotrg3d", "gemm"],
+                   help="beta_sweep is the headline metric; the others measure the remaining configurations; "
+                        "gemm times one batched split-precision product (the target of kernel captures)")
+    p.add_argument("--gemm", default="contract", choices=["contract", "single"],
+                   help="gemm workload: contraction path (chunked accumulation) or single accumulation")
+    p.add_argument("--m", type=int, default=2304, help="gemm workload: m = n")
+    p.add_argument("--k", type=int, default=2304, help="gemm workload: k")
+    p.add_argument("--batch", type=int, default=4, help="gemm workload: batch")
     p.add_argument("--chis", default=None, help="comma-separated chi list for hotrg_step / hotrg3d")
     p.add_argument("--requests", type=int, default=32, help="serving: number of requests in the arrival trace")
     return p.parse_args()
@@ -148,16 +156,21 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (NumPy/SciPy FP64 restatement) on a bounded sample
 # ---------------------------------------------------------------------------
-def cpu_solve_times(maxiter, budget):
-    """Per-chi seconds of one full BTRG solve on the host, from a bounded sample:
-    each chi runs steps until its share of the budget is spent, and the remaining
-    steps are extrapolated at the cost of the last (full-size) step."""
+def cpu_solve_times(betas, chis, maxiter, budget):
+    """Per-chi seconds of one full BTRG solve on the host, from a bounded sample: for each chi
+    the first instance of the workload with that chi runs at its own beta until its share of
+    the budget is spent (at least until the bond dimension has reached chi and one step at
+    full size has run); the steps it did not run are extrapolated at the cost of its last
+    step, which is a full-size step (every later step has the same shapes).  Returns
+    {chi: (seconds for a full solve, steps run, seconds measured, beta)}."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import tnr_oracle as o
     per = {}
     share = budget / len(CHIS)
     for chi in CHIS:
-        s = o.BTRG(o.classical_ising(0.45, "Trivial"))
+        idx = [i for i, c in enumerate(chis) if int(c) == chi]
+        beta = float(betas[idx[0]]) if idx else 0.45
+        s = o.BTRG(o.classical_ising(beta, "Trivial"))
         t0 = time.perf_counter()
         o.finalize(s)
         last = 0.0
@@ -171,18 +184,21 @@ def cpu_solve_times(maxiter, budget):
             if time.perf_counter() - t0 > share and s.T.a.shape[0] == chi:
                 break
         spent = time.perf_counter() - t0
-        per[chi] = spent + (maxiter - done) * last
-        per[chi] = (per[chi], done)
+        per[chi] = (spent + (maxiter - done) * last, done, spent, beta)
     return per
 
 
-def cpu_baseline(chis, maxiter, budget):
-    per = cpu_solve_times(maxiter, budget)
+def cpu_baseline(betas, chis, maxiter, budget):
+    """Whole-workload solves/s of the oracle on this host, estimated from cpu_solve_times;
+    returns (solves/s, sample description, seconds actually measured, extrapolated?)."""
+    per = cpu_solve_times(betas, chis, maxiter, budget)
     total = sum(per[int(c)][0] for c in chis)
-    sample = "oracle BTRG per chi in {8,16,24,32,48}: %s steps run (of %d), rest extrapolated at the last full-size " \
-             "step's cost; summed over the %d instances" % (
-                 ",".join("%d:%d" % (c, per[c][1]) for c in CHIS), maxiter, len(chis))
-    return len(chis) / total, sample
+    extrapolated = any(per[c][1] < maxiter for c in CHIS)
+    sample = "oracle BTRG, one instance per chi in {8,16,24,32,48} at its own beta: %s steps run of %d " \
+             "(measured %.1f s); unrun full-size steps extrapolated at the last step's cost; per-chi solve time " \
+             "summed over the %d instances' chi mix" % (
+                 ",".join("%d:%d" % (c, per[c][1]) for c in CHIS), maxiter, sum(per[c][2] for c in CHIS), len(chis))
+    return len(chis) / total, sample, sum(per[c][2] for c in CHIS), extrapolated
 
 
 def threads_used():
@@ -308,24 +324,32 @@ def run_ours(args, d):
     e2e = {"value": d.sum(n) / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(sum(T.array.nbytes for T in tensors)),
            "d2h_bytes_per_step": int(sum(8 * len(r) for r in norms))}
 
-    # plain FP64 GPU path on a sample of the same batch: solves/s and |df/f|
+    # plain FP64 GPU path on the same instances (all of them by default; the tests pin that path
+    # to the oracle at 1e-10): its solves/s, measured the same way as `value`, and the
+    # per-instance |df/f| of every split result against it
     plain = None
-    m = min(args.plain_sample, n)
+    m = n if args.plain_sample < 0 else min(args.plain_sample, n)
     if prec != tnr.PREC_F64 and m > 0:
         idx = list(range(m))
         sch = [tnr.BTRG(tensors[i], precision=tnr.PREC_F64) for i in idx]
         tm = {}
         ref = tnr.run_batch(sch, [chis[i] for i in idx], [args.maxiter] * m, timing=tm)
+        for sc in sch:
+            sc.close()
         f_ref = [tnr.free_energy(r, float(betas[i])) for r, i in zip(ref, idx)]
         rel = [abs(f_ours[i] - f_ref[j]) / abs(f_ref[j]) for j, i in enumerate(idx)]
-        # scale the sample's time to the whole batch by the per-chi mix of the sample
         worst = int(np.argmax(rel))
-        plain = {"solves_per_s_sample": m / (tm["device_ms"] / 1000.0), "sample_instances": m,
+        plain_sps = m / (tm["device_ms"] / 1000.0)
+        plain = {"solves_per_s": plain_sps, "instances": m, "same_instances_as_value": m == n,
+                 "split_speedup": value / plain_sps if m == n else None,
                  "max_rel_df": max(rel), "median_rel_df": statistics.median(rel),
+                 "count_rel_df_above_1e-7": int(sum(r > 1e-7 for r in rel)),
+                 "per_chi_max_rel_df": {str(c): max([r for r, i in zip(rel, idx) if int(chis[i]) == c] or [0.0])
+                                        for c in CHIS},
                  "worst": {"beta": float(betas[idx[worst]]), "chi": int(chis[idx[worst]]),
                            "f": f_ours[idx[worst]], "f_plain": f_ref[worst]}}
     elif prec == tnr.PREC_F64:
-        plain = {"solves_per_s_sample": value, "sample_instances": n, "max_rel_df": 0.0, "note": "this run is the plain path"}
+        plain = {"solves_per_s": value, "instances": n, "max_rel_df": 0.0, "note": "this run is the plain path"}
 
     # roofline of the dominant kernel class: one extra profiled pass of the same workload,
     # its lockstep groups run one after another so that each launch's CUDA-event window
@@ -380,7 +404,10 @@ def run_hotrg_step(args, tnr):
     out = []
     for chi in chis:
         T = tnr.random_hotrg_tensor(chi, 1)
-        row = {"chi": chi, "flops_contraction": 8.0 * chi ** 7 + 28.0 * chi ** 6}
+        # the engine's own contraction order: two half steps of 2 chi^7 + 4 chi^6 (hotrg_step_x2 /
+        # hotrg_step_y2) and four Gram networks of 6 chi^6 (hotrg_xproj / hotrg_yproj); the four
+        # eighs of n = chi^2 are not counted
+        row = {"chi": chi, "flops_contraction": 4.0 * chi ** 7 + 32.0 * chi ** 6}
         norms = {}
         for name, prec in (("f64", tnr.PREC_F64), ("split", tnr.PREC_SPLIT)):
             times = []
@@ -465,6 +492,18 @@ def run_hotrg3d(args, tnr):
     return {"workload": "hotrg3d: 3D Ising Z2 at beta=0.2216, HOTRG_3D", "rows": rows}
 
 
+def run_gemm(args, tnr):
+    """One warm-up and ``--steps`` timed batched m x m x k split-precision products on seeded,
+    device-resident operands: the contraction path (chunked accumulation when k > 64) or the
+    single-accumulation kernel of the truncated SVD's products."""
+    contraction = args.gemm == "contract"
+    m, k, b = args.m, args.k, args.batch
+    ms = tnr.gemm_time(m, m, k, b, False, False, tnr.PREC_SPLIT, max(args.steps, 1), contraction)
+    return {"workload": "gemm: %s m=n=%d k=%d batch=%d (split precision, plane pass included)" % (
+                args.gemm, m, k, b),
+            "ms": ms, "tflops_2mnk": 2.0 * m * m * k * b / (ms * 1e-3) / 1e12}
+
+
 def main():
     args = parse()
     d = Dist()
@@ -473,7 +512,8 @@ def main():
         import __graft_entry__ as ge
         ge.build()
         tnr = ge.package()
-        fn = {"hotrg_step": run_hotrg_step, "serving": run_serving, "hotrg3d": run_hotrg3d}[args.workload]
+        fn = {"hotrg_step": run_hotrg_step, "serving": run_serving, "hotrg3d": run_hotrg3d,
+              "gemm": run_gemm}[args.workload]
         if d.rank == 0:
             print(json.dumps(fn(args, tnr)), flush=True)
         return
@@ -481,15 +521,20 @@ def main():
         if d.rank != 0:
             return
         betas, chis = workload(args.instances, args.seed)
-        vals = []
+        vals, spent = [], []
         for i in range(args.warmup + args.steps):
-            v, sample = cpu_baseline(chis, args.maxiter, args.cpu_budget / 2)
+            v, sample, measured, extrapolated = cpu_baseline(betas, chis, args.maxiter, args.cpu_budget / 2)
             if i >= args.warmup:
                 vals.append(v)
+                spent.append(measured)
         v = statistics.median(vals)
         cores = threads_used()
+        # ms_per_step: the wall time one bench step (one bounded sample) actually took
         line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": d.world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1000.0 * args.instances / v, "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.mean(spent), "higher_is_better": True,
+                "extrapolated": extrapolated,
+                "extrapolation": "value = the whole workload's solves/s estimated from each step's sample; "
+                                 "ms_per_step = measured seconds of one sample",
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "impl": "reference",
                 "config": {"workload": "btrg_beta_sweep: %d BTRG solves, 2D Ising (Trivial), beta~U[0.30,0.60], "
@@ -504,9 +549,10 @@ def main():
     out, chis = run_ours(args, d)
     if d.rank == 0:
         if not args.no_cpu_baseline:
-            v, sample = cpu_baseline(chis, args.maxiter, args.cpu_budget)
+            betas, _ = workload(args.instances, args.seed)
+            v, sample, measured, extrapolated = cpu_baseline(betas, chis, args.maxiter, args.cpu_budget)
             out["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": threads_used(), "kind": "port",
-                                   "sample": sample}
+                                   "sample": sample, "measured_s": measured, "extrapolated": extrapolated}
         print(json.dumps(out), flush=True)
 
 

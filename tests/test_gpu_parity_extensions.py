@@ -201,14 +201,17 @@ def test_atrg3d(tnr, oracle):
 
 def test_convcrit_run(tnr, oracle):
     """run! with maxiter(30) & convcrit (src/utility/stopping.jl:7-22, evaluated on the host
-    after every device step): TRG on the Ising model at beta = 0.40, truncrank(16), stopping
-    once successive norms agree to 1e-8 (step 18 in the oracle, well before maxiter); the norms
-    equal the oracle's maxiter run of as many steps."""
+    after every device step): TRG on the Ising model at beta = 0.50, truncrank(16), stopping
+    once successive norms agree to 1e-8 (step 13 in the oracle, well before maxiter); the norms
+    equal the oracle's maxiter run of as many steps.  beta = 0.50 is well conditioned: the
+    oracle's own norms move by < 1e-14 under a 1e-14 input perturbation there, while at
+    beta = 0.40 steps 14-16 sit at a near-tie of the cut and move by 1e-6
+    (test_oracle_conditioning.py)."""
     o = oracle
     crit = tnr.maxiter(30) & tnr.convcrit(1e-8, lambda steps, d: abs(d[-1] / d[-2] - 1))
-    d = tnr.run(tnr.TRG(tnr.classical_ising("Trivial", 0.40)), tnr.truncrank(16), crit)
+    d = tnr.run(tnr.TRG(tnr.classical_ising("Trivial", 0.50)), tnr.truncrank(16), crit)
     assert 2 < len(d) < 31
-    do = o.run(o.TRG(o.classical_ising(0.40, "Trivial")), o.truncrank(16), o.maxiter(len(d) - 1))
+    do = o.run(o.TRG(o.classical_ising(0.50, "Trivial")), o.truncrank(16), o.maxiter(len(d) - 1))
     np.testing.assert_allclose(d, do, rtol=1e-10)
 
 
@@ -233,9 +236,13 @@ def test_phi4_and_sixvertex_models(tnr, oracle):
     o = oracle
     d = tnr.run(tnr.TRG(tnr.phi4_real(10, -1.0, 1.0, symmetry="Trivial")), tnr.truncrank(16), tnr.maxiter(25))
     assert tnr.free_energy(d, -1.0) == pytest.approx(0.4241912271276211, rel=1e-10)
+    # complex phi^4 (bond dimension 36): the oracle's own f moves by up to 1.1e-9 under a 1e-14
+    # input perturbation (test_oracle_conditioning.py), so f is held to 5e-9 against the oracle
+    # and to the same bar against the reference's printed 0.7583605364656325
     d = tnr.run(tnr.TRG(tnr.phi4_complex("Trivial", 6, -1.0, 1.0)), tnr.truncrank(16), tnr.maxiter(25))
     do = o.run(o.TRG(o.phi4_complex(6, -1.0, 1.0)), o.truncrank(16), o.maxiter(25))
-    assert tnr.free_energy(d, -1.0) == pytest.approx(o.free_energy(do, -1.0), rel=1e-9)
+    assert tnr.free_energy(d, -1.0) == pytest.approx(o.free_energy(do, -1.0), rel=5e-9)
+    assert tnr.free_energy(d, -1.0) == pytest.approx(0.7583605364656325, rel=5e-9)
     d = tnr.run(tnr.TRG(tnr.sixvertex()), tnr.truncrank(16), tnr.maxiter(25))
     do = o.run(o.TRG(o.sixvertex()), o.truncrank(16), o.maxiter(25))
     assert tnr.free_energy(d, 1.0) == pytest.approx(o.free_energy(do, 1.0), rel=1e-10)

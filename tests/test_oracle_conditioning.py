@@ -27,3 +27,43 @@ def test_lockstep_betas_are_well_conditioned(oracle, cls, chi, beta):
 
 def test_high_temperature_near_tie_is_ill_conditioned(oracle):
     assert _sensitivity(oracle, "TRG", 16, 0.33) > 1e-9
+
+
+def test_convcrit_betas(oracle):
+    """TRG, truncrank(16), 20 steps: at beta = 0.50 every norm moves by < 1e-13 under the
+    perturbation (the convcrit GPU case runs there); at beta = 0.40 steps 14-16 sit at a
+    near-tie of the cut and move by more than 1e-8."""
+    assert _sensitivity(oracle, "TRG", 16, 0.50, steps=20) < 1e-13
+    assert _sensitivity(oracle, "TRG", 16, 0.40, steps=20) > 1e-8
+
+
+def test_complex_phi4_free_energy_conditioning(oracle):
+    """Complex phi^4 (Trivial, K = 6, mu0 = -1, lambda = 1; bond dimension 36), TRG
+    truncrank(16), 25 steps: its mid-run norms sit near ties at the cut, and f itself moves
+    by more than 1e-10 under a 1e-14 input perturbation for at least one of three seeds
+    (measured up to 1.1e-9), so the GPU case holds f to 5e-9, not 1e-10."""
+    o = oracle
+    T0 = o.phi4_complex(6, -1.0, 1.0)
+    f0 = o.free_energy(o.run(o.TRG(T0), o.truncrank(16), o.maxiter(25)), -1.0)
+    worst = 0.0
+    for seed in (3, 4, 5):
+        rng = np.random.default_rng(seed)
+        T = o.phi4_complex(6, -1.0, 1.0)
+        T.a = T.a * (1 + 1e-14 * rng.standard_normal(T.a.shape))
+        f = o.free_energy(o.run(o.TRG(T), o.truncrank(16), o.maxiter(25)), -1.0)
+        worst = max(worst, abs(f / f0 - 1))
+    assert 1e-10 < worst < 5e-9
+
+
+@pytest.mark.parametrize("beta", [0.30, 0.33, 0.36])
+def test_high_temperature_free_energy_is_well_conditioned(oracle, beta):
+    """BTRG chi = 16, 30 steps: late-step norms of the high-temperature band sit near ties at
+    the cut, yet the free energy (norm i weighted by 2^-i) moves by < 1e-13 under a 1e-14 input
+    perturbation, so the split path's 1e-7 contract on f is meaningful there."""
+    o = oracle
+    rng = np.random.default_rng(1)
+    f0 = o.free_energy(o.run(o.BTRG(o.classical_ising(beta, "Trivial")), o.truncrank(16), o.maxiter(30)), beta)
+    T = o.classical_ising(beta, "Trivial")
+    T.a = T.a * (1 + 1e-14 * rng.standard_normal(T.a.shape))
+    f1 = o.free_energy(o.run(o.BTRG(T), o.truncrank(16), o.maxiter(30)), beta)
+    assert abs(f1 / f0 - 1) < 1e-13

@@ -4,8 +4,9 @@ Some callers cannot call cudaMalloc: code that runs inside another allocator's a
 CUDA.jl memory pool, a server that has reserved all free HBM) or on a latency-critical
 path where cudaMalloc's implicit device synchronisation would stall other streams.  The
 entry point keeps its BF16 plane scratch in a file-scope device array instead; the
-caller still owns A, B and C.  This file runs last (pytest collects it after the others)
-and must pass alone in a fresh process as well as after the rest of the suite.
+caller still owns A, B and C.  Its name sorts after every other test file, so pytest
+collects it last; it must pass alone in a fresh process as well as after the rest of the
+suite.
 """
 import ctypes as C
 
@@ -55,16 +56,18 @@ def from_device(rt, p, shape):
     return out
 
 
-def noalloc_gemm(tnr, rt, A, B, ta, tb):
+def noalloc_gemm(tnr, rt, A, B, ta, tb, alpha=1.0, beta=0.0, C0=None):
+    """C = alpha op(A) op(B) + beta C0 through the allocation-free entry point; with beta = 0
+    C starts as NaN, which the kernel must overwrite without reading."""
     m = A.shape[1] if ta else A.shape[0]
     k = A.shape[0] if ta else A.shape[1]
     n = B.shape[0] if tb else B.shape[1]
     dA, _ = to_device(rt, A)
     dB, _ = to_device(rt, B)
-    dC, _ = to_device(rt, np.full((m, n), np.nan))               # the kernel must overwrite C
+    dC, _ = to_device(rt, np.full((m, n), np.nan) if C0 is None else C0)
     err = C.create_string_buffer(512)
     try:
-        st = tnr.lib().tnr_gemm_split_noalloc(int(ta), int(tb), m, n, k, 1.0, dA, A.shape[0], dB, B.shape[0], 0.0,
+        st = tnr.lib().tnr_gemm_split_noalloc(int(ta), int(tb), m, n, k, alpha, dA, A.shape[0], dB, B.shape[0], beta,
                                               dC, m, None, err, 512)
         assert st == 0, err.value.decode()
         return from_device(rt, dC, (m, n))
@@ -77,7 +80,7 @@ def test_noalloc_matches_allocating_entry_point(tnr, rt):
     rng = np.random.default_rng(11)
     # two calls in a row with different shapes: the shared scratch keeps the first call's
     # planes, the second call must not see them
-    for m, n, k, ta, tb in [(300, 200, 77, False, True), (256, 512, 384, True, False)]:
+    for m, n, k, ta, tb in [(300, 200, 77, False, True), (256, 512, 384, True, False), (192, 96, 48, False, False)]:
         A = rng.standard_normal((k, m) if ta else (m, k))
         B = rng.standard_normal((n, k) if tb else (k, n))
         got = noalloc_gemm(tnr, rt, A, B, ta, tb)
@@ -100,3 +103,21 @@ def test_noalloc_rejects_oversized_operands(tnr):
                                           0.0, C.c_void_p(16), 2048, None, err, 512)
     assert st == 1
     assert b"16777216" in err.value
+
+
+def test_noalloc_alpha_beta_epilogue(tnr, rt):
+    """alpha != 1 and beta != 0 on a pre-filled, finite C: the epilogue reads C0 and writes
+    alpha op(A) op(B) + beta C0; the product part agrees with the allocating entry point."""
+    rng = np.random.default_rng(12)
+    for m, n, k in [(128, 64, 40), (200, 136, 200)]:
+        A, B = rng.standard_normal((m, k)), rng.standard_normal((k, n))
+        C0 = rng.standard_normal((m, n))
+        alpha, beta = -0.75, 1.5
+        got = noalloc_gemm(tnr, rt, A, B, False, False, alpha, beta, C0)
+        ref = tnr.debug_gemm(A, B, False, False, tnr.PREC_SPLIT)
+        want = alpha * ref + beta * C0
+        scale = np.linalg.norm(alpha * (A @ B)) + np.linalg.norm(beta * C0)
+        tol = 1e-12 if k <= 64 else 6e-8 * np.sqrt(k)
+        assert np.linalg.norm(got - want) / scale < tol
+        exact = alpha * (A @ B) + beta * C0
+        assert np.linalg.norm(got - exact) / scale < 6e-8 * np.sqrt(k)

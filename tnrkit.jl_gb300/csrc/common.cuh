@@ -41,6 +41,27 @@ struct Error : public std::runtime_error {
 
 // every kernel launch goes through this counter (reported by tnr_kernel_launches)
 extern std::atomic<uint64_t> g_launches;
+
+// Per-device one-time setup: `done` holds one bit per device index (0..63).  A kernel's
+// dynamic shared-memory limit and a memory pool's attributes belong to the current device's
+// context, so a process that uses several devices sets them on each.  Two threads that race
+// on the same device both set the same value, which is harmless.
+inline bool device_once(std::atomic<uint64_t>& done, int* dev_out = nullptr) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev > 63) {
+        cudaGetLastError();
+        throw ::tnr::Error(TNR_ERR_CUDA, "no current CUDA device (or device index above 63)");
+    }
+    if (dev_out) *dev_out = dev;
+    return !(done.load(std::memory_order_acquire) & (1ull << dev));
+}
+inline void device_done(std::atomic<uint64_t>& done, int dev) { done.fetch_or(1ull << dev, std::memory_order_release); }
+inline void ensure_smem_attr(std::atomic<uint64_t>& done, const void* func, int bytes) {
+    int dev = 0;
+    if (!device_once(done, &dev)) return;
+    TNR_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    device_done(done, dev);
+}
 inline void count_launch(int n = 1) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
 inline void check_launch(const char* what) {
@@ -267,17 +288,6 @@ void sum_squares(Ctx& c, const double* x, int64_t n, double* out);
 void scale_inplace(Ctx& c, double* x, int64_t n, const double* inv_scale_ptr);
 void fill_identity(Ctx& c, double* x, int64_t m, int64_t n);
 void copy_f64(Ctx& c, double* dst, const double* src, int64_t n);
-// Canonical singular vectors inside degenerate groups.  vals: the k kept singular values
-// (descending); U (m x k, ld m) and Vt (k x n, ld k) of one SVD.  Values within
-// TNR_DEGENERATE_REL * vals[0] of a group's first value form a group; inside each group
-// the vectors are rotated (U <- U W, Vt <- W^T Vt, W orthogonal) to the eigenbasis of
-// U_g^T diag(d) U_g for the fixed sequence d_r = frac((r + 1) * golden ratio).  That basis is
-// unique for distinct eigenvalues, and it is parity-pure whenever the group's span splits
-// into vectors of disjoint row supports (a Z2 block structure).  Singleton columns are
-// left bit-for-bit unchanged.  With a degenerate group present, k above the Jacobi
-// solver's size (160) is refused.
-#define TNR_DEGENERATE_REL 1e-11
-void degenerate_basis(Ctx& c, const std::vector<double>& vals, double* U, int64_t m, double* Vt, int64_t n);
 // Q (m x r, orthonormal columns spanning those of Y) by shifted CholeskyQR3; Y is overwritten
 void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q);
 // dst[0] = |src[0]|
@@ -306,8 +316,17 @@ struct TsvdOut {
 
 // M (m x n, ld = m, column-major): U (m x k), s (k), Vt (k x n)
 TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt);
+// R' = diag(s) V^T (n x n) from the SVD M = U diag(s) V^T of a column-major m x n matrix (m >= n,
+// n <= 160).  R' equals the R of any QR decomposition M = Q R up to an orthogonal factor on its
+// rows (R = W R'), for every rank of M: exactly rank-deficient M, which breaks CholeskyQR, is fine.
+void svd_r_factor(Ctx& c, const double* M, int64_t m, int n, double* R);
 // symmetric M (n x n): U (n x k) eigenvectors of the k largest |eigenvalues|, lam (k)
 TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lam);
+// The truncated SVD of M over the sectors its exact zeros reveal (connected components of the
+// bipartite graph row r -- column c iff M[r, c] != 0): one SVD per sector block, the k largest
+// values over all blocks kept, every singular vector supported on one sector (zero elsewhere).
+// A matrix without such structure is one sector: then it is tsvd itself.
+TsvdOut tsvd_sectors(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt);
 // B stacked m x n matrices (stride m*n), decomposed in lockstep: U [B][m x k], s [B][k], Vt [B][k x n]
 std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U, double* s,
                                   double* Vt);

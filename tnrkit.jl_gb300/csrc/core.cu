@@ -104,18 +104,18 @@ static size_t round_block(size_t b) {
 
 // Stream-ordered allocations: cudaMallocAsync / cudaFreeAsync never synchronise the device,
 // so many handles on many streams allocate without stalling each other.  The device's
-// default pool keeps freed memory cached (release threshold raised once per process).
+// default pool keeps freed memory cached (release threshold raised once per device).
 static void keep_pool_memory() {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        int dev = 0;
-        cudaMemPool_t mp;
-        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&mp, dev) == cudaSuccess) {
-            uint64_t thr = ~0ull;
-            cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &thr);
-        }
-        cudaGetLastError();
-    });
+    static std::atomic<uint64_t> done{0};
+    int dev = 0;
+    if (!device_once(done, &dev)) return;
+    cudaMemPool_t mp;
+    if (cudaDeviceGetDefaultMemPool(&mp, dev) == cudaSuccess) {
+        uint64_t thr = ~0ull;
+        cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    cudaGetLastError();
+    device_done(done, dev);
 }
 
 Pool::~Pool() {

@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -577,13 +578,15 @@ void split_operand(Ctx& c, const double* src, int64_t rows, int64_t K, int64_t K
 
 namespace {
 
+// The kernels' dynamic shared-memory limits are attributes of the current device's context,
+// so they are raised once per device (first tensor-core call with that device current).
+std::atomic<uint64_t> g_tc_attr_set{0};
+
 bool tc_ready() {
     if (!encode_fn()) return false;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_gemm_split_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        cudaFuncSetAttribute(k_gemm_split_tc_chunked, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES_ACC);
-    });
+    ensure_smem_attr(g_tc_attr_set, (const void*)k_gemm_split_tc, SMEM_BYTES);
+    static std::atomic<uint64_t> acc_set{0};
+    ensure_smem_attr(acc_set, (const void*)k_gemm_split_tc_chunked, SMEM_BYTES_ACC);
     return true;
 }
 
@@ -724,6 +727,7 @@ static __device__ int g_noalloc_status;
 struct NoAllocDevice {
     unsigned char* scratch = nullptr;
     int* status = nullptr;
+    bool smem_attr = false;   // k_gemm_split_tc's dynamic shared-memory limit raised on this device
 };
 constexpr int NOALLOC_MAX_DEVICES = 64;
 NoAllocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
@@ -741,6 +745,11 @@ const NoAllocDevice* noalloc_device(int dev) {
         TNR_CUDA(cudaGetSymbolAddress(&q, g_noalloc_status));
         d.scratch = static_cast<unsigned char*>(p);
         d.status = static_cast<int*>(q);
+    }
+    if (!d.smem_attr) {
+        // set here, with this device current, under the mutex (not through tc_ready's shared flag)
+        TNR_CUDA(cudaFuncSetAttribute(k_gemm_split_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        d.smem_attr = true;
     }
     return &d;
 }
@@ -767,6 +776,11 @@ extern "C" int tnr_gemm_split_noalloc(int ta, int tb, int64_t m, int64_t n, int6
     if (m < 64 || n < 16 || k < 16)
         return report(TNR_ERR_UNSUPPORTED, "split kernel shape limits: m >= 64, n >= 16, k >= 16");
     if (lda < (ta ? k : m) || ldb < (tb ? n : k) || ldc < m) return report(TNR_ERR_INVALID_ARG, "leading dimension too small");
+    // each of m, n and ceil8(k) is at most the scratch size, so the byte counts below
+    // cannot overflow (and the grid stays far inside its limits)
+    if (m > (int64_t)NOALLOC_SCRATCH_BYTES || n > (int64_t)NOALLOC_SCRATCH_BYTES || k > (int64_t)NOALLOC_SCRATCH_BYTES)
+        return report(TNR_ERR_INVALID_ARG, "operands exceed the allocation-free scratch of " +
+                                               std::to_string(NOALLOC_SCRATCH_BYTES) + " bytes (6*(m+n)*ceil8(k) bytes)");
     if ((n + BN - 1) / BN > 65535) return report(TNR_ERR_UNSUPPORTED, "n too large for the grid");
     const int64_t Kp = (k + 7) / 8 * 8;
     const size_t bytesA = (size_t)3 * m * Kp * 2, bytesB = (size_t)3 * n * Kp * 2;
@@ -782,10 +796,6 @@ extern "C" int tnr_gemm_split_noalloc(int ta, int tb, int64_t m, int64_t n, int6
         const NoAllocDevice* d = noalloc_device(dev);
         TNR_REQUIRE(encode_fn(), TNR_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        static std::once_flag once;
-        std::call_once(once, [] {
-            cudaFuncSetAttribute(k_gemm_split_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        });
         // the status word keeps the previous call's value: clear it
         TNR_CUDA(cudaMemsetAsync(d->status, 0, sizeof(int), st));
         __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(d->scratch);

@@ -189,11 +189,9 @@ static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W
     const size_t aux = 2 * (JMAX / 2 + 1) * (sizeof(T) + sizeof(int));
     const bool w_in_smem = sizeof(T) == 4;      // FP32: eigenvectors in shared memory as well
     size_t smem = (size_t)(r + 1) * r * sizeof(T) + aux + (w_in_smem ? (size_t)r * r * sizeof(T) : 0);
-    static std::once_flag once;
-    std::call_once(once, [aux, w_in_smem] {
-        size_t maxs = (size_t)(JMAX + 1) * JMAX * sizeof(T) + aux + (w_in_smem ? (size_t)JMAX * JMAX * sizeof(T) : 0);
-        cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxs);
-    });
+    static std::atomic<uint64_t> attr_set{0};
+    const size_t maxs = (size_t)(JMAX + 1) * JMAX * sizeof(T) + aux + (w_in_smem ? (size_t)JMAX * JMAX * sizeof(T) : 0);
+    ensure_smem_attr(attr_set, (const void*)k_jacobi<T>, (int)maxs);
     Buf ww(c.pool.get(), w_in_smem ? sizeof(T) : (size_t)batch * r * r * sizeof(T));
     int nt = r <= 32 ? 128 : (r <= 64 ? 256 : JTHREADS);
     int rec = prof_start(c.stream);
@@ -290,11 +288,9 @@ static void launch_chol(Ctx& c, double* G, int r, double shift, int batch) {
     TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "chol_inv: r out of range");
     size_t smem = (size_t)(r + 1) * r * sizeof(T);
     TNR_REQUIRE(smem <= 227 * 1024, TNR_ERR_UNSUPPORTED, "chol_inv: matrix too large for shared memory");
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_chol_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::min<size_t>((size_t)(JMAX + 1) * JMAX * sizeof(T), 227 * 1024));
-    });
+    static std::atomic<uint64_t> attr_set{0};
+    ensure_smem_attr(attr_set, (const void*)k_chol_inv<T>,
+                     (int)std::min<size_t>((size_t)(JMAX + 1) * JMAX * sizeof(T), 227 * 1024));
     int rec = prof_start(c.stream);
     k_chol_inv<T><<<batch, 512, smem, c.stream>>>(G, r, shift, c.d_status);
     check_launch("chol_inv");
@@ -303,68 +299,5 @@ static void launch_chol(Ctx& c, double* G, int r, double shift, int batch) {
 
 void chol_inv(Ctx& c, double* G, int r, double shift, int batch) { launch_chol<double>(c, G, r, shift, batch); }
 void chol_inv_f32(Ctx& c, double* G, int r, double shift, int batch) { launch_chol<float>(c, G, r, shift, batch); }
-
-// Group index of each kept singular vector, passed by value to the Gram kernel.
-struct DegenGroups {
-    int gid[JMAX];
-    int ng;
-};
-
-// G[i + j k] = [gid_i == gid_j] (sum_r U[r,a] d_r U[r,b] + [i == j] 2 (ng - gid_i)), a = min(i,j),
-// b = max(i,j), d_r = frac((r + 1) * golden ratio) in [0, 1).  The diagonal offsets keep every
-// group's eigenvalues in its own interval [2 (ng - gid), 2 (ng - gid) + 1), so a solver that sorts
-// by |lambda| keeps the groups in their order.  One warp per entry (warps never straddle k*k).
-__global__ void __launch_bounds__(256)
-k_degen_gram(const double* __restrict__ U, int64_t m, int k, DegenGroups g, double* __restrict__ G) {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (w >= (int64_t)k * k) return;
-    const int i = (int)(w % k), j = (int)(w / k);
-    double acc = 0.0;
-    if (g.gid[i] == g.gid[j]) {
-        const double* ua = U + (int64_t)min(i, j) * m;
-        const double* ub = U + (int64_t)max(i, j) * m;
-        for (int64_t r = lane; r < m; r += 32) {
-            const double t = (double)(r + 1) * 0.6180339887498949;
-            acc += ua[r] * (t - floor(t)) * ub[r];
-        }
-        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (i == j) acc += 2.0 * (double)(g.ng - g.gid[i]);
-    }
-    if (lane == 0) G[i + (int64_t)j * k] = acc;
-}
-
-void degenerate_basis(Ctx& c, const std::vector<double>& vals, double* U, int64_t m, double* Vt, int64_t n) {
-    const int k = (int)vals.size();
-    if (k < 2) return;
-    std::vector<int> gid(k);
-    int ng = 0;
-    const double tol = TNR_DEGENERATE_REL * std::fabs(vals[0]);
-    bool any = false;
-    for (int i = 0; i < k;) {
-        int j = i + 1;
-        while (j < k && std::fabs(vals[j] - vals[i]) <= tol) ++j;
-        any = any || j - i > 1;
-        for (int t = i; t < j; ++t) gid[t] = ng;
-        ++ng;
-        i = j;
-    }
-    if (!any) return;
-    TNR_REQUIRE(k <= JMAX, TNR_ERR_UNSUPPORTED, "degenerate_basis: more kept values than the Jacobi solver holds");
-    DegenGroups g;
-    g.ng = ng;
-    for (int t = 0; t < JMAX; ++t) g.gid[t] = t < k ? gid[t] : -1;
-    Pool* pool = c.pool.get();
-    Buf G(pool, (size_t)k * k * sizeof(double)), W(pool, (size_t)k * k * sizeof(double)), lam(pool, (size_t)k * sizeof(double));
-    const int64_t threads = (int64_t)k * k * 32;
-    k_degen_gram<<<(unsigned)((threads + 255) / 256), 256, 0, c.stream>>>(U, m, k, g, G.d());
-    check_launch("degen_gram");
-    jacobi_eigh(c, G.d(), k, k, W.d(), lam.d());
-    Buf U2(pool, (size_t)m * k * sizeof(double)), V2(pool, (size_t)k * n * sizeof(double));
-    gemm_f64(c, false, false, m, k, k, 1.0, U, m, 0, W.d(), k, 0, 0.0, U2.d(), m, 0);
-    gemm_f64(c, true, false, k, n, k, 1.0, W.d(), k, 0, Vt, k, 0, 0.0, V2.d(), k, 0);
-    copy_f64(c, U, U2.d(), m * (int64_t)k);
-    copy_f64(c, Vt, V2.d(), (int64_t)k * n);
-}
 
 }  // namespace tnr

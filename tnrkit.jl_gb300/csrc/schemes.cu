@@ -36,17 +36,17 @@ void Scheme::record(const TsvdOut& r) {
 }
 
 // SVD12 (src/utility/projectors.jl:211-217): M4 as (d1 d2) x (d3 d4) -> A = U sqrt(s), B = sqrt(s) V
-// canonical: inside every group of kept singular values equal to within the degeneracy
-// tolerance, the singular vectors are rotated to a fixed basis (degenerate_basis)
-static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B, bool canonical = false) {
+// sectors: decompose block by block over the sectors of M4's exact zeros (tsvd_sectors), so
+// that every kept vector lies in one symmetry sector, as LAPACK's vectors of these
+// block-structured matrices do
+static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B, bool sectors = false) {
     Ctx& c = *s.ctx;
     int64_t m = M4.d[0] * M4.d[1], n = M4.d[2] * M4.d[3];
     int k = (int)std::min<int64_t>(chi, std::min(m, n));
     A = make_dt(c.pool.get(), {M4.d[0], M4.d[1], (int64_t)k});
     B = make_dt(c.pool.get(), {(int64_t)k, M4.d[2], M4.d[3]});
     Buf sv(c.pool.get(), (size_t)k * sizeof(double));
-    TsvdOut r = tsvd(c, M4.p(), m, n, k, A.p(), sv.d(), B.p());
-    if (canonical) degenerate_basis(c, r.vals, A.p(), m, B.p(), n);
+    TsvdOut r = sectors ? tsvd_sectors(c, M4.p(), m, n, k, A.p(), sv.d(), B.p()) : tsvd(c, M4.p(), m, n, k, A.p(), sv.d(), B.p());
     col_scale(c, A.p(), m, k, m, sv.d(), 1);
     row_scale(c, B.p(), k, n, k, sv.d(), 1);
     s.record(r);
@@ -142,15 +142,14 @@ static void step_atrg(Scheme& s, int chi) {
 }
 
 // R of a QR decomposition Mat = Q R of a column-major m x n matrix (m >= n), up to an orthogonal
-// factor on its rows: Q by CholeskyQR3, R = Q^T Mat (n x n).  The oblique projectors of ATRG_3D
-// use R only through R and R^T R, which that factor leaves unchanged.
+// factor on its rows: R' = diag(s) V^T from Mat's SVD.  The oblique projectors of ATRG_3D see R
+// only through products whose SVD absorbs that factor (temp = R1 R2^T -> W1 temp W2^T), so they
+// are unchanged.  At truncrank(12) these matrices can be exactly rank-deficient (the reference's
+// LAPACK QR returns zero rows of R there); the SVD form needs no Cholesky of their Gram matrix.
 static Buf qr_r(Ctx& c, const double* Mat, int64_t m, int64_t n) {
     TNR_REQUIRE(m >= n && n <= 160, TNR_ERR_UNSUPPORTED, "ATRG_3D: QR of a wide matrix or above 160 columns");
-    Buf Y(c.pool.get(), (size_t)m * n * sizeof(double)), Q(c.pool.get(), (size_t)m * n * sizeof(double));
-    copy_f64(c, Y.d(), Mat, m * n);
-    orth_scaled(c, Y.d(), m, (int)n, Q.d());
     Buf R(c.pool.get(), (size_t)n * n * sizeof(double));
-    gemm_f64(c, true, false, n, n, m, 1.0, Q.d(), m, 0, Mat, m, 0, 0.0, R.d(), n, 0);
+    svd_r_factor(c, Mat, m, (int)n, R.d());
     return R;
 }
 
@@ -268,8 +267,9 @@ static void step_atrg3d(Scheme& s, int chi) {
 // pure tensor, and of sites 2 and 4 and the pure tensor transposed ((2,4),(1,3)); the new
 // pure and site tensors are five TRG contractions of those factors.  The contractions pair
 // factors of different SVDs, so the result depends on the basis each SVD picks inside a
-// degenerate group; the canonical basis keeps the vectors of a Z2-odd impurity's degenerate
-// pairs parity-pure (the choice LAPACK happens to make on such block-structured matrices)
+// degenerate group; decomposing over the sectors of the exact zeros keeps the vectors of a
+// Z2-odd impurity's degenerate pairs in one sector each (the choice LAPACK makes on such
+// block-structured matrices)
 static void step_impurity_trg(Scheme& s, int chi) {
     Ctx& c = *s.ctx;
     TNR_REQUIRE(s.T.d[0] == s.T.d[3] && s.T.d[1] == s.T.d[2], TNR_ERR_INVALID_ARG,

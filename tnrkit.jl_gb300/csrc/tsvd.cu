@@ -28,6 +28,7 @@ namespace tnr {
 constexpr int RDIRECT = 128;
 constexpr int RMAX = 128;
 constexpr int MAXIT = 40;
+constexpr int RSMALL = 160;     // largest matrix of the one-CTA Jacobi solvers
 
 static void check_status(Ctx& c, const char* where) {
     int st = c.read_status_and_clear();
@@ -135,6 +136,16 @@ static void transpose2d(Ctx& c, const double* in, int64_t m, int64_t n, double* 
     int64_t d[2] = {m, n};
     int perm[2] = {1, 0};
     permute(c, in, d, 2, perm, out);
+}
+
+void svd_r_factor(Ctx& c, const double* M, int64_t m, int n, double* R) {
+    TNR_REQUIRE(m >= n && n >= 1 && n <= RSMALL, TNR_ERR_UNSUPPORTED, "svd_r_factor: needs m >= n and n <= 160");
+    Buf Ux(c.pool.get(), (size_t)m * n * sizeof(double));
+    Buf V(c.pool.get(), (size_t)n * n * sizeof(double));
+    Buf sv(c.pool.get(), (size_t)n * sizeof(double));
+    final_svd(c, M, false, m, n, Ux.d(), sv.d(), V.d());
+    transpose2d(c, V.d(), n, n, R);
+    row_scale(c, R, n, n, n, sv.d(), 0);
 }
 
 // iterations needed so the kept subspace reaches the target angle: one iteration
