@@ -249,6 +249,14 @@ int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t 
                    const double* B, int64_t ldb, int64_t strideB,
                    double* C, int64_t ldc, int64_t strideC, int batch);
 
+/* Inverse Cholesky factors through the engine's one-CTA kernel: for each of `batch`
+ * symmetric r x r matrices G (column-major, host, lower triangle read), Linv =
+ * L^-1 with (G + shift I) = L L^T, lower triangular, zero above.  precision
+ * TNR_PREC_SPLIT runs the FP32 kernel of the split path's orthonormalisation,
+ * TNR_PREC_F64 the FP64 one; *breakdown = 1 when a pivot was not positive.
+ * No reference counterpart (parity test of the CholeskyQR kernels). */
+int tnr_debug_chol(int precision, int r, double shift, int batch, const double* G, double* Linv, int* breakdown);
+
 /* Device time of one batched GEMM of that shape on seeded N(0,1) device operands
  * (contiguous column-major, strides m*k, k*n, m*n): *ms_out = the CUDA-event time
  * of `reps` back-to-back calls / reps, after one untimed call.  For the split

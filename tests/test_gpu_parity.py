@@ -226,7 +226,7 @@ def test_split_gemm_tc(tnr, m, n, k, ta, tb, batch):
     assert np.linalg.norm(f64 - ref) / np.linalg.norm(ref) < 1e-14
 
 
-@pytest.mark.parametrize("cls,chi", [("BTRG", 24), ("TRG", 16)])
+@pytest.mark.parametrize("cls,chi", [("BTRG", 24), ("TRG", 24)])
 @pytest.mark.parametrize("precision", ["f64", "split"])
 def test_lockstep_group_equals_single(tnr, cls, chi, precision):
     """Equal-chi instances in one run_batch step in lockstep (one batched launch per kernel);
@@ -288,7 +288,7 @@ def test_split_group_fixed_point_flows(tnr, seed):
         assert abs(g / r - 1) <= 1e-7, (b, g, r)
 
 
-@pytest.mark.parametrize("chi", [16, 32])
+@pytest.mark.parametrize("chi", [24, 32])
 def test_split_high_temperature_band(tnr, oracle, chi):
     """The headline sweep draws beta ~ U[0.30, 0.60]; at beta = 0.30-0.36 late-step norms sit
     near ties at the cut (they move by 1e-7 under a 1e-14 input perturbation), while f does
@@ -308,3 +308,42 @@ def test_split_high_temperature_band(tnr, oracle, chi):
     o = oracle
     fo = o.free_energy(o.run(o.BTRG(o.classical_ising(0.33, "Trivial")), o.truncrank(chi), o.maxiter(30)), 0.33)
     assert ref[3] == pytest.approx(fo, rel=1e-12)
+
+
+def test_split_small_chi_runs_plain(tnr, oracle):
+    """A 2D split-precision solve at chi <= 16 runs every step on the plain FP64 path (the
+    split products moved f by 2.2e-7 at chi = 16, beta = 0.304): at beta = 0.45 its norms equal
+    the oracle's to 1e-10, and at beta = 0.304 (whose late norms sit at a near-tie of the cut)
+    its f equals the oracle's to 1e-12, like the plain path's."""
+    o = oracle
+    d = tnr.run(tnr.BTRG(tnr.classical_ising("Trivial", 0.45), precision=tnr.PREC_SPLIT), tnr.truncrank(16),
+                tnr.maxiter(30))
+    do = o.run(o.BTRG(o.classical_ising(0.45, "Trivial")), o.truncrank(16), o.maxiter(30))
+    np.testing.assert_allclose(d, do, rtol=1e-10)
+    d = tnr.run(tnr.BTRG(tnr.classical_ising("Trivial", 0.304), precision=tnr.PREC_SPLIT), tnr.truncrank(16),
+                tnr.maxiter(30))
+    do = o.run(o.BTRG(o.classical_ising(0.304, "Trivial")), o.truncrank(16), o.maxiter(30))
+    assert tnr.free_energy(d, 0.304) == pytest.approx(o.free_energy(do, 0.304), rel=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_chol_inv_kernel(tnr, precision):
+    """The one-CTA Cholesky + triangular-inverse kernel of CholeskyQR3 (blocked by 32 columns)
+    against NumPy on batches of SPD matrices of every block shape up to the 160 limit, and its
+    breakdown flag on an indefinite matrix."""
+    prec = tnr.PREC_F64 if precision == "f64" else tnr.PREC_SPLIT
+    rng = np.random.default_rng(5)
+    for r in (1, 7, 31, 32, 33, 64, 100, 128, 160):
+        A = rng.standard_normal((3, 2 * r + 4, r))
+        G = np.einsum('bkr,bks->brs', A, A)
+        got, bad = tnr.debug_chol(G, 0.0, prec)
+        assert not bad
+        for b in range(3):
+            ref = np.linalg.inv(np.linalg.cholesky(G[b]))
+            err = np.abs(got[b] - ref).max() / np.abs(ref).max()
+            assert err < (1e-12 if precision == "f64" else 1e-4), (r, b, err)
+            assert np.all(np.triu(got[b], 1) == 0)
+    G = np.eye(40)
+    G[17, 17] = -1.0
+    _, bad = tnr.debug_chol(G, 0.0, prec)
+    assert bad

@@ -112,6 +112,7 @@ def lib():
         "tnr_debug_gemm": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, pd, C.c_int64, C.c_int64, pd, C.c_int64,
                                C.c_int64, pd, C.c_int64, C.c_int64, I]),
         "tnr_gemm_time": (I, [I, I, I, C.c_int64, C.c_int64, C.c_int64, I, I, I, pd]),
+        "tnr_debug_chol": (I, [I, I, D, I, pd, pd, C.POINTER(I)]),
         "tnr_gemm_split_noalloc": (I, [I, I, C.c_int64, C.c_int64, C.c_int64, D, P, C.c_int64, P, C.c_int64, D, P,
                                        C.c_int64, P, C.c_char_p, Z]),
         "tnr_server_create": (I, [C.POINTER(P), Z, I, I]),
@@ -740,6 +741,21 @@ def debug_gemm(A, B, ta=False, tb=False, precision=PREC_SPLIT):
     _check(st)
     out = np.transpose(Cf, (0, 2, 1))
     return out if A.ndim == 3 else out[0]
+
+
+def debug_chol(G, shift=0.0, precision=PREC_F64):
+    """L^-1 of the Cholesky factor of G + shift I through the engine's kernel (G: [batch,] r x r);
+    returns (Linv, breakdown)."""
+    G3 = np.asarray(G, dtype=np.float64)
+    G3 = G3 if G3.ndim == 3 else G3[None]
+    batch, r = G3.shape[0], G3.shape[1]
+    Gf = np.ascontiguousarray(np.transpose(G3, (0, 2, 1)))
+    out = np.zeros_like(Gf)
+    bd = C.c_int()
+    _check(lib().tnr_debug_chol(precision, r, float(shift), batch, Gf.ctypes.data_as(C.POINTER(C.c_double)),
+                                out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(bd)))
+    L = np.transpose(out, (0, 2, 1))
+    return (L if np.ndim(G) == 3 else L[0]), bool(bd.value)
 
 
 def gemm_time(m, n, k, batch=1, ta=False, tb=False, precision=PREC_SPLIT, reps=5, contraction=False):

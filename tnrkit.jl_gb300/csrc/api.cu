@@ -629,6 +629,23 @@ int tnr_profile_read(int cls, uint64_t* launches, double* total_ms, double* work
     return guarded(nullptr, [&] { prof_read(cls, launches, total_ms, work); });
 }
 
+int tnr_debug_chol(int precision, int r, double shift, int batch, const double* G, double* Linv, int* breakdown) {
+    if (!G || !Linv || !breakdown || r < 1 || batch < 1) return fail(nullptr, TNR_ERR_INVALID_ARG, "bad chol");
+    return guarded(nullptr, [&] {
+        require_device();
+        Ctx c(nullptr, precision, 0);
+        const size_t bytes = (size_t)batch * r * r * sizeof(double);
+        Buf dG(c.pool.get(), bytes);
+        TNR_CUDA(cudaMemcpyAsync(dG.d(), G, bytes, cudaMemcpyHostToDevice, c.stream));
+        if (precision == TNR_PREC_SPLIT) chol_inv_f32(c, dG.d(), r, shift, batch);
+        else chol_inv(c, dG.d(), r, shift, batch);
+        TNR_CUDA(cudaMemcpyAsync(Linv, dG.d(), bytes, cudaMemcpyDeviceToHost, c.stream));
+        const int st = c.read_status_and_clear();
+        *breakdown = (st & ST_CHOL_BREAKDOWN) ? 1 : 0;
+        TNR_REQUIRE((st & ~ST_CHOL_BREAKDOWN) == 0, TNR_ERR_CUDA, "kernel status word " + std::to_string(st));
+    });
+}
+
 int tnr_debug_gemm(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k, const double* A, int64_t lda,
                    int64_t sA, const double* B, int64_t ldb, int64_t sB, double* C, int64_t ldc, int64_t sC, int batch) {
     if (!A || !B || !C || m < 1 || n < 1 || k < 1 || batch < 1) return fail(nullptr, TNR_ERR_INVALID_ARG, "bad gemm");

@@ -327,6 +327,11 @@ TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lam)
 // values over all blocks kept, every singular vector supported on one sector (zero elsewhere).
 // A matrix without such structure is one sector: then it is tsvd itself.
 TsvdOut tsvd_sectors(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt);
+// split precision: the final Rayleigh-Ritz step of tsvd / tsvd_batched for B instances (B = 1
+// for one matrix) from the iteration's basis Uq [B][m x r]; writes U [B][m x k], s [B][k],
+// Vt [B][k x n] and returns the B x k kept values on the host
+std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, int64_t m, int64_t n, int r, int k,
+                                   int B, const double* Uq, double* U, double* s, double* Vt);
 // B stacked m x n matrices (stride m*n), decomposed in lockstep: U [B][m x k], s [B][k], Vt [B][k x n]
 std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U, double* s,
                                   double* Vt);

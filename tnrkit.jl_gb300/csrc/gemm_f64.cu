@@ -66,7 +66,7 @@ k_dgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const d
         __syncthreads();
     }
     if (ksplit > 1) {
-        double* P = part + (int64_t)ks * m * n;
+        double* P = part + ((int64_t)b * ksplit + ks) * m * n;
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -90,16 +90,22 @@ k_dgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const d
         }
 }
 
-// C = alpha * sum_s P[s] + beta * C (fixed summation order: deterministic)
+// C_b = alpha * sum_s P[b][s] + beta * C_b for every batch entry b (fixed summation order:
+// deterministic); P holds ks partial m x n products per batch entry
 __global__ void k_splitk_reduce(const double* __restrict__ P, int ks, int64_t m, int64_t n, double alpha,
-                                double beta, double* C, int64_t ldc) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
+                                double beta, double* C, int64_t ldc, Batch2 bt) {
+    const int64_t mn = m * n, total = mn * bt.n1 * bt.n2;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = e / mn, r = e % mn;
+        const double* Pb = P + b * ks * mn;
         double s = 0.0;
-        for (int i = 0; i < ks; ++i) s += P[e + (int64_t)i * m * n];
-        int64_t gi = e % m, gj = e / m;
+        for (int i = 0; i < ks; ++i) s += Pb[r + (int64_t)i * mn];
+        const int b1 = (int)(b % bt.n1), b2 = (int)(b / bt.n1);
+        double* Cb = C + b1 * bt.sC1 + b2 * bt.sC2;
+        int64_t gi = r % m, gj = r / m;
         double v = alpha * s;
-        if (beta != 0.0) v = fma(beta, C[gi + gj * ldc], v);
-        C[gi + gj * ldc] = v;
+        if (beta != 0.0) v = fma(beta, Cb[gi + gj * ldc], v);
+        Cb[gi + gj * ldc] = v;
     }
 }
 
@@ -112,24 +118,26 @@ void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double 
     TNR_REQUIRE(gn <= 65535, TNR_ERR_UNSUPPORTED, "gemm: n too large for the grid");
     int ksplit = 1;
     int64_t tiles = gm * gn * batch;
-    if (batch == 1 && tiles < sm_count() && k >= 64) {
-        // small outputs (Gram matrices, r x r products): spread K over the SMs
-        ksplit = (int)std::min<int64_t>({k / 32, (2 * sm_count()) / tiles, 64});
+    if (tiles < 2 * sm_count() && k >= 256) {
+        // small outputs (Gram matrices, r x r products, also in lockstep batches): spread K so
+        // that every SM's FP64 pipe gets work (GB300 runs FP64 at ~2 DFMA/clk/SM, so an idle
+        // SM is lost throughput)
+        ksplit = (int)std::min<int64_t>({k / 128, (4 * sm_count() + tiles - 1) / tiles, 64});
         if (ksplit < 2) ksplit = 1;
     }
     int64_t kchunk = ksplit > 1 ? ((k + ksplit - 1) / ksplit + BK - 1) / BK * BK : k;
     if (ksplit > 1) ksplit = (int)((k + kchunk - 1) / kchunk);
     TNR_REQUIRE((int64_t)batch * ksplit <= 65535, TNR_ERR_UNSUPPORTED, "gemm: batch too large");
     Buf part;
-    if (ksplit > 1) part = Buf(c.pool.get(), (size_t)ksplit * m * n * sizeof(double));
+    if (ksplit > 1) part = Buf(c.pool.get(), (size_t)ksplit * batch * m * n * sizeof(double));
     dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)(batch * ksplit));
     int rec = prof_start(c.stream);
     k_dgemm<<<grid, 256, 0, c.stream>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt, ksplit,
                                         kchunk, part.d());
     check_launch("dgemm");
     if (ksplit > 1) {
-        int g = (int)std::min<int64_t>((m * n + 255) / 256, (int64_t)sm_count() * 8);
-        k_splitk_reduce<<<g, 256, 0, c.stream>>>(part.d(), ksplit, m, n, alpha, beta, C, ldc);
+        int g = (int)std::min<int64_t>((m * n * batch + 255) / 256, (int64_t)sm_count() * 8);
+        k_splitk_reduce<<<g, 256, 0, c.stream>>>(part.d(), ksplit, m, n, alpha, beta, C, ldc, bt);
         check_launch("splitk_reduce");
     }
     prof_stop(rec, c.stream, c.bulk_call ? PROF_GEMM_BULK : PROF_GEMM_F64, 2.0 * m * n * k * batch);
@@ -144,7 +152,7 @@ void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double 
 }
 
 #ifndef TNR_SPLIT_MIN_MNK
-#define TNR_SPLIT_MIN_MNK 4194304.0   // m n k of one instance below which a bulk product stays FP64
+#define TNR_SPLIT_MIN_MNK 4194304.0   // m n k summed over the batch below which a bulk product stays FP64
 #endif
 #ifndef TNR_SPLIT_CHUNK_KB
 #define TNR_SPLIT_CHUNK_KB 1          // K blocks of 64 per FP32 accumulation chunk of a contraction
@@ -155,9 +163,12 @@ int split_chunk_kb() { return TNR_SPLIT_CHUNK_KB; }
 void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc, const Batch2& bt,
                bool exact_sum) {
-    // products of small instances stay on the FP64 path: the early coarse-graining steps,
-    // whose norms carry the largest weights in the free energy, are all small
-    if (c.precision == TNR_PREC_SPLIT && (double)m * n * k >= TNR_SPLIT_MIN_MNK &&
+    // a product whose whole batch is too small to fill the tensor cores stays on the FP64 path
+    // (the split kernel's launch and plane pass would cost more than the FP64 GEMM); the
+    // early coarse-graining steps and 2D problems at chi <= 16, whose split products would
+    // move the free energy beyond the contract, run in FP64 through PrecisionScope
+    const double work = (double)m * n * k * bt.n1 * bt.n2;
+    if (c.precision == TNR_PREC_SPLIT && work >= TNR_SPLIT_MIN_MNK &&
         gemm_split_tc(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt, exact_sum ? TNR_SPLIT_CHUNK_KB : 0))
         return;
     c.bulk_call = true;
@@ -168,7 +179,8 @@ void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double
 void split_a_prepare(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int64_t m, int64_t k,
                      int64_t n_hint, const Batch2& bt) {
     P.active = false;
-    if (c.precision != TNR_PREC_SPLIT || (double)m * n_hint * k < TNR_SPLIT_MIN_MNK || n_hint < 16) return;
+    if (c.precision != TNR_PREC_SPLIT || (double)m * n_hint * k * bt.n1 * bt.n2 < TNR_SPLIT_MIN_MNK || n_hint < 16)
+        return;
     split_a_build(c, P, ta, A, lda, m, k, bt);
 }
 

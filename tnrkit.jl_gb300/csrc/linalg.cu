@@ -210,89 +210,141 @@ void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, dou
 }
 
 // Cholesky of (G + shift I) = L L^T in shared memory, then L^{-1} (lower) written over G.
+// Blocked by CB = 32 columns so that the CTA meets about 30 barriers instead of one or two per
+// column:
+//  * per panel: the 32 x 32 diagonal block is factored by one warp (lane l owns row l,
+//    __syncwarp only); the rows below it solve against it (one thread per row, forward
+//    substitution); the trailing lower triangle takes the rank-32 update (one warp per column);
+//  * inverse: each diagonal block is inverted by one warp (lane j owns column j); the blocks
+//    below the diagonal follow by block distance, X_ij = -X_ii (sum_t L_it X_tj), through one
+//    32 x 32 scratch block.
+// Storage in S (column-major, ld = r + 1): L in the lower triangle; X[i,j] (i > j) at the
+// transposed position S[j + i ld] (strict upper triangle, free once L is done); X[j,j] in the
+// spare row S[r + j ld].
+constexpr int CB = 32;
+constexpr int CHOL_THREADS = 256;
+
 template <class T>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(CHOL_THREADS)
 k_chol_inv(double* G, int r, double shift, int* status) {
     G += (int64_t)blockIdx.x * r * r;     // one CTA per matrix of a batch
     extern __shared__ __align__(16) unsigned char smem_c[];
     T* S = reinterpret_cast<T*>(smem_c);
     const int ld = r + 1;
-    const int tid = threadIdx.x, nt = blockDim.x;
+    T* Y = S + (size_t)ld * r;            // CB x CB scratch block, leading dimension CB + 1
+    constexpr int ldy = CB + 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = CHOL_THREADS / 32;
     __shared__ int bad;
     if (tid == 0) bad = 0;
-    for (int e = tid; e < r * r; e += nt) {
+    for (int e = tid; e < r * r; e += CHOL_THREADS) {
         int i = e % r, j = e / r;
         S[i + j * ld] = (T)((i >= j) ? G[e] + (i == j ? shift : 0.0) : 0.0);
     }
     __syncthreads();
-    // right-looking Cholesky, two barriers per column: the square root of the next pivot
-    // is taken by the lane that finishes its update (warp 0, lane 0 owns column k+1's
-    // diagonal) and published in `pivot` for the next iteration
-    const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-    __shared__ T pivot;
-    if (tid == 0) {
-        T d = S[0];
-        if (!(d > T(0)) || !isfinite(d)) { bad = 1; d = (T)1e-30; }
-        pivot = sqrt(d);
-    }
-    __syncthreads();
-    for (int k = 0; k < r; ++k) {
-        const T dk = pivot;
-        for (int i = k + 1 + tid; i < r; i += nt) S[i + k * ld] /= dk;
+    const int nblk = (r + CB - 1) / CB;
+    for (int pb = 0; pb < nblk; ++pb) {
+        const int p = pb * CB, nb = min(CB, r - p);
+        // (1) diagonal block, one warp, right-looking: lane l owns row p + l
+        if (warp == 0) {
+            for (int j = 0; j < nb; ++j) {
+                T d = S[(p + j) + (p + j) * ld];
+                if (!(d > T(0)) || !isfinite(d)) {
+                    if (lane == 0) bad = 1;
+                    d = (T)1e-30;
+                }
+                const T piv = sqrt(d);
+                T x = T(0);
+                if (lane > j && lane < nb) {
+                    x = S[(p + lane) + (p + j) * ld] / piv;
+                    S[(p + lane) + (p + j) * ld] = x;
+                }
+                if (lane == j) S[(p + j) + (p + j) * ld] = piv;
+                __syncwarp();
+                if (lane > j && lane < nb)
+                    for (int jj = j + 1; jj <= lane; ++jj) S[(p + lane) + (p + jj) * ld] -= x * S[(p + jj) + (p + j) * ld];
+                __syncwarp();
+            }
+        }
         __syncthreads();
-        if (tid == 0) S[k + k * ld] = dk;
-        // trailing update of the lower triangle: one warp per column j, lanes over rows i >= j
-        for (int j = k + 1 + warp; j < r; j += nw) {
-            const T sj = S[j + k * ld];
-            for (int i = j + lane; i < r; i += 32) S[i + j * ld] -= S[i + k * ld] * sj;
-            if (j == k + 1 && lane == 0) {
-                T d = S[j + j * ld];
-                if (!(d > T(0)) || !isfinite(d)) { bad = 1; d = (T)1e-30; }
-                pivot = sqrt(d);
+        // (2) rows below the block: L21 = A21 L11^-T, one thread per row
+        for (int i = p + nb + tid; i < r; i += CHOL_THREADS) {
+            for (int j = 0; j < nb; ++j) {
+                T acc = S[i + (p + j) * ld];
+                for (int t = 0; t < j; ++t) acc -= S[i + (p + t) * ld] * S[(p + j) + (p + t) * ld];
+                S[i + (p + j) * ld] = acc / S[(p + j) + (p + j) * ld];
+            }
+        }
+        __syncthreads();
+        // (3) trailing lower triangle: A22 -= L21 L21^T, one warp per column
+        for (int j = p + nb + warp; j < r; j += NW) {
+            for (int i = j + lane; i < r; i += 32) {
+                T acc = T(0);
+                for (int t = 0; t < nb; ++t) acc += S[i + (p + t) * ld] * S[j + (p + t) * ld];
+                S[i + j * ld] -= acc;
             }
         }
         __syncthreads();
     }
-    // inverse X = L^{-1} of the lower-triangular L, row by row: row i needs only the rows
-    // above it, so thread j < i computes X[i,j] = -(sum_{kk=j}^{i-1} L[i,kk] X[kk,j]) / L[i,i].  X shares S's storage: X[i,j], i > j, sits at the transposed
-    // position S[j + i*ld] (strict upper triangle, free once L is done) and X[j,j] = 1/L[j,j]
-    // in the spare row S[r + j*ld]; L stays in the lower triangle.
-    for (int i = tid; i < r; i += nt) S[r + i * ld] = T(1) / S[i + i * ld];
-    __syncthreads();
-    for (int i = 1; i < r; ++i) {
-        for (int j = tid; j < i; j += nt) {
-            // four partial sums: eight independent shared-memory loads per trip
-            T a0 = S[i + j * ld] * S[r + j * ld], a1 = T(0), a2 = T(0), a3 = T(0);
-            int kk = j + 1;
-            for (; kk + 3 < i; kk += 4) {
-                a0 += S[i + kk * ld] * S[j + kk * ld];
-                a1 += S[i + (kk + 1) * ld] * S[j + (kk + 1) * ld];
-                a2 += S[i + (kk + 2) * ld] * S[j + (kk + 2) * ld];
-                a3 += S[i + (kk + 3) * ld] * S[j + (kk + 3) * ld];
+    // (4) diagonal blocks of X = L^-1, one warp per block, lane j owns column j of the block
+    for (int pb = warp; pb < nblk; pb += NW) {
+        const int p = pb * CB, nb = min(CB, r - p);
+        if (lane < nb) {
+            const int j = lane;
+            S[r + (p + j) * ld] = T(1) / S[(p + j) + (p + j) * ld];
+            for (int i = j + 1; i < nb; ++i) {
+                T acc = S[(p + i) + (p + j) * ld] * S[r + (p + j) * ld];
+                for (int t = j + 1; t < i; ++t) acc += S[(p + i) + (p + t) * ld] * S[(p + j) + (p + t) * ld];
+                S[(p + j) + (p + i) * ld] = -acc / S[(p + i) + (p + i) * ld];
             }
-            for (; kk < i; ++kk) a0 += S[i + kk * ld] * S[j + kk * ld];
-            S[j + i * ld] = -((a0 + a1) + (a2 + a3)) * S[r + i * ld];
         }
-        __syncthreads();
     }
     __syncthreads();
-    for (int e = tid; e < r * r; e += nt) {
+    // (5) blocks below the diagonal, by block distance: X_ij = -X_ii Y, Y = sum_{t=j}^{i-1} L_it X_tj
+    for (int dist = 1; dist < nblk; ++dist) {
+        for (int bj = 0; bj + dist < nblk; ++bj) {
+            const int bi = bj + dist;
+            const int pi = bi * CB, ni = min(CB, r - pi), pj = bj * CB, nj = min(CB, r - pj);
+            for (int e = tid; e < ni * nj; e += CHOL_THREADS) {
+                const int ii = e % ni, jj = e / ni;
+                const int i = pi + ii, j = pj + jj;
+                // t = j: X[j,j] on the spare row; t in (j, pi): X[t,j] at S[j + t ld]
+                T acc = S[i + j * ld] * S[r + j * ld];
+                for (int t = j + 1; t < pi; ++t) acc += S[i + t * ld] * S[j + t * ld];
+                Y[ii + jj * ldy] = acc;
+            }
+            __syncthreads();
+            for (int e = tid; e < ni * nj; e += CHOL_THREADS) {
+                const int ii = e % ni, jj = e / ni;
+                const int i = pi + ii, j = pj + jj;
+                // (X_ii Y)[ii, jj] = X[i,i] Y[ii,jj] + sum_{s < ii} X[i, pi + s] Y[s, jj]
+                T acc = S[r + i * ld] * Y[ii + jj * ldy];
+                for (int s2 = 0; s2 < ii; ++s2) acc += S[(pi + s2) + i * ld] * Y[s2 + jj * ldy];
+                S[j + i * ld] = -acc;
+            }
+            __syncthreads();
+        }
+    }
+    for (int e = tid; e < r * r; e += CHOL_THREADS) {
         int i = e % r, j = e / r;
         G[e] = i > j ? (double)S[j + i * ld] : (i == j ? (double)S[r + j * ld] : 0.0);
     }
     if (tid == 0 && bad) atomicOr(status, ST_CHOL_BREAKDOWN);
 }
 
+// shared memory of k_chol_inv: the r x r matrix (ld r + 1) and the CB x CB scratch block
+template <class T>
+static size_t chol_smem(int r) { return ((size_t)(r + 1) * r + (size_t)CB * (CB + 1)) * sizeof(T); }
+
 template <class T>
 static void launch_chol(Ctx& c, double* G, int r, double shift, int batch) {
     TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "chol_inv: r out of range");
-    size_t smem = (size_t)(r + 1) * r * sizeof(T);
+    const size_t smem = chol_smem<T>(r);
     TNR_REQUIRE(smem <= 227 * 1024, TNR_ERR_UNSUPPORTED, "chol_inv: matrix too large for shared memory");
     static std::atomic<uint64_t> attr_set{0};
-    ensure_smem_attr(attr_set, (const void*)k_chol_inv<T>,
-                     (int)std::min<size_t>((size_t)(JMAX + 1) * JMAX * sizeof(T), 227 * 1024));
+    ensure_smem_attr(attr_set, (const void*)k_chol_inv<T>, (int)std::min<size_t>(chol_smem<T>(JMAX), 227 * 1024));
     int rec = prof_start(c.stream);
-    k_chol_inv<T><<<batch, 512, smem, c.stream>>>(G, r, shift, c.d_status);
+    k_chol_inv<T><<<batch, CHOL_THREADS, smem, c.stream>>>(G, r, shift, c.d_status);
     check_launch("chol_inv");
     prof_stop(rec, c.stream, PROF_CHOL, (double)r * r * r * batch);
 }

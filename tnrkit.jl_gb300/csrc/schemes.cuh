@@ -26,6 +26,10 @@ enum { FINALIZER_DEFAULT = 0, FINALIZER_TWO_BY_TWO = 1 };
 #ifndef TNR_SPLIT_FP64_STEPS_3D
 #define TNR_SPLIT_FP64_STEPS_3D 1
 #endif
+// 2D steps at chi at or below this run in FP64 in a split-precision solve (split_step_in_fp64)
+#ifndef TNR_SPLIT_MIN_CHI
+#define TNR_SPLIT_MIN_CHI 16
+#endif
 int split_fp64_steps(int kind);
 bool split_step_in_fp64(int kind, int64_t step, const int64_t* dims, int nlegs, int chi);
 

@@ -278,6 +278,18 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
     out.iters = it;
     c.last_iters = it;
     if (debug_on()) fprintf(stderr, "[tnr] tsvd m=%lld n=%lld k=%d r=%d iters=%d\n", (long long)m, (long long)n, k, r, it);
+    if (c.precision == TNR_PREC_SPLIT) {
+        // the split path's final step with its polar factor folded into the r x r problems
+        std::vector<double> kept = final_rr_split(c, PMt, M, m, n, r, k, 1, Uq.d(), U, s, Vt);
+        sum_squares(c, M, m * n, c.d_scalar);
+        std::vector<double> f = to_host(c, c.d_scalar, 1);
+        out.fro2 = f[0];
+        double kept2 = 0;
+        for (double v : kept) kept2 += v * v;
+        out.err = std::sqrt(std::max(out.fro2 - kept2, 0.0));
+        out.vals = kept;
+        return out;
+    }
     // final Rayleigh-Ritz in FP64: M ~ U (U^T M) = U B, B^T = M^T U
     polar(c, Uq.d(), m, r);
     Buf Ub(c.pool.get(), (size_t)n * r * sizeof(double));

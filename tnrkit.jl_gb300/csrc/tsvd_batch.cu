@@ -118,6 +118,59 @@ void copy_lead(Ctx& c, const double* in, int p, int k, int B, double* out) {
 
 }  // namespace
 
+// Split precision: the final Rayleigh-Ritz step of B lockstep instances.  Uq [B][m x r] is
+// orthonormal to FP32 level (CholeskyQR3 with FP32 Cholesky factors); its polar factor
+// Q' = Uq P, P = I - E/2 + 3E^2/8, E = Uq^T Uq - I, is never formed: P is folded into the
+// r x r problems.  With Z = M^T Uq (the projection, on the tensor cores with chunked
+// accumulation), Z' = M^T Q' = Z P and Z'^T Z' = P^T (Z^T Z) P = Vb S^2 Vb^T, so
+// U = Uq (P Vb_k), S_k = the column norms of Z (P Vb_k) and Vt = (Z P Vb_k / S_k)^T.
+// The eigenvectors of the r x r Gram come from an FP32 Jacobi alignment (polar-corrected
+// in FP64) and an FP64 Jacobi cleanup.  FP64 GEMM work: two Grams over the long dimension
+// and two rank-k products, against the plain path's polar step and one-sided final SVD
+// (four long-dimension products more).  A Gram of Z loses relative accuracy of singular
+// values below ~1e-8 of the largest (FP64 rounding of the squares), which is the noise floor
+// of the split products anyway.  Returns the B x k kept values (host).
+std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, int64_t m, int64_t n, int r, int k,
+                                   int B, const double* Uq, double* U, double* s, double* Vt) {
+    const int64_t mn = m * n, mr = m * r, nr = n * r, rr = (int64_t)r * r, rk = (int64_t)r * k;
+    Buf P(c.pool.get(), (size_t)B * rr * sizeof(double));
+    Buf E(c.pool.get(), (size_t)B * rr * sizeof(double));
+    Buf E2(c.pool.get(), (size_t)B * rr * sizeof(double));
+    gemm_f64(c, true, false, r, r, m, 1.0, Uq, m, Uq, m, 0.0, E.d(), r, strided(B, mr, mr, rr));
+    add_identity(c, E.d(), r, -1.0, B);
+    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, E.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
+    polar_coeff(c, E.d(), E2.d(), P.d(), r, B);
+    // the projection Z = M^T Uq (n x r)
+    Buf Z(c.pool.get(), (size_t)B * nr * sizeof(double));
+    gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq, m, 0.0, Z.d(), n, strided(B, mn, mr, nr), true);
+    // Gp = P^T (Z^T Z) P
+    Buf G(c.pool.get(), (size_t)B * rr * sizeof(double));
+    gemm_f64(c, true, false, r, r, n, 1.0, Z.d(), n, Z.d(), n, 0.0, G.d(), r, strided(B, nr, nr, rr));
+    gemm_f64(c, false, false, r, r, r, 1.0, G.d(), r, P.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));
+    gemm_f64(c, true, false, r, r, r, 1.0, P.d(), r, E.d(), r, 0.0, G.d(), r, strided(B, rr, rr, rr));
+    // eigenvectors Vb of Gp: FP32 alignment W1 (made orthogonal in FP64), FP64 cleanup W2
+    Buf W1(c.pool.get(), (size_t)B * rr * sizeof(double));
+    Buf lam(c.pool.get(), (size_t)B * r * sizeof(double));
+    jacobi_eigh_f32(c, G.d(), r, r, W1.d(), lam.d(), B, rr);
+    polar_b(c, W1.d(), r, r, B);
+    gemm_f64(c, false, false, r, r, r, 1.0, G.d(), r, W1.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));
+    gemm_f64(c, true, false, r, r, r, 1.0, W1.d(), r, E.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
+    jacobi_eigh(c, E2.d(), r, r, G.d(), lam.d(), B, rr);                  // W2 into G
+    gemm_f64(c, false, false, r, r, r, 1.0, W1.d(), r, G.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));   // Vb
+    // PV = P Vb_k (r x k)
+    Buf PV(c.pool.get(), (size_t)B * rk * sizeof(double));
+    gemm_f64(c, false, false, r, k, r, 1.0, P.d(), r, E.d(), r, 0.0, PV.d(), r, strided(B, rr, rr, rk));
+    // U = Uq PV; Ub = Z PV = Vt^T S
+    gemm_f64(c, false, false, m, k, r, 1.0, Uq, m, PV.d(), r, 0.0, U, m, strided(B, mr, rk, m * k));
+    Buf Ub(c.pool.get(), (size_t)B * n * k * sizeof(double));
+    gemm_f64(c, false, false, n, k, r, 1.0, Z.d(), n, PV.d(), r, 0.0, Ub.d(), n, strided(B, nr, rk, n * k));
+    col_norms(c, Ub.d(), n, (int64_t)k * B, n, s);
+    col_scale(c, Ub.d(), n, (int64_t)k * B, n, s, 2);
+    transpose_lead(c, Ub.d(), n, k, k, B, Vt);
+    check_status(c, "final Rayleigh-Ritz (split)");
+    return to_host(c, s, (int64_t)B * k);
+}
+
 // M: B stacked m x n matrices (ld m, stride m*n).  U [B][m x k], s [B][k], Vt [B][k x n].
 std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U, double* s,
                                   double* Vt) {
@@ -188,6 +241,11 @@ std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n,
         }
     }
     for (auto& o : outs) o.iters = it;
+    if (c.precision == TNR_PREC_SPLIT) {
+        std::vector<double> kept = final_rr_split(c, PMt, M, m, n, r, k, B, Uq.d(), U, s, Vt);
+        for (int b = 0; b < B; ++b) outs[b].vals.assign(kept.begin() + (size_t)b * k, kept.begin() + (size_t)(b + 1) * k);
+        return outs;
+    }
     polar_b(c, Uq.d(), m, r, B);
     Buf Ub(c.pool.get(), (size_t)B * nr * sizeof(double));
     Buf Vb(c.pool.get(), (size_t)B * rr * sizeof(double));
