@@ -213,6 +213,14 @@ typedef struct tnr_server_s* tnr_server;
 int tnr_server_create(tnr_server* out, size_t hbm_budget_bytes, int max_active, int precision);
 int tnr_server_submit(tnr_server s, int kind, int nlegs, const int64_t* dims, const double* data,
                       int chi, int maxiter, double btrg_k, uint64_t* id_out);
+/* The same for a Z_N-symmetric tensor (TRG, BTRG, HOTRG): symmetry_n and leg_charges as in
+ * tnr_options (sum(dims) ints, codomain legs 1-2 +charge, domain legs -charge).  The request
+ * then runs block by block over the charge sectors (contractions as one GEMM per sector,
+ * decompositions per sector with the global truncrank cut), as TensorKit's block-sparse
+ * tensors do in the reference's run!(). */
+int tnr_server_submit_sym(tnr_server s, int kind, int nlegs, const int64_t* dims, const double* data,
+                          int symmetry_n, const int32_t* leg_charges, int chi, int maxiter, double btrg_k,
+                          uint64_t* id_out);
 /* wait != 0 blocks until request `id` finishes.  Returns the request's status;
  * latency_ms = submission to completion, queue_ms = submission to admission. */
 int tnr_server_poll(tnr_server s, uint64_t id, int wait, int* done, double* norms, size_t cap,

@@ -93,6 +93,24 @@ def test_zn_models_trg(tnr, oracle, model, chi):
     np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
 
 
+# tie-free cuts over these 6 steps (the smallest relative gap at the cut is 0.3 for potts3 at
+# chi = 16 and 0.08 for clock6 at chi = 13)
+@pytest.mark.parametrize("model,chi", [("potts3", 16), ("clock6", 13)])
+def test_zn_models_hotrg_blocks(tnr, oracle, model, chi):
+    """HOTRG on Z_N tensors runs block by block over the charge sectors (blocked contractions,
+    per-sector eigh with the global truncrank cut) and matches the oracle's block-sparse path:
+    every norm to 1e-10 and every kept Gram eigenvalue to 1e-10 of the largest."""
+    o = oracle
+    if model == "potts3":
+        T, To = tnr.classical_potts(3), o.classical_potts(3)
+    else:
+        T, To = tnr.classical_clock(6, 0.7), o.classical_clock(6, 0.7)
+    s, so, d, do = _pair(tnr, o, "HOTRG", T, To, chi, 6)
+    np.testing.assert_allclose(d, do, rtol=NORM_RTOL)
+    _check_svals(s, so, 2)
+    assert s.T.shape == so.T.a.shape      # the bond dimensions the sectors hold, as in the oracle
+
+
 def test_cut_through_degenerate_pair(tnr, oracle):
     """Clock Z6 spectra come in exactly degenerate pairs (charge sectors c and -c); truncrank(12)
     cuts one, so the kept subspace depends on tie-breaking (the reference's order is not

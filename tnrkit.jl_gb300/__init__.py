@@ -42,7 +42,8 @@ EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step",
            "tnr_device_bytes", "tnr_destroy", "tnr_last_error", "tnr_status_string", "tnr_timer_start",
            "tnr_timer_stop", "tnr_run_batch", "tnr_device_info", "tnr_version", "tnr_kernel_launches",
            "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm", "tnr_gemm_time",
-           "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_poll",
+           "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_submit_sym",
+           "tnr_server_poll", "tnr_debug_chol",
            "tnr_server_stats", "tnr_server_destroy", "tnr_footprint_bytes", "tnr_create_impurity_hotrg",
            "tnr_create_impurity_trg", "tnr_finalize_impurity", "tnr_run_impurity", "tnr_create_correlation_hotrg",
            "tnr_run_correlation", "tnr_correlation_ratio", "tnr_set_finalizer", "tnr_transfer_eigvals",
@@ -117,6 +118,7 @@ def lib():
                                        C.c_int64, P, C.c_char_p, Z]),
         "tnr_server_create": (I, [C.POINTER(P), Z, I, I]),
         "tnr_server_submit": (I, [P, I, I, pi64, pd, I, I, D, C.POINTER(C.c_uint64)]),
+        "tnr_server_submit_sym": (I, [P, I, I, pi64, pd, I, C.POINTER(C.c_int32), I, I, D, C.POINTER(C.c_uint64)]),
         "tnr_server_poll": (I, [P, C.c_uint64, I, C.POINTER(I), pd, Z, pz, pd, pd]),
         "tnr_server_stats": (I, [P, C.POINTER(I), C.POINTER(I), pz]),
         "tnr_server_destroy": (I, [P]),
@@ -669,12 +671,21 @@ class Server:
         self.maxiter = {}
 
     def submit(self, T, scheme, chi, maxiter, k=-0.5):
-        a = np.asfortranarray(_as_sym(T).array, dtype=np.float64)
+        """Queue a run!(scheme(T), truncrank(chi), maxiter(maxiter)) request; a Z_N tensor (its
+        charges given) runs block by block over its charge sectors."""
+        T = _as_sym(T)
+        a = np.asfortranarray(T.array, dtype=np.float64)
         kind = self.KINDS[scheme if isinstance(scheme, str) else scheme.__name__]
         dims = (C.c_int64 * a.ndim)(*a.shape)
         rid = C.c_uint64()
-        st = lib().tnr_server_submit(self._h, kind, a.ndim, dims, a.ctypes.data_as(C.POINTER(C.c_double)), int(chi),
-                                     int(maxiter), float(k), C.byref(rid))
+        if T.charges is not None and T.N > 1:
+            q = np.ascontiguousarray(np.concatenate([np.asarray(c, dtype=np.int32) for c in T.charges]))
+            st = lib().tnr_server_submit_sym(self._h, kind, a.ndim, dims, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                             int(T.N), q.ctypes.data_as(C.POINTER(C.c_int32)), int(chi),
+                                             int(maxiter), float(k), C.byref(rid))
+        else:
+            st = lib().tnr_server_submit(self._h, kind, a.ndim, dims, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                         int(chi), int(maxiter), float(k), C.byref(rid))
         _check(st)
         self.maxiter[rid.value] = maxiter
         return rid.value

@@ -109,6 +109,24 @@ int create_common(tnr_handle* out, int kind, int nlegs, const int64_t* dims, con
         s.ctx.reset(new Ctx((cudaStream_t)o.stream, o.precision, o.seed));
         std::vector<int64_t> dv(dims, dims + nlegs);
         s.T = make_dt(s.ctx->pool.get(), dv);
+        if (o.symmetry_n > 1 && o.leg_charges &&
+            (kind == TNR_TRG || kind == TNR_BTRG || kind == TNR_HOTRG || (kind == TNR_HOTRG_3D && o.symmetry_n == 2))) {
+            // Z_N tensors run block by block over the charge sectors: signed charges, +q on
+            // the two codomain legs and -q on the domain legs (HOTRG_3D: Z2, whose charges are
+            // self-dual, as its network's adjoint legs assume)
+            const int N = o.symmetry_n;
+            s.T.N = N;
+            int64_t off = 0;
+            for (int l = 0; l < nlegs; ++l) {
+                std::vector<int> q((size_t)dims[l]);
+                for (int64_t i = 0; i < dims[l]; ++i) {
+                    const int ch = o.leg_charges[off + i];
+                    q[i] = (((l < 2 ? ch : -ch) % N) + N) % N;
+                }
+                off += dims[l];
+                s.T.q.push_back(q);
+            }
+        }
         TNR_CUDA(cudaMemcpyAsync(s.T.p(), data, s.T.size() * sizeof(double),
                                  device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s.ctx->stream));
         if (kind == TNR_BTRG) {
@@ -500,7 +518,7 @@ int tnr_run_batch(tnr_handle* hs, int n, const int* chi, const int* maxiter, int
         for (int i = 0; i < n; ++i) {
             Scheme& sc = hs[i]->s;
             bool groupable = (sc.kind == TNR_TRG || sc.kind == TNR_BTRG) && sc.steps == 0 &&
-                             sc.finalizer == FINALIZER_DEFAULT;
+                             sc.finalizer == FINALIZER_DEFAULT && !sc.T.charged();
             std::string key;
             if (groupable) {
                 uint64_t kbits = 0;                                   // k exactly, not to 6 decimals

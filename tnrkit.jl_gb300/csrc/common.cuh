@@ -158,6 +158,13 @@ struct DT {
     Buf buf;
     int rank = 0;
     int64_t d[MAXR] = {0};
+    // Z_N charges (N > 1): q[l][i] is the signed charge that basis index i of leg l contributes
+    // to the conservation law sum_l q[l][i_l] = 0 (mod N) obeyed by every nonzero entry
+    // (codomain legs carry +charge, domain legs -charge).  The data stay the dense embedding;
+    // contractions and decompositions of charged tensors run block by block over the sectors.
+    int N = 1;
+    std::vector<std::vector<int>> q;
+    bool charged() const { return N > 1 && (int)q.size() == rank; }
     double* p() const { return buf.d(); }
     int64_t size() const {
         int64_t s = 1;
@@ -332,6 +339,22 @@ TsvdOut tsvd_sectors(Ctx& c, const double* M, int64_t m, int64_t n, int k, doubl
 // Vt [B][k x n] and returns the B x k kept values on the host
 std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, int64_t m, int64_t n, int r, int k,
                                    int B, const double* Uq, double* U, double* s, double* Vt);
+// Truncated SVD / eigh of a tensor's (row legs <- column legs) matrix, nrow row legs.  An
+// uncharged tensor goes through tsvd / teigh.  A charged one decomposes sector by sector
+// (rows of class c = sum of row-leg charges, columns whose charges sum to -c), keeps the chi
+// largest values over all sectors (ties: lower sector, then lower index, first; descending
+// order), and gives the new leg the charge -c on the U side and +c on the Vt side
+// (MatrixAlgebraKit's svd_trunc / eigh_trunc! with truncrank on TensorKit's block layout).
+// The kept count can be below min(chi, m, n) when the sectors hold fewer values.
+struct DecompDT {
+    DT U;       // row legs + new leg
+    DT Vt;      // new leg + column legs (SVD only)
+    Buf s;      // kept values (|eigenvalue| order for eigh), k doubles
+    int k = 0;
+    TsvdOut info;
+};
+DecompDT svd_dt(Ctx& c, const DT& M, int nrow, int chi);
+DecompDT eigh_dt(Ctx& c, const DT& MM, int nrow, int chi);
 // B stacked m x n matrices (stride m*n), decomposed in lockstep: U [B][m x k], s [B][k], Vt [B][k x n]
 std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U, double* s,
                                   double* Vt);
@@ -345,8 +368,17 @@ std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n,
 DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::vector<int>& lA,
             const double* B, const std::vector<int64_t>& dB, const std::vector<int>& lB,
             const std::vector<int>& lOut, bool bulk = true, int batch = 1);
+// A pairwise contraction of two charged tensors (the same Z_N), one GEMM per charge sector:
+// the rows (free legs of A) of class c meet the contracted index combinations of class -c and
+// the columns (free legs of B) of class -c.  Each sector block is gathered from the dense
+// embedding, multiplied (tensor cores in split precision) and scattered into the zeroed
+// result, which carries the free legs' charges.  The work is sum_c m_c k_c n_c instead of
+// m k n: about N^2 times less for balanced sectors.
+DT contract_blocked(Ctx& c, const DT& A, const std::vector<int>& lA, const DT& B, const std::vector<int>& lB,
+                    const std::vector<int>& lOut, bool bulk);
 inline DT contract(Ctx& c, const DT& A, const std::vector<int>& lA, const DT& B,
                    const std::vector<int>& lB, const std::vector<int>& lOut, bool bulk = true) {
+    if (A.charged() && B.charged()) return contract_blocked(c, A, lA, B, lB, lOut, bulk);
     return contract(c, A.p(), A.dims(), lA, B.p(), B.dims(), lB, lOut, bulk);
 }
 DT permuted(Ctx& c, const DT& A, const std::vector<int>& perm);

@@ -342,6 +342,10 @@ DT permuted(Ctx& c, const DT& A, const std::vector<int>& perm) {
     for (int k = 0; k < A.rank; ++k) od[k] = A.d[perm[k]];
     DT o = make_dt(c.pool.get(), od);
     permute(c, A.p(), A.d, A.rank, perm.data(), o.p());
+    if (A.charged()) {
+        o.N = A.N;
+        for (int k = 0; k < A.rank; ++k) o.q.push_back(A.q[perm[k]]);
+    }
     return o;
 }
 

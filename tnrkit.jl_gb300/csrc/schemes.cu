@@ -42,6 +42,16 @@ void Scheme::record(const TsvdOut& r) {
 static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B, bool sectors = false) {
     Ctx& c = *s.ctx;
     int64_t m = M4.d[0] * M4.d[1], n = M4.d[2] * M4.d[3];
+    if (M4.charged()) {
+        // block by block over the charge sectors; A and B carry the new leg's charges
+        DecompDT d = svd_dt(c, M4, 2, chi);
+        A = std::move(d.U);
+        B = std::move(d.Vt);
+        col_scale(c, A.p(), m, d.k, m, d.s.d(), 1);
+        row_scale(c, B.p(), d.k, n, d.k, d.s.d(), 1);
+        s.record(d.info);
+        return;
+    }
     int k = (int)std::min<int64_t>(chi, std::min(m, n));
     A = make_dt(c.pool.get(), {M4.d[0], M4.d[1], (int64_t)k});
     B = make_dt(c.pool.get(), {(int64_t)k, M4.d[2], M4.d[3]});
@@ -297,6 +307,40 @@ static void step_impurity_trg(Scheme& s, int chi) {
     s.site[3] = std::move(N4);
 }
 
+// step!(::BTRG) on a charged tensor: the two SVDs block by block over the charge sectors (the
+// kept counts can be below chi), the 8-tensor network as blocked pairwise contractions
+static void step_btrg_charged(Scheme& s, int chi) {
+    Ctx& c = *s.ctx;
+    DT& T = s.T;
+    const double kexp = s.btrg_k;
+    auto half = [&](const DT& M, DT& U, DT& V, DT& Sn) {
+        DecompDT d = svd_dt(c, M, 2, chi);
+        const int64_t m = M.d[0] * M.d[1], n = M.d[2] * M.d[3];
+        Buf sa(c.pool.get(), (size_t)d.k * sizeof(double));
+        Sn = make_dt(c.pool.get(), {(int64_t)d.k});
+        pseudopow(c, d.s.d(), d.k, (1.0 - kexp) / 2.0, sa.d());
+        pseudopow(c, d.s.d(), d.k, kexp, Sn.p());
+        U = std::move(d.U);
+        V = std::move(d.Vt);
+        col_scale(c, U.p(), m, d.k, m, sa.d(), 0);
+        row_scale(c, V.p(), d.k, n, d.k, sa.d(), 0);
+        s.record(d.info);
+    };
+    DT A, B, C, D, S1n, S2n;
+    half(T, A, B, S1n);
+    half(permuted(c, T, {2, 0, 3, 1}), C, D, S2n);
+    scale_leg(c, D, 2, s.S1.p());
+    scale_leg(c, D, 1, s.S2.p());
+    scale_leg(c, B, 2, s.S2.p());
+    scale_leg(c, C, 0, s.S1.p());
+    DT X = contract(c, D, {La, Lx, Lp}, B, {Lb, Lp, Ly}, {La, Lb, Lx, Ly});
+    DT Y = contract(c, C, {Lz, Ly, Ld}, A, {Lx, Lz, Lc}, {Lx, Ly, Lc, Ld});
+    A = DT(); B = DT(); C = DT(); D = DT();
+    s.T = contract(c, X, {La, Lb, Lx, Ly}, Y, {Lx, Ly, Lc, Ld}, {La, Lb, Lc, Ld});
+    s.S1 = std::move(S1n);
+    s.S2 = std::move(S2n);
+}
+
 // step!(::BTRG) (src/schemes/btrg.jl:60-94)
 static void step_btrg(Scheme& s, int chi) {
     Ctx& c = *s.ctx;
@@ -304,6 +348,10 @@ static void step_btrg(Scheme& s, int chi) {
     TNR_REQUIRE(T.d[0] == T.d[3] && T.d[1] == T.d[2], TNR_ERR_INVALID_ARG, "BTRG needs d1 == d4 and d2 == d3");
     const double kexp = s.btrg_k;
     const int64_t d1 = T.d[0], d2 = T.d[1], d3 = T.d[2], d4 = T.d[3];
+    if (T.charged()) {
+        step_btrg_charged(s, chi);
+        return;
+    }
     // first SVD: T as (d1 d2) x (d3 d4)
     int64_t m = d1 * d2, n = d3 * d4;
     int k1 = (int)std::min<int64_t>(chi, std::min(m, n));
@@ -353,6 +401,11 @@ static void step_btrg(Scheme& s, int chi) {
 // eigh_trunc!(project_hermitian!(MM)) of a (rows x rows) Gram tensor -> U[r1, r2, k]
 static DT eig_proj(Scheme& s, const DT& MM, int chi, TsvdOut& out) {
     Ctx& c = *s.ctx;
+    if (MM.charged()) {
+        DecompDT d = eigh_dt(c, MM, 2, chi);
+        out = d.info;
+        return std::move(d.U);
+    }
     int64_t n = MM.d[0] * MM.d[1];
     int k = (int)std::min<int64_t>(chi, n);
     DT U = make_dt(c.pool.get(), {MM.d[0], MM.d[1], (int64_t)k});
@@ -373,22 +426,40 @@ static DT choose_proj(Scheme& s, DT&& U, TsvdOut& r, DT&& U2, TsvdOut& r2) {
     return std::move(U);
 }
 
+// A copy of U with every charge negated: for real data the adjoint U' of TensorKit's network
+// has the same entries and dual legs.
+static DT dual_copy(Ctx& c, const DT& U) {
+    DT o = make_dt(c.pool.get(), U.dims());
+    copy_f64(c, o.p(), U.p(), U.size());
+    o.N = U.N;
+    for (const auto& q : U.q) {
+        std::vector<int> nq(q.size());
+        for (size_t i = 0; i < q.size(); ++i) nq[i] = (U.N - q[i] % U.N) % U.N;
+        o.q.push_back(nq);
+    }
+    return o;
+}
+
 // _get_hotrg_xproj (src/schemes/hotrg.jl:82-116) with A1 = A2 = T
 static DT hotrg_xproj(Scheme& s, const DT& T, int chi) {
     Ctx& c = *s.ctx;
     TsvdOut r1, r2;
     DT U1, U2;
+    // conj(A): the same entries; a charged tensor's conjugate carries the dual charges
+    DT Tdual;
+    if (T.charged()) Tdual = dual_copy(c, T);
+    const DT& Tc = T.charged() ? Tdual : T;
     {
         // MM[-1 -2;-3 -4] = A2[-1 5;1 2] A1[-2 3;5 4] conj(A2[-3 6;1 2]) conj(A1[-4 3;6 4])
-        DT X = contract(c, T, {La, Le, Li, Lj}, T, {Lc, Lf, Li, Lj}, {La, Le, Lc, Lf}, false);
-        DT Y = contract(c, T, {Lb, Lk, Le, Ll}, T, {Ld, Lk, Lf, Ll}, {Lb, Le, Ld, Lf}, false);
+        DT X = contract(c, T, {La, Le, Li, Lj}, Tc, {Lc, Lf, Li, Lj}, {La, Le, Lc, Lf}, false);
+        DT Y = contract(c, T, {Lb, Lk, Le, Ll}, Tc, {Ld, Lk, Lf, Ll}, {Lb, Le, Ld, Lf}, false);
         DT MM = contract(c, X, {La, Le, Lc, Lf}, Y, {Lb, Le, Ld, Lf}, {La, Lb, Lc, Ld}, false);
         U1 = eig_proj(s, MM, chi, r1);
     }
     {
         // MM = conj(A2[2 5;1 -1]) conj(A1[4 3;5 -2]) A2[2 6;1 -3] A1[4 3;6 -4]
-        DT X = contract(c, T, {Lj, Le, Li, La}, T, {Lj, Lf, Li, Lc}, {Le, La, Lf, Lc}, false);
-        DT Y = contract(c, T, {Ll, Lk, Le, Lb}, T, {Ll, Lk, Lf, Ld}, {Le, Lb, Lf, Ld}, false);
+        DT X = contract(c, Tc, {Lj, Le, Li, La}, T, {Lj, Lf, Li, Lc}, {Le, La, Lf, Lc}, false);
+        DT Y = contract(c, Tc, {Ll, Lk, Le, Lb}, T, {Ll, Lk, Lf, Ld}, {Le, Lb, Lf, Ld}, false);
         DT MM = contract(c, X, {Le, La, Lf, Lc}, Y, {Le, Lb, Lf, Ld}, {La, Lb, Lc, Ld}, false);
         U2 = eig_proj(s, MM, chi, r2);
     }
@@ -400,21 +471,46 @@ static DT hotrg_yproj(Scheme& s, const DT& T, int chi) {
     Ctx& c = *s.ctx;
     TsvdOut r1, r2;
     DT U1, U2;
+    DT Tdual;
+    if (T.charged()) Tdual = dual_copy(c, T);
+    const DT& Tc = T.charged() ? Tdual : T;
     {
         // MM = A1[1 -1;2 5] A2[5 -2;4 3] conj(A1[1 -3;2 6]) conj(A2[6 -4;4 3])
-        DT X = contract(c, T, {Li, La, Lj, Lp}, T, {Li, Lc, Lj, Lr}, {La, Lp, Lc, Lr}, false);
-        DT Y = contract(c, T, {Lp, Lb, Ll, Lk}, T, {Lr, Ld, Ll, Lk}, {Lp, Lb, Lr, Ld}, false);
+        DT X = contract(c, T, {Li, La, Lj, Lp}, Tc, {Li, Lc, Lj, Lr}, {La, Lp, Lc, Lr}, false);
+        DT Y = contract(c, T, {Lp, Lb, Ll, Lk}, Tc, {Lr, Ld, Ll, Lk}, {Lp, Lb, Lr, Ld}, false);
         DT MM = contract(c, X, {La, Lp, Lc, Lr}, Y, {Lp, Lb, Lr, Ld}, {La, Lb, Lc, Ld}, false);
         U1 = eig_proj(s, MM, chi, r1);
     }
     {
         // MM = conj(A1[1 2;-1 5]) conj(A2[5 4;-2 3]) A1[1 2;-3 6] A2[6 4;-4 3]
-        DT X = contract(c, T, {Li, Lj, La, Lp}, T, {Li, Lj, Lc, Lr}, {La, Lp, Lc, Lr}, false);
-        DT Y = contract(c, T, {Lp, Ll, Lb, Lk}, T, {Lr, Ll, Ld, Lk}, {Lp, Lb, Lr, Ld}, false);
+        DT X = contract(c, Tc, {Li, Lj, La, Lp}, T, {Li, Lj, Lc, Lr}, {La, Lp, Lc, Lr}, false);
+        DT Y = contract(c, Tc, {Lp, Ll, Lb, Lk}, T, {Lr, Ll, Ld, Lk}, {Lp, Lb, Lr, Ld}, false);
         DT MM = contract(c, X, {La, Lp, Lc, Lr}, Y, {Lp, Lb, Lr, Ld}, {La, Lb, Lc, Ld}, false);
         U2 = eig_proj(s, MM, chi, r2);
     }
     return choose_proj(s, std::move(U1), r1, std::move(U2), r2);
+}
+
+// The HOTRG half steps on charged tensors, as blocked pairwise contractions in the same
+// order as the dense plans below (chi^6, chi^7, chi^6 flops); the projector on the
+// incoming side is the adjoint (dual charges).
+//   y: T'[a,b,g,d] = Ux'[i,j,a] Ux[k,l,d] A2[i,e,g,k] A1[j,b,e,l]
+//   x: T'[a,b,c,d] = A1[a,i,k,e] A2[e,j,l,d] Uy'[i,j,b] Uy[k,l,c]
+static DT hotrg_step_y_charged(Ctx& c, const DT& A1, const DT& A2, const DT& Ux) {
+    DT Ud = dual_copy(c, Ux);
+    DT W = contract(c, A1, {Lj, Lb, Le, Ll}, Ud, {Li, Lj, La}, {Lb, Le, Ll, Li, La});
+    Ud = DT();
+    DT V = contract(c, W, {Lb, Le, Ll, Li, La}, A2, {Li, Le, Lg, Lk}, {Lb, Ll, La, Lg, Lk});
+    W = DT();
+    return contract(c, V, {Lb, Ll, La, Lg, Lk}, Ux, {Lk, Ll, Ld}, {La, Lb, Lg, Ld});
+}
+static DT hotrg_step_x_charged(Ctx& c, const DT& A1, const DT& A2, const DT& Uy) {
+    DT Ud = dual_copy(c, Uy);
+    DT W = contract(c, A1, {La, Li, Lk, Le}, Ud, {Li, Lj, Lb}, {La, Lk, Le, Lj, Lb});
+    Ud = DT();
+    DT V = contract(c, W, {La, Lk, Le, Lj, Lb}, A2, {Le, Lj, Ll, Ld}, {La, Lk, Lb, Ll, Ld});
+    W = DT();
+    return contract(c, V, {La, Lk, Lb, Ll, Ld}, Uy, {Lk, Ll, Lc}, {La, Lb, Lc, Ld});
 }
 
 // _step_hotrg_y (src/schemes/hotrg.jl:42-60), A1 = A2 = T (dims dL, dD, dU, dR):
@@ -423,6 +519,7 @@ static DT hotrg_yproj(Scheme& s, const DT& T, int chi) {
 //    O[b,d,g,a] = V[b,(l,k)] Uxq[(l,k),d] per (g,a);  T' = O permuted (a,b,g,d).
 // (A1 and A2 of equal dims: the pure tensor twice for HOTRG, impurity pairs for ImpurityHOTRG)
 static DT hotrg_step_y2(Ctx& c, const DT& A1, const DT& A2, const DT& Ux) {
+    if (A1.charged() && A2.charged() && Ux.charged()) return hotrg_step_y_charged(c, A1, A2, Ux);
     const int64_t dL = A1.d[0], dD = A1.d[1], dU = A1.d[2], dR = A1.d[3], kx = Ux.d[2];
     TNR_REQUIRE(Ux.d[0] == dL && Ux.d[1] == dL && dL == dR && dD == dU, TNR_ERR_INVALID_ARG, "HOTRG y-step dims");
     for (int l = 0; l < 4; ++l) TNR_REQUIRE(A2.d[l] == A1.d[l], TNR_ERR_INVALID_ARG, "HOTRG y-step: A1/A2 dims differ");
@@ -464,6 +561,7 @@ static void hotrg_step_y(Scheme& s, const DT& Ux) { s.T = hotrg_step_y2(*s.ctx, 
 // as W[a,k,e,j,b] = A1p[(a,k,e),i] Uy[i,(j,b)];  V[a,k,l,d,b] = W[(a,k),(e,j)] A2[(e,j),(l,d)] per b;
 //    T'[a,b,c,d] = V[a,(k,l)] Uy[(k,l),c] per (d,b), written in place (ldc = dL*ky).
 static DT hotrg_step_x2(Ctx& c, const DT& A1, const DT& A2, const DT& Uy) {
+    if (A1.charged() && A2.charged() && Uy.charged()) return hotrg_step_x_charged(c, A1, A2, Uy);
     const int64_t dL = A1.d[0], dD = A1.d[1], dU = A1.d[2], dR = A1.d[3], ky = Uy.d[2];
     TNR_REQUIRE(Uy.d[0] == dD && Uy.d[1] == dD && dL == dR && dD == dU, TNR_ERR_INVALID_ARG, "HOTRG x-step dims");
     for (int l = 0; l < 4; ++l) TNR_REQUIRE(A2.d[l] == A1.d[l], TNR_ERR_INVALID_ARG, "HOTRG x-step: A1/A2 dims differ");
@@ -547,10 +645,14 @@ static DT gram3d(Scheme& s, const DT& T, bool mdagm) {
     const int Y = Lh, X = Lg, y = Ly, w = Lw;
     std::vector<int> a2 = mdagm ? std::vector<int>{Lz, w, Y, Lx, y, X} : std::vector<int>{Lz, w, Y, X, y, Lx};
     std::vector<int> a2c = mdagm ? std::vector<int>{Lv, w, Y, Lu, y, X} : std::vector<int>{Lv, w, Y, X, y, Lu};
-    DT P = contract(c, T, a2, T, a2c, {Lx, Lz, Lv, Lu}, false);
+    // the adjoint copies: the same entries; a charged tensor's adjoint carries the dual charges
+    DT Tdual;
+    if (T.charged()) Tdual = dual_copy(c, T);
+    const DT& Tc = T.charged() ? Tdual : T;
+    DT P = contract(c, T, a2, Tc, a2c, {Lx, Lz, Lv, Lu}, false);
     std::vector<int> a1 = mdagm ? std::vector<int>{Lp, Lz, Y, Lr, y, X} : std::vector<int>{Lp, Lz, Y, X, y, Lr};
     std::vector<int> a1c = mdagm ? std::vector<int>{Lp, Lv, Y, Ls, y, X} : std::vector<int>{Lp, Lv, Y, X, y, Ls};
-    DT N = contract(c, T, a1, T, a1c, {Lz, Lr, Lv, Ls}, false);
+    DT N = contract(c, T, a1, Tc, a1c, {Lz, Lr, Lv, Ls}, false);
     return contract(c, P, {Lx, Lz, Lv, Lu}, N, {Lz, Lr, Lv, Ls}, {Lr, Lx, Ls, Lu}, false);
 }
 
@@ -572,9 +674,56 @@ static DT hotrg3d_xproj(Scheme& s, const DT& T, int chi) {
 // _step_hotrg3d (hotrg3d.jl:108-117):
 //   T[a,b,c,d,e,f] = Ux[x1,x2,f] Ux[x1',x2',d] Uy[y1,y2,e] Uy[y1',y2',c] A1[a,z,y1',x1',y1,x1] A2[z,b,y2',x2',y2,x2]
 // contracted leg by leg (largest intermediate chi^8), sliced over the open leg a.
+// The same network on a Z2-charged tensor (Z2 charges are self-dual, so the network's adjoint
+// legs need no separate charges): each slice of A1 over the open leg a is copied into a
+// charged tensor and every pairwise contraction runs block by block over the charge sectors.
+static void hotrg3d_contract_charged(Scheme& s, const DT& Ux, const DT& Uy, int64_t max_entries) {
+    Ctx& c = *s.ctx;
+    const DT& T = s.T;
+    DT A1s = permuted(c, T, {1, 2, 3, 4, 5, 0});
+    const int64_t da = T.d[0];
+    int64_t per_a = 1;
+    for (int i = 1; i < 6; ++i) per_a *= T.d[i];
+    int64_t inter = (per_a / (T.d[2] * T.d[3])) * Ux.d[1] * Ux.d[2] * Uy.d[1] * Uy.d[2];
+    int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(da, max_entries / std::max<int64_t>(inter, 1)));
+    const int P_ = Lp, Q_ = Lq, R_ = Lr, S_ = Ls;
+    std::vector<int64_t> od = {T.d[1], Uy.d[2], Ux.d[2], Uy.d[2], Ux.d[2], da};
+    DT Out = make_dt(c.pool.get(), od);
+    const int64_t slab = od[0] * od[1] * od[2] * od[3] * od[4];
+    for (int64_t a0 = 0; a0 < da; a0 += chunk) {
+        const int64_t na = std::min(chunk, da - a0);
+        DT A1 = make_dt(c.pool.get(), {T.d[1], T.d[2], T.d[3], T.d[4], T.d[5], na});
+        copy_f64(c, A1.p(), A1s.p() + a0 * per_a, per_a * na);
+        A1.N = T.N;
+        for (int l = 0; l < 5; ++l) A1.q.push_back(A1s.q[l]);
+        A1.q.push_back(std::vector<int>(A1s.q[5].begin() + a0, A1s.q[5].begin() + a0 + na));
+        DT X = contract(c, A1, {Lz, P_, Q_, Ly, Lx, La}, Ux, {Q_, R_, Ld}, {Lz, P_, Ly, Lx, La, R_, Ld});
+        A1 = DT();
+        DT Yt = contract(c, X, {Lz, P_, Ly, Lx, La, R_, Ld}, Uy, {P_, S_, Lc}, {Lz, Ly, Lx, La, R_, Ld, S_, Lc});
+        X = DT();
+        DT Z = contract(c, Yt, {Lz, Ly, Lx, La, R_, Ld, S_, Lc}, T, {Lz, Lb, S_, R_, Lu, Lv},
+                        {Ly, Lx, La, Ld, Lc, Lb, Lu, Lv});
+        Yt = DT();
+        DT W = contract(c, Z, {Ly, Lx, La, Ld, Lc, Lb, Lu, Lv}, Ux, {Lx, Lv, Lf}, {Ly, La, Ld, Lc, Lb, Lu, Lf});
+        Z = DT();
+        DT O = contract(c, W, {Ly, La, Ld, Lc, Lb, Lu, Lf}, Uy, {Ly, Lu, Le}, {Lb, Lc, Ld, Le, Lf, La});
+        copy_f64(c, Out.p() + a0 * slab, O.p(), slab * na);
+        if (a0 == 0) {
+            Out.N = O.N;
+            for (int l = 0; l < 5; ++l) Out.q.push_back(O.q[l]);
+            Out.q.push_back(T.q[0]);
+        }
+    }
+    s.T = permuted(c, Out, {5, 0, 1, 2, 3, 4});
+}
+
 static void hotrg3d_contract(Scheme& s, const DT& Ux, const DT& Uy, int64_t max_entries) {
     Ctx& c = *s.ctx;
     const DT& T = s.T;
+    if (T.charged() && Ux.charged() && Uy.charged()) {
+        hotrg3d_contract_charged(s, Ux, Uy, max_entries);
+        return;
+    }
     // A1 with the open leg a moved last so slices are contiguous: A1s[z,P,Q,y,x,a]
     DT A1s = permuted(c, T, {1, 2, 3, 4, 5, 0});
     const int64_t da = T.d[0];

@@ -18,6 +18,7 @@
 #include "common.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <numeric>
 #include <vector>
 
@@ -214,6 +215,190 @@ TsvdOut tsvd_sectors(Ctx& c, const double* M, int64_t m, int64_t n, int k, doubl
     out.err = std::sqrt(std::max(fro2 - kept2, 0.0));
     out.vals = sv;
     return out;
+}
+
+namespace {
+
+// Row and column classes of a charged tensor's (row legs <- column legs) matrix, first leg
+// fastest: row class = (sum of the row legs' charges) mod N, column class = -(sum of the column
+// legs' charges) mod N; every nonzero entry joins a row and a column of the same class.
+void matrix_classes(const DT& M, int nrow, std::vector<int>& rc, std::vector<int>& cc) {
+    const int N = M.N;
+    auto classes = [&](int l0, int l1, int sign, std::vector<int>& out) {
+        int64_t total = 1;
+        for (int l = l0; l < l1; ++l) total *= M.d[l];
+        out.assign(total, 0);
+        for (int64_t e = 0; e < total; ++e) {
+            int64_t rem = e;
+            int q = 0;
+            for (int l = l0; l < l1; ++l) {
+                q += M.q[l][rem % M.d[l]];
+                rem /= M.d[l];
+            }
+            out[e] = (((sign * q) % N) + N) % N;
+        }
+    };
+    classes(0, nrow, 1, rc);
+    classes(nrow, M.rank, -1, cc);
+}
+
+DecompDT decompose_charged(Ctx& c, const DT& M, int nrow, int chi, bool eigh) {
+    const int N = M.N;
+    std::vector<int> rc, cc;
+    matrix_classes(M, nrow, rc, cc);
+    const int64_t m = (int64_t)rc.size(), n = (int64_t)cc.size();
+    struct Part {
+        int cls = 0, kb = 0;
+        std::vector<int> rows, cols;
+        Buf Ub, Vb;
+        std::vector<double> vals;
+    };
+    std::vector<Part> parts;
+    double fro2 = 0;
+    for (int cl = 0; cl < N; ++cl) {
+        Part P;
+        P.cls = cl;
+        for (int64_t i = 0; i < m; ++i)
+            if (rc[i] == cl) P.rows.push_back((int)i);
+        for (int64_t j = 0; j < n; ++j)
+            if (cc[j] == cl) P.cols.push_back((int)j);
+        if (P.rows.empty() || P.cols.empty()) continue;
+        if (eigh)
+            TNR_REQUIRE(P.rows == P.cols, TNR_ERR_INVALID_ARG,
+                        "eigh of a charged tensor: row and column sectors differ (not a Gram matrix)");
+        const int mr = (int)P.rows.size(), nc = (int)P.cols.size();
+        P.kb = std::min({chi, mr, nc});
+        if (P.kb <= 0) continue;
+        Buf rows(c.pool.get(), (size_t)mr * sizeof(int)), cols(c.pool.get(), (size_t)nc * sizeof(int));
+        TNR_CUDA(cudaMemcpyAsync(rows.d(), P.rows.data(), (size_t)mr * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        TNR_CUDA(cudaMemcpyAsync(cols.d(), P.cols.data(), (size_t)nc * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        Buf Bm(c.pool.get(), (size_t)mr * nc * sizeof(double));
+        k_gather_block<<<blocks_for((int64_t)mr * nc), 256, 0, c.stream>>>(M.p(), m, rows.as<int>(), mr,
+                                                                            cols.as<int>(), nc, Bm.d());
+        check_launch("gather_block");
+        P.Ub = Buf(c.pool.get(), (size_t)mr * P.kb * sizeof(double));
+        Buf sb(c.pool.get(), (size_t)P.kb * sizeof(double));
+        TsvdOut r;
+        if (eigh) {
+            r = teigh(c, Bm.d(), mr, P.kb, P.Ub.d(), sb.d());
+        } else {
+            P.Vb = Buf(c.pool.get(), (size_t)P.kb * nc * sizeof(double));
+            r = tsvd(c, Bm.d(), mr, nc, P.kb, P.Ub.d(), sb.d(), P.Vb.d());
+        }
+        P.vals = r.vals;
+        fro2 += r.fro2;
+        parts.push_back(std::move(P));
+    }
+    // global truncation over the sectors: the chi largest |values|, descending; ties keep the
+    // lower sector, then the lower index, first
+    struct Pick {
+        double a;
+        int part, idx;
+    };
+    std::vector<Pick> all;
+    for (int p = 0; p < (int)parts.size(); ++p)
+        for (int i = 0; i < (int)parts[p].vals.size(); ++i) all.push_back({std::fabs(parts[p].vals[i]), p, i});
+    std::stable_sort(all.begin(), all.end(), [](const Pick& a, const Pick& b) { return a.a > b.a; });
+    const int k = std::min<int>(chi, (int)all.size());
+    TNR_REQUIRE(k >= 1, TNR_ERR_INVALID_ARG, "decomposition of a charged tensor with no nonzero sector");
+    DecompDT out;
+    out.k = k;
+    std::vector<int64_t> ud(M.d, M.d + nrow), vd{(int64_t)k};
+    ud.push_back(k);
+    for (int l = nrow; l < M.rank; ++l) vd.push_back(M.d[l]);
+    out.U = make_dt(c.pool.get(), ud);
+    TNR_CUDA(cudaMemsetAsync(out.U.p(), 0, (size_t)out.U.size() * sizeof(double), c.stream));
+    if (!eigh) {
+        out.Vt = make_dt(c.pool.get(), vd);
+        TNR_CUDA(cudaMemsetAsync(out.Vt.p(), 0, (size_t)out.Vt.size() * sizeof(double), c.stream));
+    }
+    std::vector<double> sv(k);
+    std::vector<int> bond(k);
+    double kept2 = 0;
+    for (int t = 0; t < k; ++t) {
+        sv[t] = parts[all[t].part].vals[all[t].idx];
+        bond[t] = parts[all[t].part].cls;
+        kept2 += sv[t] * sv[t];
+    }
+    out.s = Buf(c.pool.get(), (size_t)k * sizeof(double));
+    TNR_CUDA(cudaMemcpyAsync(out.s.d(), sv.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    for (int p = 0; p < (int)parts.size(); ++p) {
+        std::vector<int> src, dst;
+        for (int t = 0; t < k; ++t)
+            if (all[t].part == p) {
+                src.push_back(all[t].idx);
+                dst.push_back(t);
+            }
+        if (src.empty()) continue;
+        const Part& P = parts[p];
+        const int mr = (int)P.rows.size(), nc = (int)P.cols.size(), cnt = (int)src.size();
+        Buf rows(c.pool.get(), (size_t)mr * sizeof(int)), cols(c.pool.get(), (size_t)nc * sizeof(int));
+        Buf srcd(c.pool.get(), (size_t)cnt * sizeof(int)), dstd(c.pool.get(), (size_t)cnt * sizeof(int));
+        TNR_CUDA(cudaMemcpyAsync(rows.d(), P.rows.data(), (size_t)mr * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        TNR_CUDA(cudaMemcpyAsync(cols.d(), P.cols.data(), (size_t)nc * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        TNR_CUDA(cudaMemcpyAsync(srcd.d(), src.data(), (size_t)cnt * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        TNR_CUDA(cudaMemcpyAsync(dstd.d(), dst.data(), (size_t)cnt * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        k_scatter_cols<<<blocks_for((int64_t)mr * cnt), 256, 0, c.stream>>>(P.Ub.d(), mr, rows.as<int>(),
+                                                                            srcd.as<int>(), dstd.as<int>(), cnt,
+                                                                            out.U.p(), m);
+        check_launch("scatter_cols");
+        if (!eigh) {
+            k_scatter_rows<<<blocks_for((int64_t)cnt * nc), 256, 0, c.stream>>>(P.Vb.d(), P.kb, cols.as<int>(), nc,
+                                                                                srcd.as<int>(), dstd.as<int>(), cnt,
+                                                                                out.Vt.p(), k);
+            check_launch("scatter_rows");
+        }
+    }
+    out.U.N = N;
+    for (int l = 0; l < nrow; ++l) out.U.q.push_back(M.q[l]);
+    std::vector<int> qu(k), qv(k);
+    for (int t = 0; t < k; ++t) {
+        qu[t] = (N - bond[t]) % N;
+        qv[t] = bond[t];
+    }
+    out.U.q.push_back(qu);
+    if (!eigh) {
+        out.Vt.N = N;
+        out.Vt.q.push_back(qv);
+        for (int l = nrow; l < M.rank; ++l) out.Vt.q.push_back(M.q[l]);
+    }
+    out.info.k = k;
+    out.info.fro2 = fro2;
+    out.info.err = std::sqrt(std::max(fro2 - kept2, 0.0));
+    out.info.vals = sv;
+    c.sync();      // every host index vector above outlives its copies
+    return out;
+}
+
+DecompDT decompose_plain(Ctx& c, const DT& M, int nrow, int chi, bool eigh) {
+    int64_t m = 1, n = 1;
+    for (int l = 0; l < nrow; ++l) m *= M.d[l];
+    for (int l = nrow; l < M.rank; ++l) n *= M.d[l];
+    const int k = (int)std::min<int64_t>(chi, std::min(m, n));
+    DecompDT out;
+    out.k = k;
+    std::vector<int64_t> ud(M.d, M.d + nrow), vd{(int64_t)k};
+    ud.push_back(k);
+    for (int l = nrow; l < M.rank; ++l) vd.push_back(M.d[l]);
+    out.U = make_dt(c.pool.get(), ud);
+    out.s = Buf(c.pool.get(), (size_t)k * sizeof(double));
+    if (eigh) {
+        out.info = teigh(c, M.p(), m, k, out.U.p(), out.s.d());
+    } else {
+        out.Vt = make_dt(c.pool.get(), vd);
+        out.info = tsvd(c, M.p(), m, n, k, out.U.p(), out.s.d(), out.Vt.p());
+    }
+    return out;
+}
+
+}  // namespace
+
+DecompDT svd_dt(Ctx& c, const DT& M, int nrow, int chi) {
+    return M.charged() ? decompose_charged(c, M, nrow, chi, false) : decompose_plain(c, M, nrow, chi, false);
+}
+
+DecompDT eigh_dt(Ctx& c, const DT& MM, int nrow, int chi) {
+    return MM.charged() ? decompose_charged(c, MM, nrow, chi, true) : decompose_plain(c, MM, nrow, chi, true);
 }
 
 }  // namespace tnr

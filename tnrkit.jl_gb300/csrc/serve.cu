@@ -24,6 +24,8 @@ struct Request {
     std::vector<int64_t> dims;
     std::vector<double> data;
     double btrg_k = -0.5;
+    int symmetry_n = 1;
+    std::vector<int32_t> charges;   // sum(dims) leg charges when symmetry_n > 1
     size_t footprint = 0;
     Clock::time_point t_submit, t_start, t_done;
     int status = TNR_OK;
@@ -112,6 +114,10 @@ struct tnr_server_s {
             tnr_default_options(&o);
             o.precision = precision;
             o.btrg_k = r->btrg_k;
+            if (r->symmetry_n > 1) {
+                o.symmetry_n = r->symmetry_n;
+                o.leg_charges = r->charges.data();
+            }
             int st = tnr_create(&h, r->kind, (int)r->dims.size(), r->dims.data(), r->data.data(), &o);
             if (st == TNR_OK) {
                 const size_t cap = (size_t)std::max(r->maxiter, 1) + 1;
@@ -158,6 +164,13 @@ int tnr_server_create(tnr_server* out, size_t hbm_budget_bytes, int max_active, 
 
 int tnr_server_submit(tnr_server s, int kind, int nlegs, const int64_t* dims, const double* data, int chi,
                       int maxiter, double btrg_k, uint64_t* id_out) {
+    return tnr_server_submit_sym(s, kind, nlegs, dims, data, 1, nullptr, chi, maxiter, btrg_k, id_out);
+}
+
+int tnr_server_submit_sym(tnr_server s, int kind, int nlegs, const int64_t* dims, const double* data,
+                          int symmetry_n, const int32_t* leg_charges, int chi, int maxiter, double btrg_k,
+                          uint64_t* id_out) {
+    if (symmetry_n > 1 && !leg_charges) return TNR_ERR_INVALID_ARG;
     if (!s || !dims || !data || !id_out || chi < 1) return TNR_ERR_INVALID_ARG;
     if ((kind < TNR_TRG || kind > TNR_HOTRG_3D) && kind != TNR_ATRG && kind != TNR_ATRG_3D) return TNR_ERR_INVALID_ARG;
     if (nlegs != (kind == TNR_HOTRG_3D || kind == TNR_ATRG_3D ? 6 : 4)) return TNR_ERR_INVALID_ARG;
@@ -177,6 +190,12 @@ int tnr_server_submit(tnr_server s, int kind, int nlegs, const int64_t* dims, co
         total *= dims[l];
     }
     r->data.assign(data, data + total);
+    if (symmetry_n > 1) {
+        int64_t nq = 0;
+        for (int l = 0; l < nlegs; ++l) nq += dims[l];
+        r->symmetry_n = symmetry_n;
+        r->charges.assign(leg_charges, leg_charges + nq);
+    }
     r->footprint = footprint_bytes(kind, chi, r->dims);
     r->t_submit = Clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
