@@ -45,6 +45,8 @@ def parse():
                         "|df/f|); -1 = all of them")
     p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-other-configs", action="store_true",
+                   help="skip the bounded measurements of the other configurations in the default run")
     p.add_argument("--workload", default="beta_sweep",
                    choices=["beta_sweep", "hotrg_step", "serving", "hotrg3d", "gemm"],
                    help="beta_sweep is the headline metric; the others measure the remaining configurations; "
@@ -59,10 +61,10 @@ def parse():
     return p.parse_args()
 
 
-def workload(n, seed):
+def workload(n, seed, chis=CHIS):
     rng = np.random.Generator(np.random.PCG64(seed))
     betas = rng.uniform(0.30, 0.60, n)
-    chis = rng.choice(np.array(CHIS), n)
+    chis = rng.choice(np.array(chis), n)
     return betas, chis
 
 
@@ -279,7 +281,10 @@ def run_ours(args, d):
     ge.build()
     tnr = ge.package()
     prec = tnr.PREC_SPLIT if args.precision == "split" else tnr.PREC_F64
-    betas, chis = workload(args.instances, args.seed + d.rank)
+    # --chis restricts the draw (a profiling aid, e.g. one lockstep group alone); the headline
+    # workload draws from all five
+    sweep_chis = tuple(int(x) for x in args.chis.split(",")) if args.chis else CHIS
+    betas, chis = workload(args.instances, args.seed + d.rank, sweep_chis)
     n = len(betas)
     maxit = [args.maxiter] * n
     tensors = [tnr.classical_ising("Trivial", float(b)) for b in betas]
@@ -384,7 +389,8 @@ def run_ours(args, d):
         "dtype": "bf16x3 split (fp32 accumulate) + f64" if prec == tnr.PREC_SPLIT else "f64",
         "data": "synthetic (analytic Ising tensors, seeded beta/chi draws)",
         "config": {"workload": "btrg_beta_sweep: %d BTRG solves, 2D Ising (Trivial), beta~U[0.30,0.60], "
-                               "chi~U{8,16,24,32,48}, maxiter %d, seed %d" % (n, args.maxiter, args.seed),
+                               "chi~U{%s}, maxiter %d, seed %d" % (n, ",".join(str(x) for x in sweep_chis),
+                                                                   args.maxiter, args.seed),
                    "instances_per_gpu": n, "maxiter": args.maxiter, "precision": args.precision,
                    "l2": "working set > L2: every instance keeps chi^4 tensors and chi^6-flop intermediates "
                          "resident; batch state is several GB"},
@@ -492,6 +498,59 @@ def run_hotrg3d(args, tnr):
     return {"workload": "hotrg3d: 3D Ising Z2 at beta=0.2216, HOTRG_3D", "rows": rows}
 
 
+def run_other_configs(args, tnr):
+    """The remaining configurations of the benchmark brief, bounded so that the default run stays
+    within minutes; each entry names its workload and what it measured.
+      - trg: plain TRG, 2D Ising at beta_c, Trivial, FP64, truncrank(16), maxiter(25): device time
+        of the solve and its free energy, beside the CPU oracle's time and f (the CPU baseline);
+      - hotrg_step: one HOTRG step + finalize on the seeded chi^4 tensor, chi 32/48/64, plain FP64
+        and split precision (engine contraction flops 4 chi^7 + 32 chi^6);
+      - serving: 16 Poisson(200/s) requests of the serving mix (Z2/Z3/Z6 models on the block-sparse
+        path), split precision: solves/s, p50, p99;
+      - hotrg3d: 3D Ising Z2 at beta = 0.2216, 15 iterations, split precision at chi = 16, and split
+        against plain FP64 at chi = 8 (|df/f|)."""
+    out = {}
+    # config 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tnr_oracle as o
+    s = tnr.TRG(tnr.classical_ising("Trivial"))
+    with tnr.Timer(s) as tm:
+        d = tnr.run(s, tnr.truncrank(16), tnr.maxiter(25))
+    s.close()
+    f = tnr.free_energy(d, tnr.ising_βc)
+    t0 = time.perf_counter()
+    do = o.run(o.TRG(o.classical_ising(symmetry="Trivial")), o.truncrank(16), o.maxiter(25))
+    cpu_ms = 1000 * (time.perf_counter() - t0)
+    fo = o.free_energy(do, o.ISING_BETA_C)
+    out["trg"] = {"workload": "TRG, 2D Ising (Trivial) at beta_c, FP64, truncrank(16), maxiter(25)", "ms": tm.ms,
+                  "f": f, "cpu_oracle_ms": cpu_ms, "f_rel_vs_cpu_oracle": abs(f / fo - 1),
+                  "norms_max_rel_vs_cpu_oracle": float(np.max(np.abs(np.array(d) / np.array(do) - 1)))}
+    # config 2
+    a2 = argparse.Namespace(**vars(args))
+    a2.chis, a2.steps, a2.no_cpu_baseline = "32,48,64", 1, True
+    out["hotrg_step"] = run_hotrg_step(a2, tnr)
+    # config 4
+    a4 = argparse.Namespace(**vars(args))
+    a4.requests, a4.precision = 16, "split"
+    out["serving"] = run_serving(a4, tnr)
+    # config 5
+    rows = []
+    for chi, precs in ((8, ("f64", "split")), (16, ("split",))):
+        fs = {}
+        for pname in precs:
+            T = tnr.classical_ising_3D("Z2", 0.2216)
+            s3 = tnr.HOTRG_3D(T, precision=tnr.PREC_SPLIT if pname == "split" else tnr.PREC_F64)
+            with tnr.Timer(s3) as tm:
+                d3 = tnr.run(s3, tnr.truncrank(chi), tnr.maxiter(15))
+            s3.close()
+            fs[pname] = tnr.free_energy(d3, 0.2216, 8.0)
+            rows.append({"chi": chi, "precision": pname, "ms": tm.ms, "f": fs[pname]})
+        if "f64" in fs:
+            rows[-1]["rel_df_vs_f64"] = abs(fs["split"] / fs["f64"] - 1)
+    out["hotrg3d"] = {"workload": "HOTRG_3D, 3D Ising Z2 (block-sparse) at beta=0.2216, 15 iterations", "rows": rows}
+    return out
+
+
 def run_gemm(args, tnr):
     """One warm-up and ``--steps`` timed batched m x m x k split-precision products on seeded,
     device-resident operands: the contraction path (chunked accumulation when k > 64) or the
@@ -547,6 +606,9 @@ def main():
         print(json.dumps(line), flush=True)
         return
     out, chis = run_ours(args, d)
+    if d.rank == 0 and not args.no_other_configs:
+        import __graft_entry__ as ge
+        out["other_configs"] = run_other_configs(args, ge.package())
     if d.rank == 0:
         if not args.no_cpu_baseline:
             betas, _ = workload(args.instances, args.seed)

@@ -236,11 +236,12 @@ size_t tnr_footprint_bytes(int kind, int chi, int nlegs, const int64_t* dims);
 #define TNR_PROF_GEMM_BULK 0  /* bulk contraction / projection GEMMs run in FP64; work = flops */
 #define TNR_PROF_GEMM_F64  1  /* FP64 GEMMs inside the decompositions; work = flops */
 #define TNR_PROF_JACOBI    2  /* Jacobi eigensolver; work = r^3                     */
-#define TNR_PROF_CHOL      3  /* Cholesky + inverse; work = r^3                     */
+#define TNR_PROF_CHOL      3  /* FP64 Cholesky + inverse; work = r^3                */
 #define TNR_PROF_PERMUTE   4  /* leg permutes; work = bytes read + written          */
 #define TNR_PROF_SPLIT     5  /* FP64 -> 3xBF16 operand split; work = bytes         */
 #define TNR_PROF_JACOBI32  6  /* FP32 Jacobi (basis alignment); work = r^3          */
 #define TNR_PROF_TC        7  /* split 3xBF16 tcgen05 GEMMs; work = 2 m n k flops   */
+#define TNR_PROF_CHOL32    8  /* FP32 Cholesky + inverse (split CholeskyQR); r^3    */
 int tnr_profile_enable(int on);
 int tnr_profile_reset(void);
 int tnr_profile_read(int cls, uint64_t* launches, double* total_ms, double* work);

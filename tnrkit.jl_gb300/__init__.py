@@ -634,7 +634,7 @@ def run_batch(schemes, chis, maxiters, finalize_beginning=True, timing=None):
 
 
 PROFILE_CLASSES = {"gemm_bulk": 0, "gemm_f64": 1, "jacobi": 2, "chol": 3, "permute": 4, "split": 5, "jacobi32": 6,
-                   "tc": 7}
+                   "tc": 7, "chol32": 8}
 
 
 def profile_enable(on=True):

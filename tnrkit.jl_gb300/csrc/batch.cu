@@ -25,10 +25,14 @@ struct BatchState {
     double k = -0.5;
     DT T;        // (d1, d2, d3, d4, B)
     DT S1, S2;   // (d2, B), (d1, B) for BTRG
+    // finalize! leaves T unscaled and points here at the B norms; the next step divides its
+    // singular values by them (both SVDs decompose T or a permute of it), so the batch's
+    // chi^4 tensors are not rescaled in a pass of their own
+    const double* pending = nullptr;
 };
 
 // SVD12 of every instance of M4 (d1, d2, d3, d4, B): A = U sqrt(s), Bv = sqrt(s) V
-static void svd12_b(Ctx& c, const DT& M4, int chi, int B, DT& A, DT& Bv) {
+static void svd12_b(Ctx& c, const DT& M4, int chi, int B, DT& A, DT& Bv, const double* pending) {
     const int64_t d1 = M4.d[0], d2 = M4.d[1], d3 = M4.d[2], d4 = M4.d[3];
     const int64_t m = d1 * d2, n = d3 * d4;
     const int k = (int)std::min<int64_t>(chi, std::min(m, n));
@@ -36,6 +40,7 @@ static void svd12_b(Ctx& c, const DT& M4, int chi, int B, DT& A, DT& Bv) {
     Bv = make_dt(c.pool.get(), {(int64_t)k, d3, d4, (int64_t)B});
     Buf sv(c.pool.get(), (size_t)k * B * sizeof(double));
     tsvd_batched(c, M4.p(), m, n, k, B, A.p(), sv.d(), Bv.p());
+    if (pending) scale_batched(c, sv.d(), k, B, pending);
     col_scale(c, A.p(), m, (int64_t)k * B, m, sv.d(), 1);
     row_scale_batched(c, Bv.p(), k, n * B, sv.d(), 1, n);
 }
@@ -44,9 +49,9 @@ static void svd12_b(Ctx& c, const DT& M4, int chi, int B, DT& A, DT& Bv) {
 static void step_trg_b(Ctx& c, BatchState& s, int chi) {
     const int B = s.B;
     DT A, Bv, C, D;
-    svd12_b(c, s.T, chi, B, A, Bv);
+    svd12_b(c, s.T, chi, B, A, Bv, s.pending);
     DT Tp = permuted(c, s.T, {1, 3, 0, 2, 4});
-    svd12_b(c, Tp, chi, B, C, D);
+    svd12_b(c, Tp, chi, B, C, D, s.pending);
     Tp = DT();
     DT X = contract(c, D.p(), per_dims(D), {Lb, Lp, Lq}, Bv.p(), per_dims(Bv), {La, Lr, Lp}, {La, Lb, Lq, Lr}, true, B);
     DT Y = contract(c, C.p(), per_dims(C), {Lr, Ls, Lc}, A.p(), per_dims(A), {Ls, Lq, Ld}, {Lq, Lr, Lc, Ld}, true, B);
@@ -68,6 +73,7 @@ static void step_btrg_b(Ctx& c, BatchState& s, int chi) {
         Sn = make_dt(c.pool.get(), {(int64_t)k, (int64_t)B});
         Buf sv(c.pool.get(), (size_t)k * B * sizeof(double)), sa(c.pool.get(), (size_t)k * B * sizeof(double));
         tsvd_batched(c, M4.p(), m, n, k, B, U.p(), sv.d(), V.p());
+        if (s.pending) scale_batched(c, sv.d(), k, B, s.pending);
         pseudopow(c, sv.d(), k * B, (1.0 - kexp) / 2.0, sa.d());
         pseudopow(c, sv.d(), k * B, kexp, Sn.p());
         col_scale(c, U.p(), m, (int64_t)k * B, m, sa.d(), 0);
@@ -93,10 +99,11 @@ static void step_btrg_b(Ctx& c, BatchState& s, int chi) {
     s.S2 = std::move(S2n);
 }
 
+// finalize! of every member: the norms, with T's scaling left to the next step (pending)
 static void finalize_b(Ctx& c, BatchState& s, double* d_norms) {
     const bool btrg = s.kind == TNR_BTRG;
     trace2d_batched(c, s.T.p(), s.T.d, s.B, btrg ? s.S1.p() : nullptr, btrg ? s.S2.p() : nullptr, d_norms);
-    scale_batched(c, s.T.p(), per_size(s.T), s.B, d_norms);
+    s.pending = d_norms;
 }
 
 // run!() of every member in lockstep; members are fresh schemes with equal kind, dims, k
@@ -138,9 +145,13 @@ void run_group(Ctx& c, const std::vector<Scheme*>& mem, int chi, int maxiter, bo
             PrecisionScope scope(c, split_step_in_fp64(s.kind, step0 + i, s.T.d, s.T.rank - 1, chi));
             if (s.kind == TNR_TRG) step_trg_b(c, s, chi);
             else step_btrg_b(c, s, chi);
+            s.pending = nullptr;
         }
         finalize_b(c, s, dn.d() + (at++) * B);
     }
+    // the members get their tensors back normalised, as after run!()
+    if (s.pending) scale_batched(c, s.T.p(), per_size(s.T), s.B, s.pending);
+    s.pending = nullptr;
     check_finite(c, dn.d(), (int64_t)nn * B);
     std::vector<double> h((size_t)nn * B);
     TNR_CUDA(cudaMemcpyAsync(h.data(), dn.d(), h.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));

@@ -93,7 +93,8 @@ enum ProfClass : int {
     PROF_SPLIT = 5,       // FP64 -> BF16 split conversion, work = bytes moved
     PROF_JACOBI32 = 6,    // FP32 Jacobi (alignment), work = r^3
     PROF_TC = 7,          // split 3xBF16 tcgen05 GEMMs, work = 2 m n k flops
-    PROF_NCLASS = 8
+    PROF_CHOL32 = 8,      // FP32 Cholesky + inverse (split-precision CholeskyQR), work = r^3
+    PROF_NCLASS = 9
 };
 extern std::atomic<bool> g_prof_on;
 int prof_start(cudaStream_t s);
@@ -322,13 +323,16 @@ struct TsvdOut {
 };
 
 // M (m x n, ld = m, column-major): U (m x k), s (k), Vt (k x n)
-TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt);
+// direct_max: largest min(m, n) decomposed directly (one-CTA solvers on the whole matrix) rather
+// than by subspace iteration; at most 128
+TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt,
+             int direct_max = 128);
 // R' = diag(s) V^T (n x n) from the SVD M = U diag(s) V^T of a column-major m x n matrix (m >= n,
 // n <= 160).  R' equals the R of any QR decomposition M = Q R up to an orthogonal factor on its
 // rows (R = W R'), for every rank of M: exactly rank-deficient M, which breaks CholeskyQR, is fine.
 void svd_r_factor(Ctx& c, const double* M, int64_t m, int n, double* R);
 // symmetric M (n x n): U (n x k) eigenvectors of the k largest |eigenvalues|, lam (k)
-TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lam);
+TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lam, int direct_max = 128);
 // The truncated SVD of M over the sectors its exact zeros reveal (connected components of the
 // bipartite graph row r -- column c iff M[r, c] != 0): one SVD per sector block, the k largest
 // values over all blocks kept, every singular vector supported on one sector (zero elsewhere).
@@ -382,5 +386,7 @@ inline DT contract(Ctx& c, const DT& A, const std::vector<int>& lA, const DT& B,
     return contract(c, A.p(), A.dims(), lA, B.p(), B.dims(), lB, lOut, bulk);
 }
 DT permuted(Ctx& c, const DT& A, const std::vector<int>& perm);
+// the same, every entry divided by |*scale| (a device scalar) on the way
+DT permuted_scaled(Ctx& c, const DT& A, const std::vector<int>& perm, const double* scale);
 
 }  // namespace tnr

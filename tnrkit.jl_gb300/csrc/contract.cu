@@ -5,6 +5,7 @@
 #include "common.cuh"
 
 #include <algorithm>
+#include <cstring>
 
 namespace tnr {
 
@@ -152,51 +153,109 @@ DT contract(Ctx& c, const double* A, const std::vector<int64_t>& dA, const std::
 
 namespace {
 
-// out[i + j mr] = X[ro[i] + co[j]]
+// out[i + j ld] = X[ro[i] + co[j]], i < mr, j < nc
 __global__ void k_gather_offsets(const double* __restrict__ X, const int64_t* __restrict__ ro, int64_t mr,
-                                 const int64_t* __restrict__ co, int64_t nc, double* __restrict__ out) {
+                                 const int64_t* __restrict__ co, int64_t nc, double* __restrict__ out, int64_t ld) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mr * nc; e += (int64_t)gridDim.x * blockDim.x)
-        out[e] = X[ro[e % mr] + co[e / mr]];
+        out[e % mr + (e / mr) * ld] = X[ro[e % mr] + co[e / mr]];
 }
 
-// X[ro[i] + co[j]] = in[i + j mr]
-__global__ void k_scatter_offsets(const double* __restrict__ in, const int64_t* __restrict__ ro, int64_t mr,
-                                  const int64_t* __restrict__ co, int64_t nc, double* __restrict__ X) {
+// X[ro[i] + co[j]] = in[i + j ld], i < mr, j < nc
+__global__ void k_scatter_offsets(const double* __restrict__ in, int64_t ld, const int64_t* __restrict__ ro,
+                                  int64_t mr, const int64_t* __restrict__ co, int64_t nc, double* __restrict__ X) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mr * nc; e += (int64_t)gridDim.x * blockDim.x)
-        X[ro[e % mr] + co[e / mr]] = in[e];
+        X[ro[e % mr] + co[e / mr]] = in[e % mr + (e / mr) * ld];
 }
 
 unsigned grid_of(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
-// Every combination of a group of legs (first leg fastest): its offsets under two stride sets
-// and its charge sum mod N (charges from `qs`, one vector per leg).
-struct Combos {
-    std::vector<int64_t> off1, off2;
-    std::vector<int> q;
+// A group of legs (first leg fastest) split by charge class.  Every leg's basis indices are
+// listed class by class on the host (O(sum of dims)); a class of the group is the union of the
+// products of per-leg lists whose classes sum to it ("tuples", at most N^L of them), and the
+// device expands the tuples into the combinations' offsets under two stride sets.  Nothing of
+// size O(combinations) is built or copied on the host.
+constexpr int MAXL = MAXR;
+struct TupleDesc {
+    int64_t start, size;          // position of the tuple in its class's list, its combinations
+    int off[MAXL], len[MAXL];     // per leg: the class list's offset in `lists` and its length
 };
-Combos enumerate(const std::vector<int64_t>& dims, const std::vector<int64_t>& st1, const std::vector<int64_t>& st2,
-                 const std::vector<const std::vector<int>*>& qs, int N) {
-    Combos c;
-    int64_t total = 1;
-    for (auto d : dims) total *= d;
-    c.off1.assign(total, 0);
-    c.off2.assign(total, 0);
-    c.q.assign(total, 0);
-    for (int64_t e = 0; e < total; ++e) {
-        int64_t rem = e, o1 = 0, o2 = 0;
-        int q = 0;
-        for (size_t l = 0; l < dims.size(); ++l) {
-            const int64_t i = rem % dims[l];
-            rem /= dims[l];
-            o1 += i * st1[l];
-            o2 += i * st2[l];
-            q += (*qs[l])[i];
+
+__global__ void k_expand_offsets(const TupleDesc* __restrict__ tup, int ntup, const int* __restrict__ lists, int L,
+                                 const int64_t* __restrict__ st, int64_t total, int64_t* __restrict__ o1,
+                                 int64_t* __restrict__ o2) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = ntup - 1;             // the last tuple whose start is <= e
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tup[mid].start <= e) lo = mid;
+            else hi = mid - 1;
         }
-        c.off1[e] = o1;
-        c.off2[e] = o2;
-        c.q[e] = ((q % N) + N) % N;
+        const int t = lo;
+        int64_t j = e - tup[t].start, a = 0, b = 0;
+        for (int l = 0; l < L; ++l) {
+            const int n = tup[t].len[l];
+            const int i = lists[tup[t].off[l] + (int)(j % n)];
+            j /= n;
+            a += (int64_t)i * st[l];
+            b += (int64_t)i * st[MAXL + l];
+        }
+        o1[e] = a;
+        o2[e] = b;
     }
-    return c;
+}
+
+struct GroupPlan {
+    std::vector<int> lists;                      // per leg, per class: the basis indices
+    std::vector<std::vector<TupleDesc>> tuples;  // per class of the group
+    std::vector<int64_t> count;                  // per class: combinations
+};
+
+GroupPlan plan_group(const std::vector<int64_t>& dims, const std::vector<const std::vector<int>*>& qs, int N) {
+    const int L = (int)dims.size();
+    TNR_REQUIRE(L <= MAXL, TNR_ERR_UNSUPPORTED, "contract: too many legs in a group");
+    GroupPlan g;
+    std::vector<std::vector<int>> off(L, std::vector<int>(N, 0)), len(L, std::vector<int>(N, 0));
+    for (int l = 0; l < L; ++l)
+        for (int cl = 0; cl < N; ++cl) {
+            off[l][cl] = (int)g.lists.size();
+            for (int64_t i = 0; i < dims[l]; ++i)
+                if ((*qs[l])[i] == cl) g.lists.push_back((int)i);
+            len[l][cl] = (int)g.lists.size() - off[l][cl];
+        }
+    g.tuples.assign(N, {});
+    g.count.assign(N, 0);
+    int64_t ntuples = 1;
+    for (int l = 0; l < L; ++l) ntuples *= N;
+    for (int64_t t = 0; t < ntuples; ++t) {
+        int64_t r = t, size = 1;
+        int sum = 0;
+        TupleDesc d{};
+        for (int l = 0; l < L; ++l) {
+            const int cl = (int)(r % N);
+            r /= N;
+            sum += cl;
+            d.off[l] = off[l][cl];
+            d.len[l] = len[l][cl];
+            size *= d.len[l];
+        }
+        if (size == 0) continue;
+        const int cl = sum % N;
+        d.start = g.count[cl];
+        d.size = size;
+        g.count[cl] += size;
+        g.tuples[cl].push_back(d);
+    }
+    return g;
+}
+
+// device offsets of one class of a group (tuples `d_t`, `ntup` of them; lists and strides on the
+// device): o1 / o2 under the two stride sets.  An empty group (L = 0) is the single
+// combination with offset 0.
+void expand_class(Ctx& c, const TupleDesc* d_t, int ntup, int64_t total, const int* d_lists, int L,
+                  const int64_t* d_st, int64_t* o1, int64_t* o2) {
+    if (!ntup || !total) return;
+    k_expand_offsets<<<grid_of(total), 256, 0, c.stream>>>(d_t, ntup, d_lists, L, d_st, total, o1, o2);
+    check_launch("expand_offsets");
 }
 
 std::vector<int64_t> col_major_strides(const DT& t) {
@@ -263,38 +322,77 @@ DT contract_blocked(Ctx& c, const DT& A, const std::vector<int>& lA, const DT& B
         const int ib = idx_of(lB, x);
         dFB.push_back(B.d[ib]); s1FB.push_back(sB[ib]); s2FB.push_back(sO[idx_of(lOut, x)]); qFB.push_back(&B.q[ib]);
     }
-    const Combos cFA = enumerate(dFA, s1FA, s2FA, qFA, N), cK = enumerate(dK, s1K, s2K, qK, N),
-                 cFB = enumerate(dFB, s1FB, s2FB, qFB, N);
+    const GroupPlan g[3] = {plan_group(dFA, qFA, N), plan_group(dK, qK, N), plan_group(dFB, qFB, N)};
+    const std::vector<int64_t>* st[3][2] = {{&s1FA, &s2FA}, {&s1K, &s2K}, {&s1FB, &s2FB}};
+    // everything the device needs in one upload: per group its strides, per-leg class lists and
+    // tuples of every class (one host-to-device copy per contraction)
+    std::vector<unsigned char> blob;
+    auto put = [&](const void* p, size_t bytes) {
+        const size_t at = (blob.size() + 15) / 16 * 16;
+        blob.resize(at + bytes);
+        if (bytes) std::memcpy(blob.data() + at, p, bytes);
+        return at;
+    };
+    size_t at_st[3], at_lists[3];
+    std::vector<size_t> at_tup[3];
+    for (int q = 0; q < 3; ++q) {
+        at_tup[q].assign(N, 0);
+        int64_t sv[2 * MAXL] = {};
+        for (size_t l = 0; l < st[q][0]->size(); ++l) {
+            sv[l] = (*st[q][0])[l];
+            sv[MAXL + l] = (*st[q][1])[l];
+        }
+        at_st[q] = put(sv, sizeof sv);
+        at_lists[q] = put(g[q].lists.data(), g[q].lists.size() * sizeof(int));
+        for (int cl = 0; cl < N; ++cl)
+            at_tup[q][cl] = put(g[q].tuples[cl].data(), g[q].tuples[cl].size() * sizeof(TupleDesc));
+    }
+    Buf dblob(c.pool.get(), std::max<size_t>(blob.size(), 16));
+    TNR_CUDA(cudaMemcpyAsync(dblob.d(), blob.data(), blob.size(), cudaMemcpyHostToDevice, c.stream));
+    const unsigned char* base = dblob.as<unsigned char>();
+    auto expand = [&](int q, int cl, int64_t* o1, int64_t* o2) {
+        expand_class(c, reinterpret_cast<const TupleDesc*>(base + at_tup[q][cl]), (int)g[q].tuples[cl].size(),
+                     g[q].count[cl], reinterpret_cast<const int*>(base + at_lists[q]), (int)st[q][0]->size(),
+                     reinterpret_cast<const int64_t*>(base + at_st[q]), o1, o2);
+    };
     for (int cl = 0; cl < N; ++cl) {
         const int ncl = (N - cl) % N;
-        std::vector<int64_t> rA, rO, kA, kB, cB, cO;
-        for (size_t e = 0; e < cFA.q.size(); ++e)
-            if (cFA.q[e] == cl) { rA.push_back(cFA.off1[e]); rO.push_back(cFA.off2[e]); }
-        for (size_t e = 0; e < cK.q.size(); ++e)
-            if (cK.q[e] == ncl) { kA.push_back(cK.off1[e]); kB.push_back(cK.off2[e]); }
-        for (size_t e = 0; e < cFB.q.size(); ++e)
-            if (cFB.q[e] == ncl) { cB.push_back(cFB.off1[e]); cO.push_back(cFB.off2[e]); }
-        const int64_t mc = (int64_t)rA.size(), kc = (int64_t)kA.size(), nc = (int64_t)cB.size();
+        const int64_t mc = g[0].count[cl], kc = g[1].count[ncl], nc = g[2].count[ncl];
         if (!mc || !kc || !nc) continue;   // an empty sector contributes nothing (O is zero there)
         Buf ofs(c.pool.get(), (size_t)(2 * mc + 2 * kc + 2 * nc) * sizeof(int64_t));
         int64_t* d = ofs.as<int64_t>();
-        std::vector<int64_t> all;
-        all.reserve(2 * (mc + kc + nc));
-        for (auto* v : {&rA, &rO, &kA, &kB, &cB, &cO}) all.insert(all.end(), v->begin(), v->end());
-        TNR_CUDA(cudaMemcpyAsync(d, all.data(), all.size() * sizeof(int64_t), cudaMemcpyHostToDevice, c.stream));
-        const int64_t *d_rA = d, *d_rO = d + mc, *d_kA = d + 2 * mc, *d_kB = d + 2 * mc + kc,
-                      *d_cB = d + 2 * mc + 2 * kc, *d_cO = d + 2 * mc + 2 * kc + nc;
-        Buf Ab(c.pool.get(), (size_t)mc * kc * sizeof(double)), Bb(c.pool.get(), (size_t)kc * nc * sizeof(double));
-        Buf Cb(c.pool.get(), (size_t)mc * nc * sizeof(double));
-        k_gather_offsets<<<grid_of(mc * kc), 256, 0, c.stream>>>(A.p(), d_rA, mc, d_kA, kc, Ab.d());
+        int64_t *d_rA = d, *d_rO = d + mc, *d_kA = d + 2 * mc, *d_kB = d + 2 * mc + kc,
+                *d_cB = d + 2 * mc + 2 * kc, *d_cO = d + 2 * mc + 2 * kc + nc;
+        expand(0, cl, d_rA, d_rO);
+        expand(1, ncl, d_kA, d_kB);
+        expand(2, ncl, d_cB, d_cO);
+        // The sector GEMM C_c = A_c B_c (mc x kc by kc x nc).  Sector blocks can be thin (a
+        // single Z2 leg of chi = 16 leaves 8 columns), below the tensor-core kernel's limits
+        // (rows >= 64, columns >= 16, K >= 16): in split precision a thin block is computed
+        // transposed when that gives it 64 rows (C_c^T = B_c^T A_c^T), and its columns and K
+        // are zero-padded to 16, rather than falling back to the FP64 pipe.
+        const bool split = bulk && c.precision == TNR_PREC_SPLIT;
+        const bool swap = split && mc < 64 && nc >= 64;
+        const int64_t M = swap ? nc : mc, Nn = swap ? mc : nc;
+        const int64_t *gA_r = swap ? d_cB : d_rA, *gA_c = swap ? d_kB : d_kA;    // rows / K offsets of op "A"
+        const int64_t *gB_r = swap ? d_kA : d_kB, *gB_c = swap ? d_rA : d_cB;    // K / column offsets of op "B"
+        const int64_t *sO_r = swap ? d_cO : d_rO, *sO_c = swap ? d_rO : d_cO;
+        const double* XA = swap ? B.p() : A.p();
+        const double* XB = swap ? A.p() : B.p();
+        const bool pad = split && M >= 64 && (Nn < 16 || kc < 16);
+        const int64_t Np = pad ? std::max<int64_t>(Nn, 16) : Nn, Kp = pad ? std::max<int64_t>(kc, 16) : kc;
+        Buf Ab(c.pool.get(), (size_t)M * Kp * sizeof(double)), Bb(c.pool.get(), (size_t)Kp * Np * sizeof(double));
+        Buf Cb(c.pool.get(), (size_t)M * Np * sizeof(double));
+        if (Kp > kc) TNR_CUDA(cudaMemsetAsync(Ab.d(), 0, (size_t)M * Kp * sizeof(double), c.stream));
+        if (Kp > kc || Np > Nn) TNR_CUDA(cudaMemsetAsync(Bb.d(), 0, (size_t)Kp * Np * sizeof(double), c.stream));
+        k_gather_offsets<<<grid_of(M * kc), 256, 0, c.stream>>>(XA, gA_r, M, gA_c, kc, Ab.d(), M);
         check_launch("gather_offsets");
-        k_gather_offsets<<<grid_of(kc * nc), 256, 0, c.stream>>>(B.p(), d_kB, kc, d_cB, nc, Bb.d());
+        k_gather_offsets<<<grid_of(kc * Nn), 256, 0, c.stream>>>(XB, gB_r, kc, gB_c, Nn, Bb.d(), Kp);
         check_launch("gather_offsets");
-        if (bulk) gemm_bulk(c, false, false, mc, nc, kc, 1.0, Ab.d(), mc, Bb.d(), kc, 0.0, Cb.d(), mc, Batch2(), true);
-        else gemm_f64(c, false, false, mc, nc, kc, 1.0, Ab.d(), mc, Bb.d(), kc, 0.0, Cb.d(), mc, Batch2());
-        k_scatter_offsets<<<grid_of(mc * nc), 256, 0, c.stream>>>(Cb.d(), d_rO, mc, d_cO, nc, O.p());
+        if (bulk) gemm_bulk(c, false, false, M, Np, Kp, 1.0, Ab.d(), M, Bb.d(), Kp, 0.0, Cb.d(), M, Batch2(), true);
+        else gemm_f64(c, false, false, M, Np, Kp, 1.0, Ab.d(), M, Bb.d(), Kp, 0.0, Cb.d(), M, Batch2());
+        k_scatter_offsets<<<grid_of(M * Nn), 256, 0, c.stream>>>(Cb.d(), M, sO_r, M, sO_c, Nn, O.p());
         check_launch("scatter_offsets");
-        // (a host-to-device copy from pageable memory has read `all` when it returns)
     }
     return O;
 }

@@ -337,6 +337,18 @@ void permute(Ctx& c, const double* in, const int64_t* in_dims, int rank, const i
     prof_stop(rec, c.stream, PROF_PERMUTE, 16.0 * total);
 }
 
+DT permuted_scaled(Ctx& c, const DT& A, const std::vector<int>& perm, const double* scale) {
+    std::vector<int64_t> od(A.rank);
+    for (int k = 0; k < A.rank; ++k) od[k] = A.d[perm[k]];
+    DT o = make_dt(c.pool.get(), od);
+    permute(c, A.p(), A.d, A.rank, perm.data(), o.p(), scale);
+    if (A.charged()) {
+        o.N = A.N;
+        for (int k = 0; k < A.rank; ++k) o.q.push_back(A.q[perm[k]]);
+    }
+    return o;
+}
+
 DT permuted(Ctx& c, const DT& A, const std::vector<int>& perm) {
     std::vector<int64_t> od(A.rank);
     for (int k = 0; k < A.rank; ++k) od[k] = A.d[perm[k]];

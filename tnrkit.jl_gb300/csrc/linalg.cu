@@ -346,7 +346,7 @@ static void launch_chol(Ctx& c, double* G, int r, double shift, int batch) {
     int rec = prof_start(c.stream);
     k_chol_inv<T><<<batch, CHOL_THREADS, smem, c.stream>>>(G, r, shift, c.d_status);
     check_launch("chol_inv");
-    prof_stop(rec, c.stream, PROF_CHOL, (double)r * r * r * batch);
+    prof_stop(rec, c.stream, sizeof(T) == 8 ? PROF_CHOL : PROF_CHOL32, (double)r * r * r * batch);
 }
 
 void chol_inv(Ctx& c, double* G, int r, double shift, int batch) { launch_chol<double>(c, G, r, shift, batch); }

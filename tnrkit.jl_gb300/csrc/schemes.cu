@@ -47,6 +47,7 @@ static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B, bool sectors =
         DecompDT d = svd_dt(c, M4, 2, chi);
         A = std::move(d.U);
         B = std::move(d.Vt);
+        if (s.pending) scale_inplace(c, d.s.d(), d.k, s.pending);   // T's folded normalisation
         col_scale(c, A.p(), m, d.k, m, d.s.d(), 1);
         row_scale(c, B.p(), d.k, n, d.k, d.s.d(), 1);
         s.record(d.info);
@@ -57,6 +58,7 @@ static void svd12(Scheme& s, const DT& M4, int chi, DT& A, DT& B, bool sectors =
     B = make_dt(c.pool.get(), {(int64_t)k, M4.d[2], M4.d[3]});
     Buf sv(c.pool.get(), (size_t)k * sizeof(double));
     TsvdOut r = sectors ? tsvd_sectors(c, M4.p(), m, n, k, A.p(), sv.d(), B.p()) : tsvd(c, M4.p(), m, n, k, A.p(), sv.d(), B.p());
+    if (s.pending) scale_inplace(c, sv.d(), k, s.pending);        // T's folded normalisation
     col_scale(c, A.p(), m, k, m, sv.d(), 1);
     row_scale(c, B.p(), k, n, k, sv.d(), 1);
     s.record(r);
@@ -316,6 +318,7 @@ static void step_btrg_charged(Scheme& s, int chi) {
     auto half = [&](const DT& M, DT& U, DT& V, DT& Sn) {
         DecompDT d = svd_dt(c, M, 2, chi);
         const int64_t m = M.d[0] * M.d[1], n = M.d[2] * M.d[3];
+        if (s.pending) scale_inplace(c, d.s.d(), d.k, s.pending);   // T's folded normalisation
         Buf sa(c.pool.get(), (size_t)d.k * sizeof(double));
         Sn = make_dt(c.pool.get(), {(int64_t)d.k});
         pseudopow(c, d.s.d(), d.k, (1.0 - kexp) / 2.0, sa.d());
@@ -361,6 +364,7 @@ static void step_btrg(Scheme& s, int chi) {
     {
         Buf sv(c.pool.get(), (size_t)k1 * sizeof(double)), sa(c.pool.get(), (size_t)k1 * sizeof(double));
         TsvdOut r = tsvd(c, T.p(), m, n, k1, A.p(), sv.d(), B.p());
+        if (s.pending) scale_inplace(c, sv.d(), k1, s.pending);   // T's folded normalisation
         pseudopow(c, sv.d(), k1, (1.0 - kexp) / 2.0, sa.d());
         pseudopow(c, sv.d(), k1, kexp, S1n.p());
         col_scale(c, A.p(), m, k1, m, sa.d(), 0);
@@ -377,6 +381,7 @@ static void step_btrg(Scheme& s, int chi) {
     {
         Buf sv(c.pool.get(), (size_t)k2 * sizeof(double)), sa(c.pool.get(), (size_t)k2 * sizeof(double));
         TsvdOut r = tsvd(c, P.p(), m2, n2, k2, C.p(), sv.d(), D.p());
+        if (s.pending) scale_inplace(c, sv.d(), k2, s.pending);
         pseudopow(c, sv.d(), k2, (1.0 - kexp) / 2.0, sa.d());
         pseudopow(c, sv.d(), k2, kexp, S2n.p());
         col_scale(c, C.p(), m2, k2, m2, sa.d(), 0);
@@ -518,18 +523,22 @@ static DT hotrg_step_x_charged(Ctx& c, const DT& A1, const DT& A2, const DT& Uy)
 // as W2[b,l,e,i,a] = A1p[j,(b,l,e)] Uxp[j,(i,a)];  V[b,l,k,g,a] = W2[(b,l),(e,i)] A2p[(e,i),(k,g)] per a;
 //    O[b,d,g,a] = V[b,(l,k)] Uxq[(l,k),d] per (g,a);  T' = O permuted (a,b,g,d).
 // (A1 and A2 of equal dims: the pure tensor twice for HOTRG, impurity pairs for ImpurityHOTRG)
-static DT hotrg_step_y2(Ctx& c, const DT& A1, const DT& A2, const DT& Ux) {
-    if (A1.charged() && A2.charged() && Ux.charged()) return hotrg_step_y_charged(c, A1, A2, Ux);
+// in_scale: A1 and A2 are read divided by |*in_scale| (a folded normalisation), or NULL
+static DT hotrg_step_y2(Ctx& c, const DT& A1, const DT& A2, const DT& Ux, const double* in_scale = nullptr) {
+    if (A1.charged() && A2.charged() && Ux.charged()) {
+        TNR_REQUIRE(!in_scale, TNR_ERR_INVALID_ARG, "HOTRG: a folded normalisation on the charged path");
+        return hotrg_step_y_charged(c, A1, A2, Ux);
+    }
     const int64_t dL = A1.d[0], dD = A1.d[1], dU = A1.d[2], dR = A1.d[3], kx = Ux.d[2];
     TNR_REQUIRE(Ux.d[0] == dL && Ux.d[1] == dL && dL == dR && dD == dU, TNR_ERR_INVALID_ARG, "HOTRG y-step dims");
     for (int l = 0; l < 4; ++l) TNR_REQUIRE(A2.d[l] == A1.d[l], TNR_ERR_INVALID_ARG, "HOTRG y-step: A1/A2 dims differ");
-    DT A1p = permuted(c, A1, {0, 1, 3, 2});         // [j,b,l,e]
+    DT A1p = permuted_scaled(c, A1, {0, 1, 3, 2}, in_scale);         // [j,b,l,e]
     DT Uxp = permuted(c, Ux, {1, 0, 2});            // [j,i,a]
     const int64_t mW = dD * dR * dU, nW = dL * kx;
     DT W2 = make_dt(c.pool.get(), {dD, dR, dU, dL, kx});
     gemm_bulk(c, true, false, mW, nW, dL, 1.0, A1p.p(), dL, 0, Uxp.p(), dL, 0, 0.0, W2.p(), mW, 0, 1, true);
     A1p = DT(); Uxp = DT();
-    DT A2p = permuted(c, A2, {1, 0, 3, 2});         // [e,i,k,g]
+    DT A2p = permuted_scaled(c, A2, {1, 0, 3, 2}, in_scale);         // [e,i,k,g]
     DT V = make_dt(c.pool.get(), {dD, dR, dR, dU, kx});
     {
         Batch2 bt;
@@ -554,7 +563,7 @@ static DT hotrg_step_y2(Ctx& c, const DT& A1, const DT& A2, const DT& Ux) {
     return permuted(c, O, {3, 0, 2, 1});
 }
 
-static void hotrg_step_y(Scheme& s, const DT& Ux) { s.T = hotrg_step_y2(*s.ctx, s.T, s.T, Ux); }
+static void hotrg_step_y(Scheme& s, const DT& Ux) { s.T = hotrg_step_y2(*s.ctx, s.T, s.T, Ux, s.pending); }
 
 // _step_hotrg_x (src/schemes/hotrg.jl:62-80):
 //   T'[a,b,c,d] = A1[a,i,k,e] A2[e,j,l,d] Uy[i,j,b] Uy[k,l,c]
@@ -877,7 +886,15 @@ void Scheme::step(int chi, double* d_corr) {
 }
 
 // finalize! (src/utility/finalize.jl:4-14,62-66): norm into *d_norm, T /= norm
-void Scheme::finalize_async(double* d_norm) {
+// TRG and BTRG fold T's normalisation into the next step's singular values; HOTRG (dense)
+// into the permutes of its y half step (its projector Grams see T unscaled, which changes
+// their eigenvalues by |n|^-4 and not their eigenvectors)
+bool Scheme::folds_normalisation() const {
+    if (finalizer != FINALIZER_DEFAULT) return false;
+    return kind == TNR_TRG || kind == TNR_BTRG || (kind == TNR_HOTRG && !T.charged());
+}
+
+void Scheme::finalize_async(double* d_norm, bool scale) {
     Ctx& c = *ctx;
     TNR_REQUIRE(kind != TNR_CORRELATION_HOTRG, TNR_ERR_INVALID_ARG,
                 "CorrelationHOTRG finalizes inside step!: run it with tnr_run_correlation");
@@ -901,7 +918,7 @@ void Scheme::finalize_async(double* d_norm) {
         case TNR_ATRG_3D: trace3d(c, T.p(), T.d, d_norm); break;
         default: throw Error(TNR_ERR_INVALID_ARG, "unknown scheme kind");
     }
-    scale_inplace(c, T.p(), T.size(), d_norm);
+    if (scale) scale_inplace(c, T.p(), T.size(), d_norm);
 }
 
 // finalize!(::ImpurityHOTRG) (src/utility/finalize.jl:91-101)
@@ -967,16 +984,45 @@ std::vector<double> Scheme::run(int chi, int maxiter, bool finalize_beginning) {
     const int nsteps = std::max(maxiter, 1);       // the loop body runs before the first check
     const int nn = nsteps + (finalize_beginning ? 1 : 0);
     Buf norms(c.pool.get(), (size_t)nn * sizeof(double));
-    int at = 0;
-    if (finalize_beginning) finalize_async(norms.d() + at++);
-    for (int i = 0; i < nsteps; ++i) {
-        step(chi);
-        finalize_async(norms.d() + at++);
+    const bool fold = folds_normalisation();
+    int at = 0, last_in = -1;                      // last_in: the norm folded into the last step
+    if (finalize_beginning) {
+        finalize_async(norms.d() + at, !fold);
+        if (fold) pending = norms.d() + at;
+        ++at;
     }
+    try {
+        for (int i = 0; i < nsteps; ++i) {
+            last_in = pending ? at - 1 : -1;
+            step(chi);
+            pending = nullptr;
+            finalize_async(norms.d() + at, !fold);
+            if (fold) pending = norms.d() + at;
+            ++at;
+        }
+        if (pending) scale_inplace(c, T.p(), T.size(), pending);   // T normalised when run!() returns
+    } catch (...) {
+        pending = nullptr;
+        throw;
+    }
+    pending = nullptr;
     check_finite(c, norms.d(), nn);
     std::vector<double> h = dvec_to_host(c, norms.d(), nn);
     int st = c.read_status_and_clear();
     TNR_REQUIRE(!(st & ST_NONFINITE), TNR_ERR_NONFINITE, "run!: non-finite norm");
+    if (last_in >= 0) {
+        // the last step decomposed T before its normalisation: its recorded values are in T's
+        // unnormalised scale (singular values |n| times, HOTRG's x-projector Gram |n|^4 times)
+        const double n = std::fabs(h[last_in]);
+        if (kind == TNR_HOTRG) {
+            const double n4 = n * n * n * n;
+            const int k0 = last_counts.empty() ? 0 : last_counts[0];
+            for (int i = 0; i < k0 && i < (int)last_vals.size(); ++i) last_vals[i] /= n4;
+            for (int i = 0; i < 2 && i < (int)last_eps.size(); ++i) last_eps[i] /= n4;
+        } else {
+            for (double& v : last_vals) v /= n;
+        }
+    }
     return h;
 }
 

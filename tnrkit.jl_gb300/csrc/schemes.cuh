@@ -57,6 +57,11 @@ struct Scheme {
     int finalizer = FINALIZER_DEFAULT;
     double btrg_k = -0.5;
     int64_t steps = 0;
+    // run!() folds each step's normalisation into the next step: finalize! leaves T unscaled
+    // and `pending` points at its norm n on the device; the next step's decompositions divide
+    // their singular values by |n| (and HOTRG's permutes read T scaled), so the chi^4 tensor is
+    // never rescaled in a pass of its own.  The last norm is applied when run!() ends.
+    const double* pending = nullptr;
     int64_t max_slice_entries = int64_t(1) << 31;   // HOTRG_3D slicing budget (entries)
     std::vector<double> last_vals; // kept singular values / eigenvalues of the last step
     std::vector<int> last_counts;
@@ -66,7 +71,8 @@ struct Scheme {
     // d_corr: CorrelationHOTRG's three norms of the step (device, may be null)
     void step(int chi, double* d_corr = nullptr);
     std::vector<double> run_correlation(int chi, int maxiter);   // three norms per step
-    void finalize_async(double* d_norm);
+    void finalize_async(double* d_norm, bool scale = true);
+    bool folds_normalisation() const;
     double finalize();
     std::vector<double> run(int chi, int maxiter, bool finalize_beginning);
     // ImpurityHOTRG: the four trace norms (pure, +1, -1, second order) into d4[0..3]; every

@@ -279,11 +279,14 @@ DecompDT decompose_charged(Ctx& c, const DT& M, int nrow, int chi, bool eigh) {
         P.Ub = Buf(c.pool.get(), (size_t)mr * P.kb * sizeof(double));
         Buf sb(c.pool.get(), (size_t)P.kb * sizeof(double));
         TsvdOut r;
+        // a sector block far wider than the values it keeps goes through subspace iteration:
+        // the direct path would run the one-CTA solvers on the whole block
+        const int p = std::min(mr, nc), direct_max = (3 * P.kb + 8 >= p) ? 128 : 64;
         if (eigh) {
-            r = teigh(c, Bm.d(), mr, P.kb, P.Ub.d(), sb.d());
+            r = teigh(c, Bm.d(), mr, P.kb, P.Ub.d(), sb.d(), direct_max);
         } else {
             P.Vb = Buf(c.pool.get(), (size_t)P.kb * nc * sizeof(double));
-            r = tsvd(c, Bm.d(), mr, nc, P.kb, P.Ub.d(), sb.d(), P.Vb.d());
+            r = tsvd(c, Bm.d(), mr, nc, P.kb, P.Ub.d(), sb.d(), P.Vb.d(), direct_max);
         }
         P.vals = r.vals;
         fro2 += r.fro2;

@@ -73,10 +73,96 @@ struct tnr_server_s {
     std::vector<std::thread> workers;
     int dev = 0;
 
+    // Requests that can step in lockstep: TRG / BTRG on uncharged tensors with equal legs, chi,
+    // maxiter and k (the server's precision is shared).  Such requests admitted together run as
+    // one lockstep batch (tnr_run_batch: batched GEMMs, one CTA per member in the small solvers).
+    static bool batchable(const Request* r) {
+        return (r->kind == TNR_TRG || r->kind == TNR_BTRG) && r->symmetry_n <= 1;
+    }
+    static bool same_group(const Request* a, const Request* b) {
+        return batchable(a) && batchable(b) && a->kind == b->kind && a->dims == b->dims && a->chi == b->chi &&
+               a->maxiter == b->maxiter && std::memcmp(&a->btrg_k, &b->btrg_k, sizeof(double)) == 0;
+    }
+    static constexpr int MAX_GROUP = 64;
+
+    // a handle for request r (its status and message on failure)
+    tnr_handle create_for(Request* r) {
+        tnr_handle h = nullptr;
+        tnr_options o;
+        tnr_default_options(&o);
+        o.precision = precision;
+        o.btrg_k = r->btrg_k;
+        if (r->symmetry_n > 1) {
+            o.symmetry_n = r->symmetry_n;
+            o.leg_charges = r->charges.data();
+        }
+        const int st = tnr_create(&h, r->kind, (int)r->dims.size(), r->dims.data(), r->data.data(), &o);
+        if (st != TNR_OK) {
+            char buf[512];
+            tnr_last_error(nullptr, buf, sizeof buf);
+            r->status = st;
+            r->err = buf;
+            if (h) tnr_destroy(h);
+            return nullptr;
+        }
+        return h;
+    }
+
+    void run_one(Request* r) {
+        tnr_handle h = create_for(r);
+        if (!h) return;
+        const size_t cap = (size_t)std::max(r->maxiter, 1) + 1;
+        r->norms.resize(cap);
+        size_t n = 0;
+        int st = tnr_run(h, r->chi, r->maxiter, 1, r->norms.data(), cap, &n);
+        r->norms.resize(n);
+        if (st != TNR_OK) {
+            char buf[512];
+            tnr_last_error(h, buf, sizeof buf);
+            r->err = buf;
+        }
+        tnr_destroy(h);
+        r->status = st;
+    }
+
+    void run_group_of(std::vector<Request*>& grp) {
+        std::vector<tnr_handle> hs;
+        std::vector<Request*> live;
+        for (Request* r : grp) {
+            tnr_handle h = create_for(r);
+            if (h) {
+                hs.push_back(h);
+                live.push_back(r);
+            }
+        }
+        if (hs.empty()) return;
+        const int n = (int)hs.size();
+        const size_t stride = (size_t)std::max(live[0]->maxiter, 1) + 1;
+        std::vector<int> chis(n, live[0]->chi), its(n, live[0]->maxiter);
+        std::vector<double> norms(stride * n);
+        std::vector<size_t> counts(n, 0);
+        const int st = tnr_run_batch(hs.data(), n, chis.data(), its.data(), 1, norms.data(), stride, counts.data(),
+                                     nullptr, nullptr);
+        std::string msg;
+        if (st != TNR_OK) {
+            char buf[512];
+            tnr_last_error(nullptr, buf, sizeof buf);
+            msg = buf;
+        }
+        for (int i = 0; i < n; ++i) {
+            Request* r = live[i];
+            r->status = st;
+            r->err = msg;
+            if (st == TNR_OK) r->norms.assign(norms.begin() + (size_t)i * stride, norms.begin() + (size_t)i * stride + counts[i]);
+            tnr_destroy(hs[i]);
+        }
+    }
+
     void worker() {
         cudaSetDevice(dev);
         for (;;) {
-            Request* r = nullptr;
+            std::vector<Request*> grp;
+            size_t grp_bytes = 0;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 // admit the oldest queued request that fits the free budget (first fit)
@@ -101,44 +187,38 @@ struct tnr_server_s {
                 }
                 for (auto it = queue.begin(); it != queue.end(); ++it)
                     if ((*it)->footprint <= budget - in_use) {
-                        r = *it;
+                        grp.push_back(*it);
+                        grp_bytes = (*it)->footprint;
                         queue.erase(it);
                         break;
                     }
-                in_use += r->footprint;
+                // continuous batching: queued requests that can step in lockstep with it join it,
+                // as far as the free budget allows
+                for (auto it = queue.begin(); it != queue.end() && (int)grp.size() < MAX_GROUP;) {
+                    if (same_group(grp[0], *it) && grp_bytes + (*it)->footprint <= budget - in_use) {
+                        grp_bytes += (*it)->footprint;
+                        grp.push_back(*it);
+                        it = queue.erase(it);
+                    } else {
+                        ++it;
+                    }
+                }
+                in_use += grp_bytes;
                 ++active;
             }
-            r->t_start = Clock::now();
-            tnr_handle h = nullptr;
-            tnr_options o;
-            tnr_default_options(&o);
-            o.precision = precision;
-            o.btrg_k = r->btrg_k;
-            if (r->symmetry_n > 1) {
-                o.symmetry_n = r->symmetry_n;
-                o.leg_charges = r->charges.data();
-            }
-            int st = tnr_create(&h, r->kind, (int)r->dims.size(), r->dims.data(), r->data.data(), &o);
-            if (st == TNR_OK) {
-                const size_t cap = (size_t)std::max(r->maxiter, 1) + 1;
-                r->norms.resize(cap);
-                size_t n = 0;
-                st = tnr_run(h, r->chi, r->maxiter, 1, r->norms.data(), cap, &n);
-                r->norms.resize(n);
-            }
-            if (st != TNR_OK) {
-                char buf[512];
-                tnr_last_error(h, buf, sizeof buf);
-                r->err = buf;
-            }
-            if (h) tnr_destroy(h);
-            r->status = st;
-            r->t_done = Clock::now();
+            const auto t0 = Clock::now();
+            for (Request* r : grp) r->t_start = t0;
+            if (grp.size() == 1) run_one(grp[0]);
+            else run_group_of(grp);
+            const auto t1 = Clock::now();
             {
                 std::lock_guard<std::mutex> lk(mu);
-                in_use -= r->footprint;
+                for (Request* r : grp) {
+                    r->t_done = t1;
+                    r->done = true;
+                }
+                in_use -= grp_bytes;
                 --active;
-                r->done = true;
             }
             cv.notify_all();
             cv_done.notify_all();

@@ -212,13 +212,13 @@ static bool debug_on() {
 #endif
 static double target_angle(Ctx& c) { return c.precision == TNR_PREC_F64 ? TNR_TARGET_F64 : 1e-9; }
 
-TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt) {
+TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt, int direct_max) {
     TsvdOut out;
     const int64_t p = std::min(m, n);
     k = (int)std::min<int64_t>(k, p);
     out.k = k;
     if (k <= 0) return out;
-    if (p <= RDIRECT) {
+    if (p <= std::min(RDIRECT, direct_max)) {
         const int pp = (int)p;
         const bool wide = m < n;
         const int64_t rows = wide ? n : m;               // X = M (tall) or M^T
@@ -312,13 +312,13 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
     return out;
 }
 
-TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk) {
+TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk, int direct_max) {
     TsvdOut out;
     k = (int)std::min<int64_t>(k, n);
     out.k = k;
     if (k <= 0) return out;
     sum_squares(c, M, n * n, c.d_scalar);
-    if (n <= RDIRECT) {
+    if (n <= std::min(RDIRECT, direct_max)) {
         const int nn = (int)n;
         Buf W(c.pool.get(), (size_t)nn * nn * sizeof(double));
         Buf l(c.pool.get(), (size_t)nn * sizeof(double));

@@ -84,6 +84,24 @@ norms_per_entry(g) = g.kind == TNR_IMPURITY_HOTRG ? 4 : g.kind == TNR_IMPURITY_T
 
 btrg_k(scheme) = scheme isa TNRKit.BTRG ? scheme.k : -0.5
 
+# Z_N charges of a symmetric tensor for the block-sparse path: the charge of every basis
+# index of every leg (codomain legs, then domain legs), in the order of the dense embedding
+# `convert(Array, t)` (sector by sector, each repeated dim(V, c) times).  A Trivial tensor
+# gives (nothing, 1).
+zn_order(::Type{TensorKit.ZNIrrep{N}}) where {N} = N
+zn_order(::Type) = 1
+function leg_charges(t)
+    N = zn_order(TensorKit.sectortype(t))
+    N > 1 || return nothing, 1
+    qs = Int32[]
+    for V in (TensorKit.codomain(t)..., TensorKit.domain(t)...)
+        for c in TensorKit.sectors(V)
+            append!(qs, fill(Int32(mod(c.n, N)), TensorKit.dim(V, c)))
+        end
+    end
+    return qs, N
+end
+
 mutable struct GPU{S} <: TNRScheme{Float64, Any}
     scheme::S
     handle::Ptr{Cvoid}
@@ -96,9 +114,15 @@ mutable struct GPU{S} <: TNRScheme{Float64, Any}
         opts = Ref(Options(precision, k, 1, Ptr{Int32}(C_NULL), UInt64(seed), C_NULL))
         h = Ref{Ptr{Cvoid}}(C_NULL)
         if kind <= TNR_HOTRG_3D || kind >= TNR_ATRG
-            st = ccall((:tnr_create, libtnr), Cint,
-                (Ptr{Ptr{Cvoid}}, Cint, Cint, Ptr{Int64}, Ptr{Float64}, Ref{Options}),
-                h, kind, length(dims), dims, arr, opts)
+            qs, N = leg_charges(scheme isa TNRKit.CorrelationHOTRG ? scheme.Tpure : scheme.T)
+            st = GC.@preserve qs begin
+                if qs !== nothing
+                    opts = Ref(Options(precision, k, N, pointer(qs), UInt64(seed), C_NULL))
+                end
+                ccall((:tnr_create, libtnr), Cint,
+                    (Ptr{Ptr{Cvoid}}, Cint, Cint, Ptr{Int64}, Ptr{Float64}, Ref{Options}),
+                    h, kind, length(dims), dims, arr, opts)
+            end
         else
             imps = map(dense_array, impurity_tensors(scheme))
             if kind == TNR_IMPURITY_HOTRG
@@ -275,9 +299,17 @@ function submit!(s::Server, scheme::TNRScheme, chi::Integer, maxiter::Integer)
     arr = dense_tensor(scheme)
     dims = Int64[size(arr)...]
     id = Ref{UInt64}(0)
-    check(ccall((:tnr_server_submit, libtnr), Cint,
-        (Ptr{Cvoid}, Cint, Cint, Ptr{Int64}, Ptr{Float64}, Cint, Cint, Cdouble, Ref{UInt64}),
-        s.ptr, scheme_kind(scheme), length(dims), dims, arr, chi, maxiter, btrg_k(scheme), id))
+    qs, N = leg_charges(scheme.T)
+    if qs === nothing
+        check(ccall((:tnr_server_submit, libtnr), Cint,
+            (Ptr{Cvoid}, Cint, Cint, Ptr{Int64}, Ptr{Float64}, Cint, Cint, Cdouble, Ref{UInt64}),
+            s.ptr, scheme_kind(scheme), length(dims), dims, arr, chi, maxiter, btrg_k(scheme), id))
+    else
+        # a Z_N request runs block by block over its charge sectors
+        check(ccall((:tnr_server_submit_sym, libtnr), Cint,
+            (Ptr{Cvoid}, Cint, Cint, Ptr{Int64}, Ptr{Float64}, Cint, Ptr{Int32}, Cint, Cint, Cdouble, Ref{UInt64}),
+            s.ptr, scheme_kind(scheme), length(dims), dims, arr, N, qs, chi, maxiter, btrg_k(scheme), id))
+    end
     return id[]
 end
 
