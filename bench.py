@@ -53,7 +53,8 @@ def parse():
                         "gemm times one batched split-precision product (the target of kernel captures)")
     p.add_argument("--gemm", default="contract", choices=["contract", "single"],
                    help="gemm workload: contraction path (chunked accumulation) or single accumulation")
-    p.add_argument("--m", type=int, default=2304, help="gemm workload: m = n")
+    p.add_argument("--m", type=int, default=2304, help="gemm workload: m")
+    p.add_argument("--n", type=int, default=0, help="gemm workload: n (0: n = m)")
     p.add_argument("--k", type=int, default=2304, help="gemm workload: k")
     p.add_argument("--batch", type=int, default=4, help="gemm workload: batch")
     p.add_argument("--chis", default=None, help="comma-separated chi list for hotrg_step / hotrg3d")
@@ -559,15 +560,18 @@ def run_other_configs(args, tnr):
 
 
 def run_gemm(args, tnr):
-    """One warm-up and ``--steps`` timed batched m x m x k split-precision products on seeded,
+    """One warm-up and ``--steps`` timed batched m x n x k split-precision products on seeded,
     device-resident operands: the contraction path (chunked accumulation when k > 64) or the
     single-accumulation kernel of the truncated SVD's products."""
     contraction = args.gemm == "contract"
     m, k, b = args.m, args.k, args.batch
-    ms = tnr.gemm_time(m, m, k, b, False, False, tnr.PREC_SPLIT, max(args.steps, 1), contraction)
-    return {"workload": "gemm: %s m=n=%d k=%d batch=%d (split precision, plane pass included)" % (
-                args.gemm, m, k, b),
-            "ms": ms, "tflops_2mnk": 2.0 * m * m * k * b / (ms * 1e-3) / 1e12}
+    n = args.n or m
+    prec = tnr.PREC_SPLIT if args.precision == "split" else tnr.PREC_F64
+    ms = tnr.gemm_time(m, n, k, b, False, False, prec, max(args.steps, 1), contraction)
+    shape = ("m=n=%d" % m) if n == m else ("m=%d n=%d" % (m, n))
+    return {"workload": "gemm: %s %s k=%d batch=%d (%s)" % (
+                args.gemm, shape, k, b, "split precision, plane pass included" if prec == tnr.PREC_SPLIT else "FP64"),
+            "ms": ms, "tflops_2mnk": 2.0 * m * n * k * b / (ms * 1e-3) / 1e12}
 
 
 def main():

@@ -175,6 +175,12 @@ int tnr_btrg_bonds(tnr_handle h, double* s1, size_t cap1, size_t* n1,
 /* Bytes of device memory the scheme holds now (tensor + workspace). */
 int tnr_device_bytes(tnr_handle h, size_t* bytes_out);
 
+/* Statistics of the truncated decompositions run on this handle since it was created:
+ * how many, how many of them the spectral-gap fallback decomposed in full FP64 (the
+ * subspace iteration could not resolve the gap at chi), and the most subspace iterations
+ * one of them took.  Any pointer may be NULL.  No reference counterpart (diagnostic). */
+int tnr_decomposition_stats(tnr_handle h, uint64_t* decompositions, uint64_t* gap_fallbacks, int* max_iters);
+
 int  tnr_destroy(tnr_handle h);
 int  tnr_last_error(tnr_handle h, char* buf, size_t cap); /* h may be NULL: global */
 const char* tnr_status_string(int status);
@@ -285,8 +291,8 @@ int tnr_gemm_time(int precision, int ta, int tb, int64_t m, int64_t n, int64_t k
  * where cudaMalloc's implicit device synchronisation stalls other streams).
  *   - limits: m >= 64, n >= 16, k >= 16 and 6 * (m + n) * ceil8(k) bytes <= 16 MiB;
  *     larger operands are rejected with TNR_ERR_INVALID_ARG and a message in err;
- *   - the first call on a device resolves the scratch's device address with that
- *     device current; make that first call before any stream capture;
+ *   - the first call on a device resolves the scratch's device address and sets the
+ *     kernel's shared-memory limit with that device current;
  *   - every call shares the one scratch array: calls that overlap on the GPU
  *     (different streams, different host threads) race; serialise them;
  *   - runs on `stream` (NULL = legacy default stream) and returns after

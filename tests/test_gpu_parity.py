@@ -365,3 +365,48 @@ def test_chol_inv_kernel(tnr, precision):
     G[17, 17] = -1.0
     _, bad = tnr.debug_chol(G, 0.0, prec)
     assert bad
+
+
+
+@pytest.mark.parametrize("precision", ["f64", "split"])
+def test_gap_fallback_flat_spectrum(tnr, oracle, flat_spectrum_tensor, precision):
+    """Spectral-gap fallback: a TRG tensor (d = 12) whose first decomposition is near-flat at
+    chi = 24 (sigma_24 / sigma_25 - 1 = 1e-5) is decomposed in full FP64 (the exact one-CTA
+    Jacobi path for the 144 x 144 matrix) in both precisions, and the handle reports it.
+    One step: the first decomposition's kept singular values equal the oracle's (LAPACK SVD)
+    to 1e-10 of the largest in both precisions, the second's in FP64 (in split precision it
+    may iterate on split products).  Norms over two steps: 2e-9 in FP64, where a
+    1e-14 perturbation of the input moves the oracle's own norms by up to 5e-10
+    (test_oracle_conditioning.py); 1e-6 in split precision, the bound of its contractions'
+    products (6e-8 sqrt(K) at K = 576)."""
+    o = oracle
+    a = flat_spectrum_tensor(12, 1e-5, 3)
+    prec = tnr.PREC_F64 if precision == "f64" else tnr.PREC_SPLIT
+    s = tnr.TRG(a, precision=prec)
+    tnr.run(s, tnr.truncrank(24), tnr.maxiter(1))
+    so = o.TRG(o.Tensor(a, 2, None, 1))
+    o.run(so, o.truncrank(24), o.maxiter(1))
+    ndec, nfall, _ = s.decomposition_stats()
+    assert ndec == 2 and nfall >= 1, (ndec, nfall)
+    got, ref = s.singular_values(), so.svals[-2:]
+    for g, r in list(zip(got, ref))[:2 if precision == "f64" else 1]:
+        r = np.asarray(r)
+        assert len(g) == len(r) == 24
+        np.testing.assert_allclose(g, r, rtol=0, atol=SVAL_TOL * abs(r[0]))
+    s2 = tnr.TRG(a, precision=prec)
+    d = np.array(tnr.run(s2, tnr.truncrank(24), tnr.maxiter(2)))
+    do = np.array(o.run(o.TRG(o.Tensor(a, 2, None, 1)), o.truncrank(24), o.maxiter(2)))
+    np.testing.assert_allclose(d, do, rtol=2e-9 if precision == "f64" else 1e-6)
+
+
+def test_gap_fallback_in_lockstep_group(tnr, oracle, flat_spectrum_tensor):
+    """A lockstep group whose members include a flat-spectrum tensor: that member alone is
+    decomposed again by the FP64 gap fallback and its norms equal the oracle's to 2e-9 (the
+    problem's conditioning, as above); the other member's norms equal its single run's."""
+    o = oracle
+    ts = [flat_spectrum_tensor(12, 1e-5, 3), np.random.default_rng(11).standard_normal((12,) * 4)]
+    out = tnr.run_batch([tnr.TRG(t) for t in ts], [24, 24], [2, 2])
+    do = o.run(o.TRG(o.Tensor(ts[0], 2, None, 1)), o.truncrank(24), o.maxiter(2))
+    np.testing.assert_allclose(out[0], do, rtol=2e-9)
+    single = tnr.run(tnr.TRG(ts[1]), tnr.truncrank(24), tnr.maxiter(2))
+    np.testing.assert_allclose(out[1], single, rtol=NORM_RTOL)

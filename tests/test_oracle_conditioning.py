@@ -67,3 +67,20 @@ def test_high_temperature_free_energy_is_well_conditioned(oracle, beta):
     T.a = T.a * (1 + 1e-14 * rng.standard_normal(T.a.shape))
     f1 = o.free_energy(o.run(o.BTRG(T), o.truncrank(16), o.maxiter(30)), beta)
     assert abs(f1 / f0 - 1) < 1e-13
+
+
+def test_flat_spectrum_tensor_conditioning(oracle, flat_spectrum_tensor):
+    """The gap-fallback GPU case (TRG, d = 12, sigma_i = 1 - 1e-5 i, truncrank(24), 2 steps):
+    a 1e-14 relative perturbation of the input moves the oracle's norms by more than 1e-11 (a
+    gap of 1e-5 at the cut) and by less than 2e-9, the GPU test's FP64 tolerance."""
+    o = oracle
+    a = flat_spectrum_tensor(12, 1e-5, 3)
+    n0 = np.array(o.run(o.TRG(o.Tensor(a, 2, None, 1)), o.truncrank(24), o.maxiter(2)))
+    rng = np.random.default_rng(99)
+    moves = []
+    for _ in range(4):
+        ap = a * (1 + 1e-14 * rng.standard_normal(a.shape))
+        n1 = np.array(o.run(o.TRG(o.Tensor(ap, 2, None, 1)), o.truncrank(24), o.maxiter(2)))
+        moves.append(float(np.abs(n1 / n0 - 1).max()))
+    assert max(moves) > 1e-11, moves
+    assert max(moves) < 2e-9, moves

@@ -39,7 +39,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "iterati
 
 EXPORTS = ["tnr_default_options", "tnr_create", "tnr_create_device", "tnr_step", "tnr_finalize", "tnr_run",
            "tnr_free_energy", "tnr_get_tensor", "tnr_singular_values", "tnr_truncation_errors", "tnr_btrg_bonds",
-           "tnr_device_bytes", "tnr_destroy", "tnr_last_error", "tnr_status_string", "tnr_timer_start",
+           "tnr_device_bytes", "tnr_decomposition_stats", "tnr_destroy", "tnr_last_error", "tnr_status_string", "tnr_timer_start",
            "tnr_timer_stop", "tnr_run_batch", "tnr_device_info", "tnr_version", "tnr_kernel_launches",
            "tnr_profile_enable", "tnr_profile_reset", "tnr_profile_read", "tnr_debug_gemm", "tnr_gemm_time",
            "tnr_gemm_split_noalloc", "tnr_server_create", "tnr_server_submit", "tnr_server_submit_sym",
@@ -101,6 +101,7 @@ def lib():
         "tnr_truncation_errors": (I, [P, pd, Z, pz]),
         "tnr_btrg_bonds": (I, [P, pd, Z, pz, pd, Z, pz]),
         "tnr_device_bytes": (I, [P, pz]),
+        "tnr_decomposition_stats": (I, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(I)]),
         "tnr_destroy": (I, [P]),
         "tnr_last_error": (I, [P, C.c_char_p, Z]),
         "tnr_status_string": (C.c_char_p, [I]),
@@ -284,6 +285,12 @@ class _Scheme:
         b = C.c_size_t()
         _check(lib().tnr_device_bytes(self._h, C.byref(b)), self._h)
         return b.value
+
+    def decomposition_stats(self):
+        """(decompositions, gap fallbacks decomposed in full FP64, most subspace iterations)."""
+        nd, nf, mi = C.c_uint64(), C.c_uint64(), C.c_int()
+        _check(lib().tnr_decomposition_stats(self._h, C.byref(nd), C.byref(nf), C.byref(mi)), self._h)
+        return nd.value, nf.value, mi.value
 
     def close(self):
         if getattr(self, "_h", None):

@@ -443,6 +443,15 @@ int tnr_device_bytes(tnr_handle h, size_t* bytes_out) {
     return TNR_OK;
 }
 
+int tnr_decomposition_stats(tnr_handle h, uint64_t* decompositions, uint64_t* gap_fallbacks, int* max_iters) {
+    if (!h) return fail(h, TNR_ERR_INVALID_ARG, "NULL handle");
+    const Ctx& c = *h->s.ctx;
+    if (decompositions) *decompositions = c.decompositions;
+    if (gap_fallbacks) *gap_fallbacks = c.gap_fallbacks;
+    if (max_iters) *max_iters = c.max_iters;
+    return TNR_OK;
+}
+
 int tnr_destroy(tnr_handle h) {
     if (!h) return TNR_OK;
     int st = guarded(nullptr, [&] { h->s.ctx->sync(); });

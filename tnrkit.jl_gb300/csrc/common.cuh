@@ -16,6 +16,40 @@
 
 namespace tnr {
 
+#ifdef __CUDACC__
+// FP32 <-> FP64 conversions with integer operations only: FP64 arithmetic, conversions
+// included, runs at a small fraction of the FP32 rate on this part.
+// FP32 -> FP64: exponent rebias and mantissa shift; FP32 subnormals (below 2^-126) become
+// signed zero, infinities and NaNs keep their class.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu, mant = u & 0x7FFFFFu, sign = u & 0x80000000u;
+    const uint32_t e64 = e == 255u ? 2047u : e + 896u;
+    const uint32_t hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
+    const uint32_t lo = e == 0u ? 0u : (mant << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// FP64 -> FP32, rounded to nearest (ties to even) on the 29 dropped mantissa bits; |x| below
+// 2^-126 becomes signed zero, |x| beyond the FP32 range infinity, NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi = (uint32_t)(u >> 32), lo = (uint32_t)u;
+    const uint32_t sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    if (e <= 896) return __uint_as_float(sign);
+    if (e >= 1151) {
+        const bool nan = e == 2047 && (((hi & 0xFFFFFu) | lo) != 0u);
+        return __uint_as_float(sign | 0x7F800000u | (nan ? 0x00400000u : 0u));
+    }
+    const uint32_t m23 = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const uint32_t rem = lo & 0x1FFFFFFFu;
+    uint32_t bits = ((uint32_t)(e - 896) << 23) | m23;
+    if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) bits += 1u;   // a carry moves the exponent
+    return __uint_as_float(sign | bits);
+}
+#endif
+
 // ---------------------------------------------------------------------------
 // errors: C++ exceptions inside the library, status codes at the C ABI
 // ---------------------------------------------------------------------------
@@ -190,8 +224,12 @@ struct Ctx {
     int* d_status = nullptr;       // device status word
     double* d_scalar = nullptr;    // small device scratch (norms, reductions)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // statistics of the last decompositions
+    // statistics of the decompositions
     int last_iters = 0;
+    uint64_t decompositions = 0;   // truncated SVDs / eigendecompositions run
+    uint64_t gap_fallbacks = 0;    // of them, decomposed in full FP64 for a too small gap
+    int max_iters = 0;             // most subspace iterations of one of them
+    bool exact_jacobi = false;     // the gap fallback: FP64 Jacobi converged to 1e-15
     bool bulk_call = false;        // the FP64 GEMM in flight serves a bulk contraction
     Ctx(cudaStream_t s, int prec, uint64_t seed_);
     ~Ctx();
@@ -232,6 +270,9 @@ void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double
 // subspace iterations of the truncated SVD / eigensolver from sigma estimates (tsvd.cu)
 int iterations_needed(std::vector<double> v, int k, int r, int power, double target, int cap);
 int iteration_cap(const Ctx& c);
+// the estimates say the gap at k is too small for the subspace iteration (tsvd.cu)
+bool gap_too_small(const Ctx& c, std::vector<double> v, int k, int r, int power, double target, int cap);
+
 void sigma_estimates(Ctx& c, const double* X, int64_t n, int r, int B, double* G, double* W, double* Xa, double* lam);
 
 // K blocks per accumulation chunk of the contraction GEMMs in split precision
@@ -269,6 +310,10 @@ bool split_a_build(Ctx& c, SplitA& P, bool ta, const double* A, int64_t lda, int
 // batch > 1: `batch` matrices strideG apart; W (r x r) and lam (r) outputs packed per matrix
 void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch = 1,
                  int64_t strideG = 0);
+// the same with the FP64 rotation thresholds given: rotate (p, q) while |g_pq| > max(rel sqrt|g_pp g_qq|,
+// floor |G|_F) (jacobi_eigh: rel 1e-12, floor 1e-22)
+void jacobi_eigh_tol(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch,
+                     int64_t strideG, double rel, double floor);
 // G <- Cholesky factor inverse: on exit Linv (lower) with (G + shift I) = L L^T; returns via status
 void chol_inv(Ctx& c, double* G, int r, double shift, int batch = 1);
 // FP32 versions (one SM runs FP32 at 64x its FP64 rate): results returned in FP64 buffers
@@ -321,6 +366,10 @@ struct TsvdOut {
     int iters = 0;
     std::vector<double> vals;  // kept values (host copy)
 };
+
+// the gap fallback of one m x n matrix: decomposed exactly in FP64 (min(m, n) <= 160) or
+// iterated in FP64 on a 160-wide subspace; outputs as tsvd's
+TsvdOut tsvd_gap_fallback(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt);
 
 // M (m x n, ld = m, column-major): U (m x k), s (k), Vt (k x n)
 // direct_max: largest min(m, n) decomposed directly (one-CTA solvers on the whole matrix) rather

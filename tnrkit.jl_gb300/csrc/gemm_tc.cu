@@ -2,17 +2,19 @@
 //
 // C (FP64) = alpha * op(A) op(B) + beta * C with every FP64 operand split into three
 // BF16 planes x = x0 + x1 + x2 (each the BF16 rounding of the previous residual).
-// Six plane products x_i y_j with i + j <= 2 are accumulated in an FP32 accumulator
-// in tensor memory (TMEM): about 24 bits of each operand and FP32 accumulation,
-// smallest terms first, the leading x0 y0 last.  The contractions of a coarse-graining
+// Six plane products x_i y_j with i + j <= 2 are accumulated in FP32 in tensor memory
+// (TMEM): about 24 bits of each operand and FP32 accumulation, the five small products
+// in one accumulator and the leading x0 y0 in another, added once at the end.  The contractions of a coarse-graining
 // step use the chunked variant below (unbiased accumulation over long K).
 //
 //  * split pass: FP64 -> BF16 planes in a K-major [batch][plane][rows][Kp] layout
 //    (shared-memory tiled transpose where the source is not K-contiguous);
-//  * GEMM: 128 x BN tile per CTA, TMA loads with 128-byte swizzle into a
-//    STAGES-deep mbarrier pipeline, one thread issues tcgen05.mma (kind::f16,
-//    M=128, K=16), tcgen05.commit frees stages, the four warps read the FP32
-//    accumulator with tcgen05.ld and write FP64 C (coalesced along the rows).
+//  * GEMM: 128 x BN tile per CTA.  A pipeline stage holds one K block of 32 of all
+//    three planes of both operands (two TMA loads of 3 x 8 KB, 64-byte swizzle), so
+//    every plane is fetched from L2 once for the six products that use it; a
+//    STAGES-deep mbarrier ring, one thread issues tcgen05.mma (kind::f16, M=128,
+//    K=16), tcgen05.commit frees stages, the four warps read the FP32 accumulators
+//    with tcgen05.ld and write FP64 C (coalesced along the rows).
 // Every wait is bounded by a 2-second global-timer limit and reports through the
 // context status word instead of hanging.
 #include "common.cuh"
@@ -30,16 +32,21 @@ namespace tnr {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3, NTHREADS = 128;
-constexpr int TILE_A_BYTES = BM * BK * 2;   // 16 KB
-constexpr int TILE_B_BYTES = BN * BK * 2;   // 16 KB
-constexpr int STAGE_BYTES = TILE_A_BYTES + TILE_B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 4, NTHREADS = 128;
+constexpr int PLANES = 3;
+constexpr int TILE_A_BYTES = BM * BK * 2;                       // 8 KB: one plane of A
+constexpr int TILE_B_BYTES = BN * BK * 2;                       // 8 KB: one plane of B
+constexpr int STAGE_A_BYTES = PLANES * TILE_A_BYTES;            // 24 KB
+constexpr int STAGE_BYTES = PLANES * (TILE_A_BYTES + TILE_B_BYTES);   // 48 KB
+// tiles | barriers | slack: the slack keeps every shared-memory descriptor of the MMAs inside
+// the CTA's allocation even past the last tile
+constexpr int SMEM_TAIL = 256 /*barriers*/ + 8192 /*slack*/;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + SMEM_TAIL;
 constexpr int NTERMS = 6;
 
-// plane pairs, smallest contributions first
-__constant__ int c_pa[NTERMS] = {2, 1, 0, 1, 0, 0};
-__constant__ int c_pb[NTERMS] = {0, 1, 2, 0, 1, 0};
+// plane pairs, smallest contributions first; the last (x0 y0) goes to its own accumulator
+__host__ __device__ constexpr int term_pa(int t) { return t == 0 ? 2 : (t == 1 || t == 3) ? 1 : 0; }
+__host__ __device__ constexpr int term_pb(int t) { return t == 2 ? 2 : (t == 1 || t == 4) ? 1 : 0; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -91,14 +98,15 @@ __device__ __forceinline__ void tma_load_4d(const CUtensorMap* map, uint64_t* ba
         : "memory");
 }
 
-// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+// tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of BK = 32 BF16),
+// 8-row groups 512 B apart; tiles start 1024-byte aligned (matrix base offset 0)
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     uint64_t d = 0;
     d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
     d |= (uint64_t)1 << 16;                          // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)(512 >> 4) << 32;                 // stride byte offset: 8 rows x 64 B
     d |= (uint64_t)1 << 46;                          // descriptor version (fixed 0b001)
-    d |= (uint64_t)2 << 61;                          // swizzle: 128 B
+    d |= (uint64_t)4 << 61;                          // swizzle: 64 B
     return d;
 }
 
@@ -129,22 +137,10 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// FP32 -> FP64 with integer operations only (FP64 arithmetic is scarce on this part):
-// exponent rebias and mantissa shift; FP32 subnormals (below 2^-126) become signed zero,
-// infinities and NaNs keep their class.
-__device__ __forceinline__ double f32_to_f64(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xFFu, mant = u & 0x7FFFFFu, sign = u & 0x80000000u;
-    const uint32_t e64 = e == 255u ? 2047u : e + 896u;
-    const uint32_t hi = e == 0u ? sign : (sign | (e64 << 20) | (mant >> 3));
-    const uint32_t lo = e == 0u ? 0u : (mant << 29);
-    return __hiloint2double((int)hi, (int)lo);
-}
-
 struct TcArgs {
     int64_t m, n;
-    int nkb;            // K blocks of 64 in this launch
-    int kb0;            // first K block (chunked accumulation)
+    int nkb;            // K blocks of BK = 32 in this launch
+    int kb0;            // first K block
     double alpha, beta;
     double* C;
     int64_t ldc;
@@ -168,7 +164,7 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile_m = blockIdx.x, tile_n = blockIdx.y, b = blockIdx.z;
-    const int niter = NTERMS * a.nkb;
+    const int niter = a.nkb;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -181,8 +177,9 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
     }
     if (warp == 0) {
+        // two accumulators: the five small plane products, and x0 y0
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(BN));
+                     "r"(2 * BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -192,22 +189,22 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     bool ok = true;
 
     if (warp == 0 && lane == 0) {
-        // TMA producer
+        // TMA producer: one K block of all three planes of A and of B per stage
         const int ab = a.a_batched ? b : 0, bb = a.b_batched ? b : 0;
         for (int it = 0; it < niter && ok; ++it) {
             const int s = it % STAGES;
             const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
             ok = mbar_wait(&empty[s], ph ^ 1u, a.status);
             if (!ok) break;
-            const int t = it / a.nkb, kb = it % a.nkb;
             unsigned char* sa = tiles + s * STAGE_BYTES;
-            unsigned char* sb = sa + TILE_A_BYTES;
+            unsigned char* sb = sa + STAGE_A_BYTES;
             mbar_expect_tx(&full[s], STAGE_BYTES);
-            tma_load_4d(&tmA, &full[s], sa, (a.kb0 + kb) * BK, tile_m * BM, c_pa[t], ab);
-            tma_load_4d(&tmB, &full[s], sb, (a.kb0 + kb) * BK, tile_n * BN, c_pb[t], bb);
+            tma_load_4d(&tmA, &full[s], sa, (a.kb0 + it) * BK, tile_m * BM, 0, ab);
+            tma_load_4d(&tmB, &full[s], sb, (a.kb0 + it) * BK, tile_n * BN, 0, bb);
         }
     } else if (warp == 1 && lane == 0) {
-        // MMA issuer
+        // MMA issuer: per stage the six plane products, the small ones into columns [0, BN),
+        // x0 y0 into [BN, 2 BN), so that the small terms never add into the large accumulator
         for (int it = 0; it < niter && ok; ++it) {
             const int s = it % STAGES;
             const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
@@ -215,10 +212,17 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
-            const uint32_t sb = sa + TILE_A_BYTES;
+            const uint32_t sb = sa + STAGE_A_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk)
-                mma_bf16(tmem, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (it > 0 || kk > 0) ? 1u : 0u);
+            for (int t = 0; t < NTERMS; ++t) {
+                const uint32_t d = t < NTERMS - 1 ? tmem : tmem + BN;
+                const uint32_t at = sa + term_pa(t) * TILE_A_BYTES, bt = sb + term_pb(t) * TILE_B_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const bool first = it == 0 && kk == 0 && (t == 0 || t == NTERMS - 1);
+                    mma_bf16(d, smem_desc(at + kk * 32), smem_desc(bt + kk * 32), first ? 0u : 1u);
+                }
+            }
             mma_commit(&empty[s]);
         }
         mma_commit(accum);
@@ -235,8 +239,11 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     const bool add_c = a.alpha == 1.0 && a.beta == 1.0;   // C += op(A) op(B): one FP64 add
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
-        float v[16];
+        float v[16], vb[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN + c0), vb);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = __fadd_rn(vb[j], v[j]);
         if (row < a.m) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
@@ -259,7 +266,7 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
     }
 }
 
@@ -267,16 +274,19 @@ k_gemm_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
 // Chunked-accumulation variant for the contractions of a coarse-graining step.  The
 // tensor cores truncate when they add into an FP32 accumulator (about 2^-25 of its
 // value per K = 16 step, one sign for same-sign sums), so a long K builds a bias
-// (-6e-6 relative at K = 2304).  Here K runs in chunks of `chunk` K blocks, each on a
-// fresh accumulator; two TMEM accumulators alternate so the MMA of chunk c+1 overlaps
-// the drain of chunk c.  Eight drain warps (warp & 3 = TMEM lane quadrant, warp >> 2 =
+// (-6e-6 relative at K = 2304).  Here K runs in chunks of `chunk` x 64, each chunk on
+// a fresh pair of accumulators (the five small plane products, and x0 y0), so that only
+// the few x0 y0 steps of one chunk truncate at the full magnitude; the stages of a chunk
+// are released one by one.  Two accumulator pairs (all 512 TMEM columns) alternate so
+// the MMA of chunk c+1 overlaps the drain of chunk c.  Eight drain warps (warp & 3 = TMEM lane quadrant, warp >> 2 =
 // column half) add every chunk into register pairs (hi, lo) with FP32 TwoSum (round to
 // nearest), and round hi + lo once at the end.  Warp 8 issues the TMA loads, warp 9
 // the MMAs, warps 10-11 only fill the last warpgroup.  Every wait is bounded as in
 // k_gemm_split_tc.
 // ---------------------------------------------------------------------------
-constexpr int ACC_STAGES = 6;                 // one CTA per SM: a deeper ring covers the L2 latency
-constexpr int SMEM_BYTES_ACC = ACC_STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int ACC_STAGES = 4;                 // 192 KB: one CTA per SM
+constexpr int SMEM_BYTES_ACC = ACC_STAGES * STAGE_BYTES + 1024 /*align*/ + SMEM_TAIL;
+constexpr int MAX_CHUNK = 8;                      // chunks of at most 8 x 64
 constexpr int ACC_WARPS = 8;
 // drain warps + the TMA and MMA warps, rounded up to whole warpgroups (registers are
 // granted per group of four warps, so ten warps cost as much as twelve)
@@ -321,8 +331,9 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile_m = blockIdx.x, tile_n = blockIdx.y, b = blockIdx.z;
-    const int nkb = a.nkb;
-    const int nchunks = (nkb + chunk - 1) / chunk;
+    const int nkb = a.nkb;                    // stages (K blocks of BK = 32)
+    const int cs = chunk * (64 / BK);         // stages per chunk
+    const int nchunks = (nkb + cs - 1) / cs;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < ACC_STAGES; ++s) {
@@ -338,8 +349,9 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
     }
     if (warp == 0) {
+        // accumulator pair of buffer u: small products at columns 2u BN, x0 y0 at (2u + 1) BN
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(2 * BN));
+                     "r"(4 * BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -349,52 +361,49 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
     bool ok = true;
 
     if (warp == ACC_WARPS && lane == 0) {
-        // TMA producer: chunk-major, within a chunk the plane products smallest first
+        // TMA producer: one K block of all three planes of A and of B per stage, in K order
         const int ab = a.a_batched ? b : 0, bb = a.b_batched ? b : 0;
-        int it = 0;
-        for (int c = 0; c < nchunks && ok; ++c) {
-            const int kbeg = c * chunk, kend = min(nkb, kbeg + chunk);
-            for (int t = 0; t < NTERMS && ok; ++t)
-                for (int kb = kbeg; kb < kend; ++kb, ++it) {
-                    const int s = it % ACC_STAGES;
-                    const uint32_t ph = (uint32_t)(it / ACC_STAGES) & 1u;
-                    ok = mbar_wait(&empty[s], ph ^ 1u, a.status);
-                    if (!ok) break;
-                    unsigned char* sa = tiles + s * STAGE_BYTES;
-                    unsigned char* sb = sa + TILE_A_BYTES;
-                    mbar_expect_tx(&full[s], STAGE_BYTES);
-                    tma_load_4d(&tmA, &full[s], sa, (a.kb0 + kb) * BK, tile_m * BM, c_pa[t], ab);
-                    tma_load_4d(&tmB, &full[s], sb, (a.kb0 + kb) * BK, tile_n * BN, c_pb[t], bb);
-                }
+        for (int it = 0; it < nkb && ok; ++it) {
+            const int s = it % ACC_STAGES;
+            const uint32_t ph = (uint32_t)(it / ACC_STAGES) & 1u;
+            ok = mbar_wait(&empty[s], ph ^ 1u, a.status);
+            if (!ok) break;
+            unsigned char* sa = tiles + s * STAGE_BYTES;
+            unsigned char* sb = sa + STAGE_A_BYTES;
+            mbar_expect_tx(&full[s], STAGE_BYTES);
+            tma_load_4d(&tmA, &full[s], sa, (a.kb0 + it) * BK, tile_m * BM, 0, ab);
+            tma_load_4d(&tmB, &full[s], sb, (a.kb0 + it) * BK, tile_n * BN, 0, bb);
         }
     } else if (warp == ACC_WARPS + 1 && lane == 0) {
-        // MMA issuer: chunk c into accumulator c & 1, once the drain of chunk c - 2 is done
-        int it = 0;
+        // MMA issuer: chunk c into accumulator pair c & 1, once the drain of chunk c - 2 is
+        // done; every stage's six products go out as soon as it lands, and the stage is freed
         for (int c = 0; c < nchunks && ok; ++c) {
             const int buf = c & 1;
             if (c >= 2) {
                 ok = mbar_wait(&acc_empty[buf], (uint32_t)((c >> 1) - 1) & 1u, a.status);
                 if (!ok) break;
             }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t d = tmem + (uint32_t)(buf * BN);
-            const int kbeg = c * chunk, kend = min(nkb, kbeg + chunk);
-            bool first = true;
-            for (int t = 0; t < NTERMS && ok; ++t)
-                for (int kb = kbeg; kb < kend; ++kb, ++it) {
-                    const int s = it % ACC_STAGES;
-                    const uint32_t ph = (uint32_t)(it / ACC_STAGES) & 1u;
-                    ok = mbar_wait(&full[s], ph, a.status);
-                    if (!ok) break;
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
-                    const uint32_t sb = sa + TILE_A_BYTES;
+            const uint32_t d_small = tmem + (uint32_t)(2 * buf * BN), d_big = d_small + BN;
+            const int ibeg = c * cs, iend = min(nkb, ibeg + cs);
+            for (int it = ibeg; it < iend && ok; ++it) {
+                const int s = it % ACC_STAGES;
+                ok = mbar_wait(&full[s], (uint32_t)(it / ACC_STAGES) & 1u, a.status);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
+                const uint32_t sb = sa + STAGE_A_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < BK / 16; ++kk)
-                        mma_bf16(d, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (first && kk == 0) ? 0u : 1u);
-                    first = false;
-                    mma_commit(&empty[s]);
+                for (int t = 0; t < NTERMS; ++t) {
+                    const uint32_t d = t < NTERMS - 1 ? d_small : d_big;
+                    const uint32_t at = sa + term_pa(t) * TILE_A_BYTES, bt = sb + term_pb(t) * TILE_B_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+                        const bool first = it == ibeg && kk == 0 && (t == 0 || t == NTERMS - 1);
+                        mma_bf16(d, smem_desc(at + kk * 32), smem_desc(bt + kk * 32), first ? 0u : 1u);
+                    }
                 }
+                mma_commit(&empty[s]);
+            }
             mma_commit(&acc_full[buf]);
         }
     } else if (warp < ACC_WARPS) {
@@ -408,13 +417,18 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
             ok = warp_wait(&acc_full[buf], (uint32_t)(c >> 1) & 1u, a.status, lane);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN + half * ACC_COLS);
+            // x0 y0 into (hi, lo) by TwoSum; the small products (2^-8 of it) straight into lo
+            const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(2 * buf * BN + half * ACC_COLS);
 #pragma unroll
             for (int q = 0; q < ACC_COLS / 16; ++q) {
-                float v[16];
-                tmem_ld16(base + (uint32_t)(q * 16), v);
+                float v[16], w[16];
+                tmem_ld16(base + (uint32_t)(BN + q * 16), v);
+                tmem_ld16(base + (uint32_t)(q * 16), w);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) two_sum_acc(hi[q * 16 + j], lo[q * 16 + j], v[j]);
+                for (int j = 0; j < 16; ++j) {
+                    two_sum_acc(hi[q * 16 + j], lo[q * 16 + j], v[j]);
+                    lo[q * 16 + j] = __fadd_rn(lo[q * 16 + j], w[j]);
+                }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -448,7 +462,7 @@ k_gemm_split_tc_chunked(const __grid_constant__ CUtensorMap tmA, const __grid_co
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(4 * BN));
     }
 }
 
@@ -549,16 +563,16 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// planes [nb][3][rows][Kp] bf16 -> 4D map {Kp, rows, 3, nb}, box {64, box_rows, 1, 1}
+// planes [nb][3][rows][Kp] bf16 -> 4D map {Kp, rows, 3, nb}, box {32, box_rows, 3, 1}
 void make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t Kp, int nb, int box_rows) {
     EncodeTiledFn fn = encode_fn();
     TNR_REQUIRE(fn, TNR_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[4] = {(cuuint64_t)Kp, (cuuint64_t)rows, 3, (cuuint64_t)nb};
     cuuint64_t strides[3] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * 2 * rows, (cuuint64_t)Kp * 2 * rows * 3};
-    cuuint32_t box[4] = {BK, (cuuint32_t)box_rows, 1, 1};
+    cuuint32_t box[4] = {BK, (cuuint32_t)box_rows, PLANES, 1};   // all three planes of a K block
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     TNR_REQUIRE(r == CUDA_SUCCESS, TNR_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
 }
@@ -624,6 +638,7 @@ void launch_tc_chunked(Ctx& c, const CUtensorMap& mA, const CUtensorMap& mB, int
                        int nkb, int chunk, double alpha, double beta, double* C, int64_t ldc, const Batch2& bt,
                        bool a_b, bool b_b) {
     const int batch = bt.n1 * bt.n2;
+    TNR_REQUIRE(chunk >= 1 && chunk <= MAX_CHUNK, TNR_ERR_UNSUPPORTED, "split chunk out of range");
     TcArgs args;
     args.m = m;
     args.n = n;
@@ -703,8 +718,8 @@ bool gemm_split_tc_a(Ctx& c, const SplitA& P, bool tb, int64_t n, const double* 
     Buf pb;
     CUtensorMap mB;
     const bool b_b = split_b(c, tb, n, P.k, P.Kp, B, ldb, bt, pb, mB);
-    const int nkb = (int)((P.Kp + BK - 1) / BK);
-    if (chunk_kb > 0 && nkb > chunk_kb)
+    const int nkb = (int)((P.Kp + BK - 1) / BK);      // K blocks of 32; chunk_kb counts blocks of 64
+    if (chunk_kb > 0 && nkb > chunk_kb * (64 / BK))
         launch_tc_chunked(c, P.map, mB, P.m, n, P.k, nkb, chunk_kb, alpha, beta, C, ldc, bt, P.batched, b_b);
     else
         launch_tc(c, P.map, mB, P.m, n, P.k, 0, nkb, alpha, beta, C, ldc, bt, P.batched, b_b);

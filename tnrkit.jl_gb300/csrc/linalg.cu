@@ -43,7 +43,7 @@ template <> struct JTol<float> { static constexpr double rel = 2e-7, floor = TNR
 template <class T>
 __global__ void __launch_bounds__(JTHREADS)
 k_jacobi(const double* __restrict__ Gin, int64_t ldg, int64_t strideG, int r, double* __restrict__ Wout,
-         double* __restrict__ lam, T* __restrict__ Ww, int* status) {
+         double* __restrict__ lam, T* __restrict__ Ww, int* status, double rel_tol, double floor_tol) {
     // one CTA per matrix of a batch
     Gin += (int64_t)blockIdx.x * strideG;
     Wout += (int64_t)blockIdx.x * r * r;
@@ -81,8 +81,8 @@ k_jacobi(const double* __restrict__ Gin, int64_t ldg, int64_t strideG, int r, do
         if (tid == 0) fro = sqrt(acc);
     }
     __syncthreads();
-    const T abs_floor = (T)JTol<T>::floor * fro;
-    const T reltol = (T)JTol<T>::rel;
+    const T abs_floor = (T)floor_tol * fro;
+    const T reltol = (T)rel_tol;
     int sweep = 0;
     bool converged = (r <= 1);
     const int max_sweeps = sizeof(T) == 4 ? JMAX_SWEEPS_F32 : JMAX_SWEEPS;
@@ -184,7 +184,7 @@ k_jacobi(const double* __restrict__ Gin, int64_t ldg, int64_t strideG, int r, do
 
 template <class T>
 static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch,
-                          int64_t strideG) {
+                          int64_t strideG, double rel = JTol<T>::rel, double floor = JTol<T>::floor) {
     TNR_REQUIRE(r >= 1 && r <= JMAX, TNR_ERR_UNSUPPORTED, "jacobi_eigh: r out of range");
     const size_t aux = 2 * (JMAX / 2 + 1) * (sizeof(T) + sizeof(int));
     const bool w_in_smem = sizeof(T) == 4;      // FP32: eigenvectors in shared memory as well
@@ -195,13 +195,18 @@ static void launch_jacobi(Ctx& c, const double* G, int64_t ldg, int r, double* W
     Buf ww(c.pool.get(), w_in_smem ? sizeof(T) : (size_t)batch * r * r * sizeof(T));
     int nt = r <= 32 ? 128 : (r <= 64 ? 256 : JTHREADS);
     int rec = prof_start(c.stream);
-    k_jacobi<T><<<batch, nt, smem, c.stream>>>(G, ldg, strideG, r, W, lam, ww.as<T>(), c.d_status);
+    k_jacobi<T><<<batch, nt, smem, c.stream>>>(G, ldg, strideG, r, W, lam, ww.as<T>(), c.d_status, rel, floor);
     check_launch("jacobi");
     prof_stop(rec, c.stream, sizeof(T) == 8 ? PROF_JACOBI : PROF_JACOBI32, (double)r * r * r * batch);
 }
 
 void jacobi_eigh(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch, int64_t strideG) {
     launch_jacobi<double>(c, G, ldg, r, W, lam, batch, strideG);
+}
+
+void jacobi_eigh_tol(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch, int64_t strideG,
+                     double rel, double floor) {
+    launch_jacobi<double>(c, G, ldg, r, W, lam, batch, strideG, rel, floor);
 }
 
 void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch,
@@ -239,41 +244,64 @@ k_chol_inv(double* G, int r, double shift, int* status) {
     if (tid == 0) bad = 0;
     for (int e = tid; e < r * r; e += CHOL_THREADS) {
         int i = e % r, j = e / r;
-        S[i + j * ld] = (T)((i >= j) ? G[e] + (i == j ? shift : 0.0) : 0.0);
+        if (sizeof(T) == 4) {
+            // FP32: convert with integer operations, shift in FP32 (no FP64 arithmetic)
+            const float v = i >= j ? f64_to_f32_rn(G[e]) : 0.0f;
+            S[i + j * ld] = (T)(i == j ? v + (float)shift : v);
+        } else {
+            S[i + j * ld] = (T)((i >= j) ? G[e] + (i == j ? shift : 0.0) : 0.0);
+        }
     }
     __syncthreads();
     const int nblk = (r + CB - 1) / CB;
     for (int pb = 0; pb < nblk; ++pb) {
         const int p = pb * CB, nb = min(CB, r - p);
-        // (1) diagonal block, one warp, right-looking: lane l owns row p + l
+        // (1) diagonal block, one warp, right-looking, in registers: lane l holds row p + l; the
+        // column of the pivot comes from the other lanes by shuffles
         if (warp == 0) {
-            for (int j = 0; j < nb; ++j) {
-                T d = S[(p + j) + (p + j) * ld];
-                if (!(d > T(0)) || !isfinite(d)) {
-                    if (lane == 0) bad = 1;
-                    d = (T)1e-30;
+            T a[CB];
+#pragma unroll
+            for (int jj = 0; jj < CB; ++jj)
+                a[jj] = (jj <= lane && lane < nb && jj < nb) ? S[(p + lane) + (p + jj) * ld] : T(0);
+#pragma unroll
+            for (int j = 0; j < CB; ++j) {
+                if (j < nb) {                                   // warp-uniform
+                    T d = __shfl_sync(0xffffffffu, a[j], j);
+                    if (!(d > T(0)) || !isfinite(d)) {
+                        if (lane == 0) bad = 1;
+                        d = (T)1e-30;
+                    }
+                    const T piv = sqrt(d);
+                    if (lane == j) a[j] = piv;
+                    else if (lane > j) a[j] = a[j] / piv;      // L[l][j]
+                    const T x = a[j];
+#pragma unroll
+                    for (int jj = j + 1; jj < CB; ++jj) {
+                        const T v = __shfl_sync(0xffffffffu, a[j], jj);   // L[jj][j]
+                        if (lane >= jj) a[jj] -= x * v;
+                    }
                 }
-                const T piv = sqrt(d);
-                T x = T(0);
-                if (lane > j && lane < nb) {
-                    x = S[(p + lane) + (p + j) * ld] / piv;
-                    S[(p + lane) + (p + j) * ld] = x;
-                }
-                if (lane == j) S[(p + j) + (p + j) * ld] = piv;
-                __syncwarp();
-                if (lane > j && lane < nb)
-                    for (int jj = j + 1; jj <= lane; ++jj) S[(p + lane) + (p + jj) * ld] -= x * S[(p + jj) + (p + j) * ld];
-                __syncwarp();
             }
+#pragma unroll
+            for (int jj = 0; jj < CB; ++jj)
+                if (jj <= lane && lane < nb && jj < nb) S[(p + lane) + (p + jj) * ld] = a[jj];
         }
         __syncthreads();
-        // (2) rows below the block: L21 = A21 L11^-T, one thread per row
+        // (2) rows below the block: L21 = A21 L11^-T, one thread per row, the row in registers
         for (int i = p + nb + tid; i < r; i += CHOL_THREADS) {
-            for (int j = 0; j < nb; ++j) {
-                T acc = S[i + (p + j) * ld];
-                for (int t = 0; t < j; ++t) acc -= S[i + (p + t) * ld] * S[(p + j) + (p + t) * ld];
-                S[i + (p + j) * ld] = acc / S[(p + j) + (p + j) * ld];
+            T x[CB];
+#pragma unroll
+            for (int j = 0; j < CB; ++j) {
+                if (j < nb) {
+                    T acc = S[i + (p + j) * ld];
+#pragma unroll
+                    for (int t = 0; t < j; ++t) acc -= x[t] * S[(p + j) + (p + t) * ld];
+                    x[j] = acc / S[(p + j) + (p + j) * ld];
+                }
             }
+#pragma unroll
+            for (int j = 0; j < CB; ++j)
+                if (j < nb) S[i + (p + j) * ld] = x[j];
         }
         __syncthreads();
         // (3) trailing lower triangle: A22 -= L21 L21^T, one warp per column
@@ -286,16 +314,33 @@ k_chol_inv(double* G, int r, double shift, int* status) {
         }
         __syncthreads();
     }
-    // (4) diagonal blocks of X = L^-1, one warp per block, lane j owns column j of the block
+    // (4) diagonal blocks of X = L^-1, one warp per block, lane j owns column j of the block in
+    // registers (x[t] = X[p + t][p + j]); rows of L are read as shared-memory broadcasts
     for (int pb = warp; pb < nblk; pb += NW) {
         const int p = pb * CB, nb = min(CB, r - p);
-        if (lane < nb) {
-            const int j = lane;
-            S[r + (p + j) * ld] = T(1) / S[(p + j) + (p + j) * ld];
-            for (int i = j + 1; i < nb; ++i) {
-                T acc = S[(p + i) + (p + j) * ld] * S[r + (p + j) * ld];
-                for (int t = j + 1; t < i; ++t) acc += S[(p + i) + (p + t) * ld] * S[(p + j) + (p + t) * ld];
-                S[(p + j) + (p + i) * ld] = -acc / S[(p + i) + (p + i) * ld];
+        const int j = lane;
+        T x[CB];
+#pragma unroll
+        for (int i = 0; i < CB; ++i) {
+            if (i < nb) {
+                T v = T(0);
+                if (i == j) {
+                    v = T(1) / S[(p + j) + (p + j) * ld];
+                } else if (i > j) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int t = 0; t < i; ++t)
+                        if (t >= j) acc += S[(p + i) + (p + t) * ld] * x[t];
+                    v = -acc / S[(p + i) + (p + i) * ld];
+                }
+                x[i] = v;
+            }
+        }
+        if (j < nb) {
+#pragma unroll
+            for (int i = 0; i < CB; ++i) {
+                if (i == j) S[r + (p + j) * ld] = x[i];
+                else if (i > j && i < nb) S[(p + j) + (p + i) * ld] = x[i];
             }
         }
     }
@@ -327,7 +372,8 @@ k_chol_inv(double* G, int r, double shift, int* status) {
     }
     for (int e = tid; e < r * r; e += CHOL_THREADS) {
         int i = e % r, j = e / r;
-        G[e] = i > j ? (double)S[j + i * ld] : (i == j ? (double)S[r + j * ld] : 0.0);
+        const T v = i > j ? S[j + i * ld] : (i == j ? S[r + j * ld] : T(0));
+        G[e] = sizeof(T) == 4 ? f32_to_f64((float)v) : (double)v;
     }
     if (tid == 0 && bad) atomicOr(status, ST_CHOL_BREAKDOWN);
 }

@@ -96,6 +96,14 @@ static void polar(Ctx& c, double* Q, int64_t m, int r) {
 
 // Exact SVD of the tall X = op(M) (m x p, p <= 128): X V = Ux diag(s), Ux unit columns.
 // trans=false: X = M (ld m); trans=true: X = M^T with M stored p x m (ld p).
+// FP64 cleanup Jacobi of the final decompositions: rotations stop at 1e-12 of the diagonal,
+// which leaves vectors of values that differ by a relative gap g rotated by ~1e-12 / g.  The gap
+// fallback converges it to 1e-15 (FP64 rounding of the Gram), for gaps down to ~1e-5.
+static void jacobi_final(Ctx& c, const double* G, int p, double* W, double* lam) {
+    if (c.exact_jacobi) jacobi_eigh_tol(c, G, p, p, W, lam, 1, 0, 1e-15, 1e-22);
+    else jacobi_eigh(c, G, p, p, W, lam);
+}
+
 static void final_svd(Ctx& c, const double* M, bool trans, int64_t m, int p, double* Ux, double* s, double* V) {
     Buf G(c.pool.get(), (size_t)p * p * sizeof(double));
     Buf W1(c.pool.get(), (size_t)p * p * sizeof(double));
@@ -109,7 +117,7 @@ static void final_svd(Ctx& c, const double* M, bool trans, int64_t m, int p, dou
     // pass 2: X W1 has nearly orthogonal columns; FP64 Jacobi cleans up the rest
     gemm_f64(c, trans, false, m, p, p, 1.0, M, ldm, 0, W1.d(), p, 0, 0.0, Ux, m, 0);
     gemm_f64(c, true, false, p, p, m, 1.0, Ux, m, 0, Ux, m, 0, 0.0, G.d(), p, 0);
-    jacobi_eigh(c, G.d(), p, p, W2.d(), lam.d());
+    jacobi_final(c, G.d(), p, W2.d(), lam.d());
     gemm_f64(c, false, false, p, p, p, 1.0, W1.d(), p, 0, W2.d(), p, 0, 0.0, V, p, 0);
     gemm_f64(c, trans, false, m, p, p, 1.0, M, ldm, 0, V, p, 0, 0.0, Ux, m, 0);
     col_norms(c, Ux, m, p, m, s);
@@ -127,7 +135,7 @@ static void final_eigh(Ctx& c, const double* H, int p, double* W, double* lam) {
     polar(c, W1.d(), p, p);
     gemm_f64(c, false, false, p, p, p, 1.0, H, p, 0, W1.d(), p, 0, 0.0, T.d(), p, 0);
     gemm_f64(c, true, false, p, p, p, 1.0, W1.d(), p, 0, T.d(), p, 0, 0.0, G.d(), p, 0);
-    jacobi_eigh(c, G.d(), p, p, W2.d(), lam);
+    jacobi_final(c, G.d(), p, W2.d(), lam);
     gemm_f64(c, false, false, p, p, p, 1.0, W1.d(), p, 0, W2.d(), p, 0, 0.0, W, p, 0);
     check_status(c, "final_eigh");
 }
@@ -174,6 +182,35 @@ int iterations_needed(std::vector<double> v, int k, int r, int power, double tar
 
 int iteration_cap(const Ctx& c) { return c.precision == TNR_PREC_F64 ? MAXIT : 16; }
 
+// The spectral gap at k is too small for the subspace iteration: the estimates say the kept
+// subspace would not reach the target angle within the iteration cap (sigma_r / sigma_k too
+// close to 1).  Same estimate rules as iterations_needed, without the cap.  In split precision
+// estimates below ~1e-7 sigma_1 are product noise, so only a kept tail above 1e-5 sigma_1
+// counts (no TRG/BTRG decomposition of the Ising model at chi 24-32, beta 0.30-0.60, needs more
+// than the split cap of 16 iterations by the exact spectra).
+bool gap_too_small(const Ctx& c, std::vector<double> v, int k, int r, int power, double target, int cap) {
+    std::sort(v.begin(), v.end(), [](double a, double b) { return std::fabs(a) > std::fabs(b); });
+    const double vk = std::fabs(v[k - 1]), v1 = std::fabs(v[0]);
+    if (!(v1 > 0) || vk <= 1e-13 * v1) return false;
+    if (c.precision != TNR_PREC_F64 && vk <= 1e-5 * v1) return false;
+    const double vr = std::max(std::fabs(v[r - 1]), 1e-15 * v1);
+    const double rho = std::pow(vr / vk, (double)power);
+    if (rho >= 0.999) return true;
+    return std::ceil(std::log(target) / std::log(rho)) + 2 > cap;
+}
+
+// runs the decomposition in FP64 precision whatever the context's precision (the gap fallback)
+struct F64Scope {
+    Ctx& c;
+    int saved;
+    bool saved_exact;
+    explicit F64Scope(Ctx& cc) : c(cc), saved(cc.precision), saved_exact(cc.exact_jacobi) {
+        c.precision = TNR_PREC_F64;
+        c.exact_jacobi = true;
+    }
+    ~F64Scope() { c.precision = saved; c.exact_jacobi = saved_exact; }
+};
+
 // sigma estimates of the columns of X (n x r, batch B of stride n r): column norms of X
 // aligned with its Ritz vectors.  One FP32 Jacobi on the FP64 Gram leaves ~1e-7 of the
 // leading directions in the small columns; FP64 precision aligns the aligned basis once
@@ -212,13 +249,32 @@ static bool debug_on() {
 #endif
 static double target_angle(Ctx& c) { return c.precision == TNR_PREC_F64 ? TNR_TARGET_F64 : 1e-9; }
 
+// r_override > 0: the subspace width (the gap fallback's widest subspace)
+static TsvdOut tsvd_impl(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt,
+                         int direct_max, int r_override);
+
 TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt, int direct_max) {
+    ++c.decompositions;
+    TsvdOut o = tsvd_impl(c, M, m, n, k, U, s, Vt, std::min(direct_max, RDIRECT), 0);
+    c.max_iters = std::max(c.max_iters, o.iters);
+    return o;
+}
+
+TsvdOut tsvd_gap_fallback(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt) {
+    ++c.gap_fallbacks;
+    F64Scope scope(c);
+    if (std::min(m, n) <= RSMALL) return tsvd_impl(c, M, m, n, k, U, s, Vt, RSMALL, 0);
+    return tsvd_impl(c, M, m, n, k, U, s, Vt, RDIRECT, RSMALL);
+}
+
+static TsvdOut tsvd_impl(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, double* s, double* Vt,
+                         int direct_max, int r_override) {
     TsvdOut out;
     const int64_t p = std::min(m, n);
     k = (int)std::min<int64_t>(k, p);
     out.k = k;
     if (k <= 0) return out;
-    if (p <= std::min(RDIRECT, direct_max)) {
+    if (p <= direct_max) {
         const int pp = (int)p;
         const bool wide = m < n;
         const int64_t rows = wide ? n : m;               // X = M (tall) or M^T
@@ -244,6 +300,7 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
     }
     int r = (int)std::min<int64_t>({p, (int64_t)RMAX, (int64_t)((3 * k + 7) / 8 * 8)});
     r = std::max(r, std::min((int)p, k + 8));
+    if (r_override > 0) r = (int)std::min<int64_t>(p, r_override);
     Buf Om(c.pool.get(), (size_t)n * r * sizeof(double));
     Buf Y(c.pool.get(), (size_t)m * r * sizeof(double));
     Buf Uq(c.pool.get(), (size_t)m * r * sizeof(double));
@@ -271,8 +328,14 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
         orth_scaled(c, Y.d(), m, r, Uq.d());
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, lam.d(), r);
-            need = std::max(it + 1, iterations_needed(est, k, r, 2, target_angle(c), iteration_cap(c)));
             check_status(c, "tsvd");
+            if (it == 0 && r_override == 0 && gap_too_small(c, est, k, r, 2, target_angle(c), iteration_cap(c))) {
+                // the gap at k is too small for the iteration: a matrix the one-CTA solvers hold
+                // is decomposed exactly in FP64 (the full Jacobi path); a larger one is iterated
+                // in FP64 on the widest subspace they hold
+                return tsvd_gap_fallback(c, M, m, n, k, U, s, Vt);
+            }
+            need = std::max(it + 1, iterations_needed(est, k, r, 2, target_angle(c), iteration_cap(c)));
         }
     }
     out.iters = it;
@@ -312,13 +375,24 @@ TsvdOut tsvd(Ctx& c, const double* M, int64_t m, int64_t n, int k, double* U, do
     return out;
 }
 
+static TsvdOut teigh_impl(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk, int direct_max,
+                          int r_override);
+
 TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk, int direct_max) {
+    ++c.decompositions;
+    TsvdOut o = teigh_impl(c, M, n, k, U, lamk, std::min(direct_max, RDIRECT), 0);
+    c.max_iters = std::max(c.max_iters, o.iters);
+    return o;
+}
+
+static TsvdOut teigh_impl(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk, int direct_max,
+                          int r_override) {
     TsvdOut out;
     k = (int)std::min<int64_t>(k, n);
     out.k = k;
     if (k <= 0) return out;
     sum_squares(c, M, n * n, c.d_scalar);
-    if (n <= std::min(RDIRECT, direct_max)) {
+    if (n <= direct_max) {
         const int nn = (int)n;
         Buf W(c.pool.get(), (size_t)nn * nn * sizeof(double));
         Buf l(c.pool.get(), (size_t)nn * sizeof(double));
@@ -337,6 +411,7 @@ TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk
     }
     int r = (int)std::min<int64_t>({n, (int64_t)RMAX, (int64_t)((3 * k + 7) / 8 * 8)});
     r = std::max(r, std::min((int)n, k + 8));
+    if (r_override > 0) r = (int)std::min<int64_t>(n, r_override);
     Buf Om(c.pool.get(), (size_t)n * r * sizeof(double));
     Buf Y(c.pool.get(), (size_t)n * r * sizeof(double));
     Buf Q(c.pool.get(), (size_t)n * r * sizeof(double));
@@ -358,8 +433,15 @@ TsvdOut teigh(Ctx& c, const double* M, int64_t n, int k, double* U, double* lamk
         orth_scaled(c, Y.d(), n, r, Q.d());
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, l.d(), r);
-            need = std::max(it + 1, iterations_needed(est, k, r, 1, target_angle(c), iteration_cap(c)));
             check_status(c, "teigh");
+            if (it == 0 && r_override == 0 && gap_too_small(c, est, k, r, 1, target_angle(c), iteration_cap(c))) {
+                // the gap fallback, as in tsvd
+                ++c.gap_fallbacks;
+                F64Scope scope(c);
+                if (n <= RSMALL) return teigh_impl(c, M, n, k, U, lamk, RSMALL, 0);
+                return teigh_impl(c, M, n, k, U, lamk, direct_max, RSMALL);
+            }
+            need = std::max(it + 1, iterations_needed(est, k, r, 1, target_angle(c), iteration_cap(c)));
         }
     }
     out.iters = it;

@@ -155,7 +155,10 @@ std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, i
     polar_b(c, W1.d(), r, r, B);
     gemm_f64(c, false, false, r, r, r, 1.0, G.d(), r, W1.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));
     gemm_f64(c, true, false, r, r, r, 1.0, W1.d(), r, E.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
-    jacobi_eigh(c, E2.d(), r, r, G.d(), lam.d(), B, rr);                  // W2 into G
+    // the FP64 cleanup resolves what the split products carry: rotations below 1e-10 of the pair's
+    // diagonal scale or 1e-16 of |G| (eigenvalues below ~1e-16 of the largest, singular values
+    // below ~1e-8 of the largest, lie under the split noise floor) are not worth a sweep
+    jacobi_eigh_tol(c, E2.d(), r, r, G.d(), lam.d(), B, rr, 1e-10, 1e-16);   // W2 into G
     gemm_f64(c, false, false, r, r, r, 1.0, W1.d(), r, G.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));   // Vb
     // PV = P Vb_k (r x k)
     Buf PV(c.pool.get(), (size_t)B * rk * sizeof(double));
@@ -171,9 +174,27 @@ std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, i
     return to_host(c, s, (int64_t)B * k);
 }
 
+static std::vector<TsvdOut> tsvd_batched_impl(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U,
+                                              double* s, double* Vt, std::vector<int>& flagged);
+
 // M: B stacked m x n matrices (ld m, stride m*n).  U [B][m x k], s [B][k], Vt [B][k x n].
+// A member whose gap at k is too small for the subspace iteration leaves the batch's
+// iteration count alone and is decomposed again on its own by the FP64 gap fallback.
 std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U, double* s,
                                   double* Vt) {
+    std::vector<int> flagged;
+    c.decompositions += (uint64_t)std::max(B, 0);
+    std::vector<TsvdOut> outs = tsvd_batched_impl(c, M, m, n, k, B, U, s, Vt, flagged);
+    const int64_t kk = outs.empty() ? 0 : outs[0].k;
+    for (int b : flagged)
+        outs[(size_t)b] = tsvd_gap_fallback(c, M + (size_t)b * m * n, m, n, (int)kk, U + (size_t)b * m * kk,
+                                            s + (size_t)b * kk, Vt + (size_t)b * kk * n);
+    for (auto& o : outs) c.max_iters = std::max(c.max_iters, o.iters);
+    return outs;
+}
+
+static std::vector<TsvdOut> tsvd_batched_impl(Ctx& c, const double* M, int64_t m, int64_t n, int k, int B, double* U,
+                                              double* s, double* Vt, std::vector<int>& flagged) {
     std::vector<TsvdOut> outs((size_t)B);
     const int64_t p = std::min(m, n);
     k = (int)std::min<int64_t>(k, p);
@@ -232,10 +253,12 @@ std::vector<TsvdOut> tsvd_batched(Ctx& c, const double* M, int64_t m, int64_t n,
         if (it == 0 || it == 2) {
             std::vector<double> est = to_host(c, lam.d(), (int64_t)B * r);
             int mx = 2;
-            for (int b = 0; b < B; ++b)
-                mx = std::max(mx, iterations_needed(std::vector<double>(est.begin() + (size_t)b * r,
-                                                                        est.begin() + (size_t)(b + 1) * r),
-                                                    k, r, 2, target, iteration_cap(c)));
+            for (int b = 0; b < B; ++b) {
+                std::vector<double> eb(est.begin() + (size_t)b * r, est.begin() + (size_t)(b + 1) * r);
+                if (it == 0 && gap_too_small(c, eb, k, r, 2, target, iteration_cap(c))) flagged.push_back(b);
+                if (std::find(flagged.begin(), flagged.end(), b) != flagged.end()) continue;
+                mx = std::max(mx, iterations_needed(eb, k, r, 2, target, iteration_cap(c)));
+            }
             need = std::max(it + 1, mx);
             check_status(c, "tsvd (batched)");
         }
