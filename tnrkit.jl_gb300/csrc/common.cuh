@@ -267,6 +267,11 @@ void gemm_bulk(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double
                const double* A, int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB,
                double beta, double* C, int64_t ldc, int64_t sC, int batch = 1, bool exact_sum = false);
 
+// CholeskyQR passes of the split-precision orthonormalisation (the FP64 path always runs three)
+#ifndef TNR_SPLIT_ORTH_PASSES
+#define TNR_SPLIT_ORTH_PASSES 3
+#endif
+
 // subspace iterations of the truncated SVD / eigensolver from sigma estimates (tsvd.cu)
 int iterations_needed(std::vector<double> v, int k, int r, int power, double target, int cap);
 int iteration_cap(const Ctx& c);
@@ -317,6 +322,10 @@ void jacobi_eigh_tol(Ctx& c, const double* G, int64_t ldg, int r, double* W, dou
 // G <- Cholesky factor inverse: on exit Linv (lower) with (G + shift I) = L L^T; returns via status
 void chol_inv(Ctx& c, double* G, int r, double shift, int batch = 1);
 // FP32 versions (one SM runs FP32 at 64x its FP64 rate): results returned in FP64 buffers
+// the FP64 cleanup of an FP32-aligned (nearly diagonal) G with the diagonal in FP64 and the
+// off-diagonal part and W - I in FP32: same outputs and thresholds as jacobi_eigh_tol
+void jacobi_eigh_mixed(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch,
+                       int64_t strideG, double rel, double floor);
 void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, double* lam, int batch = 1,
                      int64_t strideG = 0);
 void chol_inv_f32(Ctx& c, double* G, int r, double shift, int batch = 1);

@@ -675,6 +675,17 @@ bool split_b(Ctx& c, bool tb, int64_t n, int64_t k, int64_t Kp, const double* B,
     return b_b;
 }
 
+// the GEMM on planes already split: A's (P) and B's map
+bool launch_planes(Ctx& c, const SplitA& P, const CUtensorMap& mB, bool b_b, int64_t n, double alpha, double beta,
+                   double* C, int64_t ldc, const Batch2& bt, int chunk_kb) {
+    const int nkb = (int)((P.Kp + BK - 1) / BK);      // K blocks of 32; chunk_kb counts blocks of 64
+    if (chunk_kb > 0 && nkb > chunk_kb * (64 / BK))
+        launch_tc_chunked(c, P.map, mB, P.m, n, P.k, nkb, chunk_kb, alpha, beta, C, ldc, bt, P.batched, b_b);
+    else
+        launch_tc(c, P.map, mB, P.m, n, P.k, 0, nkb, alpha, beta, C, ldc, bt, P.batched, b_b);
+    return true;
+}
+
 }  // namespace
 
 bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
@@ -684,6 +695,10 @@ bool gemm_split_tc(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, do
     if (!tc_shape_ok(m, n, k, batch) || !tc_ready()) return false;
     SplitA P;
     if (!split_a_build(c, P, ta, A, lda, m, k, bt)) return false;
+    // a Gram X^T X (same matrices, same batch strides): op(B)'s rows are op(A)'s rows, so
+    // B uses A's planes and map (BM == BN) and the plane pass runs once
+    if (ta && !tb && A == B && lda == ldb && m == n && bt.sA1 == bt.sB1 && bt.sA2 == bt.sB2 && BM == BN)
+        return launch_planes(c, P, P.map, P.batched, n, alpha, beta, C, ldc, bt, chunk_kb);
     return gemm_split_tc_a(c, P, tb, n, B, ldb, alpha, beta, C, ldc, bt, chunk_kb);
 }
 
@@ -718,12 +733,7 @@ bool gemm_split_tc_a(Ctx& c, const SplitA& P, bool tb, int64_t n, const double* 
     Buf pb;
     CUtensorMap mB;
     const bool b_b = split_b(c, tb, n, P.k, P.Kp, B, ldb, bt, pb, mB);
-    const int nkb = (int)((P.Kp + BK - 1) / BK);      // K blocks of 32; chunk_kb counts blocks of 64
-    if (chunk_kb > 0 && nkb > chunk_kb * (64 / BK))
-        launch_tc_chunked(c, P.map, mB, P.m, n, P.k, nkb, chunk_kb, alpha, beta, C, ldc, bt, P.batched, b_b);
-    else
-        launch_tc(c, P.map, mB, P.m, n, P.k, 0, nkb, alpha, beta, C, ldc, bt, P.batched, b_b);
-    return true;
+    return launch_planes(c, P, mB, b_b, n, alpha, beta, C, ldc, bt, chunk_kb);
 }
 
 // ---------------------------------------------------------------------------

@@ -51,7 +51,7 @@ static std::vector<double> to_host(Ctx& c, const double* d, int n) {
 // 1e-6 max(1, r/16) then 1e-7.
 void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q) {
     const bool f64 = c.precision == TNR_PREC_F64;
-    const int passes = 3;
+    const int passes = f64 ? 3 : TNR_SPLIT_ORTH_PASSES;
     Buf G(c.pool.get(), (size_t)r * r * sizeof(double));
     Buf ds(c.pool.get(), (size_t)r * sizeof(double));
     double* src = Y;

@@ -48,7 +48,7 @@ Batch2 strided(int B, int64_t sA, int64_t sB, int64_t sC) {
 // precision; split-kernel Grams and FP32 Cholesky in split precision)
 void orth_b(Ctx& c, double* Y, int64_t m, int r, int B, double* Q) {
     const bool f64 = c.precision == TNR_PREC_F64;
-    const int passes = 3;
+    const int passes = f64 ? 3 : TNR_SPLIT_ORTH_PASSES;
     Buf G(c.pool.get(), (size_t)B * r * r * sizeof(double));
     Buf ds(c.pool.get(), (size_t)B * r * sizeof(double));
     double* src = Y;
@@ -155,10 +155,11 @@ std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, i
     polar_b(c, W1.d(), r, r, B);
     gemm_f64(c, false, false, r, r, r, 1.0, G.d(), r, W1.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));
     gemm_f64(c, true, false, r, r, r, 1.0, W1.d(), r, E.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
-    // the FP64 cleanup resolves what the split products carry: rotations below 1e-10 of the pair's
+    // the cleanup resolves what the split products carry: rotations below 1e-10 of the pair's
     // diagonal scale or 1e-16 of |G| (eigenvalues below ~1e-16 of the largest, singular values
-    // below ~1e-8 of the largest, lie under the split noise floor) are not worth a sweep
-    jacobi_eigh_tol(c, E2.d(), r, r, G.d(), lam.d(), B, rr, 1e-10, 1e-16);   // W2 into G
+    // below ~1e-8 of the largest, lie under the split noise floor) are not worth a sweep; E2 is
+    // nearly diagonal, so the mixed-precision Jacobi (FP64 diagonal) holds FP64 accuracy
+    jacobi_eigh_mixed(c, E2.d(), r, r, G.d(), lam.d(), B, rr, 1e-10, 1e-16);   // W2 into G
     gemm_f64(c, false, false, r, r, r, 1.0, W1.d(), r, G.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));   // Vb
     // PV = P Vb_k (r x k)
     Buf PV(c.pool.get(), (size_t)B * rk * sizeof(double));
