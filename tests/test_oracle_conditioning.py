@@ -19,7 +19,7 @@ def _sensitivity(o, cls, chi, beta, steps=12, seed=5):
     return float(np.abs(n1 / n0 - 1).max())
 
 
-@pytest.mark.parametrize("cls,chi", [("TRG", 16), ("BTRG", 24)])
+@pytest.mark.parametrize("cls,chi", [("TRG", 16), ("TRG", 24), ("BTRG", 24)])
 @pytest.mark.parametrize("beta", [0.40, 0.44, 0.47])
 def test_lockstep_betas_are_well_conditioned(oracle, cls, chi, beta):
     assert _sensitivity(oracle, cls, chi, beta) < 1e-12

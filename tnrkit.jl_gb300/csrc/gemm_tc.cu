@@ -543,6 +543,47 @@ __global__ void k_split_planes(SplitArgs a) {
     }
 }
 
+// The same planes for a K-contiguous source (sk == 1): no transpose, so no shared memory;
+// a thread splits 4 consecutive k of one row and writes 8 bytes per plane.  Needs Kp % 4 == 0
+// and rows * Kp / 4 * nb below 4e9 (32-bit item index plus the grid stride).
+__global__ void k_split_planes_kfast(SplitArgs a) {
+    const uint32_t nk4 = (uint32_t)(a.Kp / 4);
+    const uint32_t per_b = (uint32_t)a.rows * nk4;
+    const uint32_t total = per_b * (uint32_t)a.nb;
+    const int64_t plane = a.rows * a.Kp;
+    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+        const uint32_t bi = it / per_b, rem = it - bi * per_b;
+        const uint32_t i = rem / nk4;
+        const int64_t k = (int64_t)(rem - i * nk4) * 4;
+        const int b1 = (int)(bi % (uint32_t)a.n1), b2 = (int)(bi / (uint32_t)a.n1);
+        const double* S = a.src + b1 * a.s1 + b2 * a.s2 + (int64_t)i * a.si;
+        __nv_bfloat16 p0[4], p1[4], p2[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split3(k + e < a.K ? S[k + e] : 0.0, p0[e], p1[e], p2[e]);
+        __nv_bfloat16* D = a.dst + (int64_t)bi * 3 * plane + (int64_t)i * a.Kp + k;
+        uint2 u0, u1, u2;
+        memcpy(&u0, p0, 8);
+        memcpy(&u1, p1, 8);
+        memcpy(&u2, p2, 8);
+        *reinterpret_cast<uint2*>(D) = u0;
+        *reinterpret_cast<uint2*>(D + plane) = u1;
+        *reinterpret_cast<uint2*>(D + 2 * plane) = u2;
+    }
+}
+
+// planes of one operand on `st`: the K-contiguous kernel where it applies, else the tiled one
+void launch_split(const SplitArgs& sa, cudaStream_t st) {
+    if (sa.sk == 1 && sa.Kp % 4 == 0 && (double)sa.rows * (sa.Kp / 4) * sa.nb < 4.0e9) {   // index + stride < 2^32
+        const int64_t items = sa.rows * (sa.Kp / 4) * sa.nb;
+        const int g = (int)std::min<int64_t>((items + 255) / 256, (int64_t)sm_count() * 8);
+        k_split_planes_kfast<<<g, 256, 0, st>>>(sa);
+    } else {
+        const int64_t ntiles = ((sa.rows + 31) / 32) * ((sa.Kp + 31) / 32) * sa.nb;
+        const int g = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 16);
+        k_split_planes<<<g, dim3(32, 8), 0, st>>>(sa);
+    }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -580,10 +621,8 @@ void make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t Kp, int nb
 void split_operand(Ctx& c, const double* src, int64_t rows, int64_t K, int64_t Kp, int64_t si, int64_t sk,
                    int64_t s1, int64_t s2, int n1, int nb, __nv_bfloat16* dst) {
     SplitArgs sa{src, rows, K, Kp, si, sk, s1, s2, n1, nb, dst};
-    int64_t ntiles = ((rows + 31) / 32) * ((Kp + 31) / 32) * nb;
-    int g = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 16);
     int rec = prof_start(c.stream);
-    k_split_planes<<<g, dim3(32, 8), 0, c.stream>>>(sa);
+    launch_split(sa, c.stream);
     check_launch("split_planes");
     prof_stop(rec, c.stream, PROF_SPLIT, (double)rows * K * nb * 8 + (double)rows * Kp * nb * 6);
 }
@@ -828,9 +867,7 @@ extern "C" int tnr_gemm_split_noalloc(int ta, int tb, int64_t m, int64_t n, int6
         SplitArgs sa{A, m, k, Kp, ta ? lda : 1, ta ? 1 : lda, 0, 0, 1, 1, pa};
         SplitArgs sb{B, n, k, Kp, tb ? 1 : ldb, tb ? ldb : 1, 0, 0, 1, 1, pb};
         for (const SplitArgs* s : {&sa, &sb}) {
-            int64_t ntiles = ((s->rows + 31) / 32) * ((Kp + 31) / 32);
-            int g = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 16);
-            k_split_planes<<<g, dim3(32, 8), 0, st>>>(*s);
+            launch_split(*s, st);
             check_launch("split_planes (allocation-free)");
         }
         CUtensorMap mA, mB;

@@ -120,8 +120,8 @@ void copy_lead(Ctx& c, const double* in, int p, int k, int B, double* out) {
 
 // Split precision: the final Rayleigh-Ritz step of B lockstep instances.  Uq [B][m x r] is
 // orthonormal to FP32 level (CholeskyQR3 with FP32 Cholesky factors); its polar factor
-// Q' = Uq P, P = I - E/2 + 3E^2/8, E = Uq^T Uq - I, is never formed: P is folded into the
-// r x r problems.  With Z = M^T Uq (the projection, on the tensor cores with chunked
+// Q' = Uq P, P = (I + E)^(-1/2) to fourth order in E = Uq^T Uq - I, is never formed: P is
+// folded into the r x r problems.  With Z = M^T Uq (the projection, on the tensor cores with chunked
 // accumulation), Z' = M^T Q' = Z P and Z'^T Z' = P^T (Z^T Z) P = Vb S^2 Vb^T, so
 // U = Uq (P Vb_k), S_k = the column norms of Z (P Vb_k) and Vt = (Z P Vb_k / S_k)^T.
 // The eigenvectors of the r x r Gram come from an FP32 Jacobi alignment (polar-corrected
@@ -138,8 +138,42 @@ std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, i
     Buf E2(c.pool.get(), (size_t)B * rr * sizeof(double));
     gemm_f64(c, true, false, r, r, m, 1.0, Uq, m, Uq, m, 0.0, E.d(), r, strided(B, mr, mr, rr));
     add_identity(c, E.d(), r, -1.0, B);
-    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, E.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
-    polar_coeff(c, E.d(), E2.d(), P.d(), r, B);
+    // The polar factor below is a series in E (error ~0.25 ||E||^5).  A numerically rank-deficient
+    // M leaves noise directions in the basis that the split CholeskyQR3 (split Grams, FP32
+    // factors) may orthonormalise poorly (||E|| ~ 0.2 was seen); a batch with ||E||_F above 1e-2
+    // first takes one FP64 CholeskyQR pass on its exact Gram I + E, after which E is at FP64
+    // rounding.
+    Buf enrm(c.pool.get(), (size_t)B * sizeof(double));
+    fro_norms_batched(c, E.d(), rr, B, enrm.d());
+    std::vector<double> em = to_host(c, enrm.d(), B);
+    Buf Uq2;
+    if (!em.empty() && *std::max_element(em.begin(), em.end()) > 1e-2) {
+        Uq2 = Buf(c.pool.get(), (size_t)B * mr * sizeof(double));
+        double shift = 0.0;
+        for (int attempt = 0;; ++attempt) {
+            copy_f64(c, E2.d(), E.d(), rr * B);
+            add_identity(c, E2.d(), r, 1.0 + shift, B);
+            chol_inv(c, E2.d(), r, 0.0, B);
+            int st = c.read_status_and_clear();
+            if (!(st & ST_CHOL_BREAKDOWN)) break;
+            TNR_REQUIRE(attempt < 8, TNR_ERR_NOT_CONVERGED, "final Rayleigh-Ritz: basis re-orthonormalisation failed");
+            shift = std::max(shift * 30.0, 1e-14);
+        }
+        gemm_f64(c, false, true, m, r, r, 1.0, Uq, m, E2.d(), r, 0.0, Uq2.d(), m, strided(B, mr, rr, mr));
+        Uq = Uq2.d();
+        gemm_f64(c, true, false, r, r, m, 1.0, Uq, m, Uq, m, 0.0, E.d(), r, strided(B, mr, mr, rr));
+        add_identity(c, E.d(), r, -1.0, B);
+    }
+    // P = (I + E)^(-1/2) = I + E (-1/2 + E (3/8 + E (-5/16 + 35/128 E))) (Horner, three r x r products)
+    lincomb2(c, P.d(), rr * B, 35.0 / 128.0, E.d(), 0.0, E.d());
+    add_identity(c, P.d(), r, -5.0 / 16.0, B);
+    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, P.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
+    add_identity(c, E2.d(), r, 3.0 / 8.0, B);
+    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, E2.d(), r, 0.0, P.d(), r, strided(B, rr, rr, rr));
+    add_identity(c, P.d(), r, -0.5, B);
+    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, P.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
+    add_identity(c, E2.d(), r, 1.0, B);
+    copy_f64(c, P.d(), E2.d(), rr * B);
     // the projection Z = M^T Uq (n x r)
     Buf Z(c.pool.get(), (size_t)B * nr * sizeof(double));
     gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq, m, 0.0, Z.d(), n, strided(B, mn, mr, nr), true);
