@@ -330,8 +330,6 @@ void jacobi_eigh_f32(Ctx& c, const double* G, int64_t ldg, int r, double* W, dou
                      int64_t strideG = 0);
 void chol_inv_f32(Ctx& c, double* G, int r, double shift, int batch = 1);
 void add_identity(Ctx& c, double* X, int r, double alpha, int batch = 1);
-// out[b] = Frobenius norm of each of B arrays of len entries (stride len)
-void fro_norms_batched(Ctx& c, const double* X, int64_t len, int B, double* out);
 void polar_coeff(Ctx& c, const double* E, const double* E2, double* C, int r, int batch = 1);
 // X (k x n_total, ld k) rows scaled per batch: X[i, j] *= f(s[(j / n_per) * k + i])
 void row_scale_batched(Ctx& c, double* X, int64_t k, int64_t n_total, const double* s, int mode, int64_t n_per);

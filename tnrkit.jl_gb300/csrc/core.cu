@@ -503,27 +503,6 @@ void fill_identity(Ctx& c, double* x, int64_t m, int64_t n) {
     check_launch("identity");
 }
 
-// out[b] = Frobenius norm of the len entries of each of the B arrays (stride len); one CTA each
-__global__ void k_fro_batched(const double* X, int64_t len, double* out) {
-    X += (int64_t)blockIdx.x * len;
-    double a = 0.0;
-    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) a = fma(X[i], X[i], a);
-    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    __shared__ double wa[32];
-    if ((threadIdx.x & 31) == 0) wa[threadIdx.x >> 5] = a;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        a = threadIdx.x < (blockDim.x >> 5) ? wa[threadIdx.x] : 0.0;
-        for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (threadIdx.x == 0) out[blockIdx.x] = sqrt(a);
-    }
-}
-void fro_norms_batched(Ctx& c, const double* X, int64_t len, int B, double* out) {
-    if (B <= 0) return;
-    k_fro_batched<<<B, 256, 0, c.stream>>>(X, len, out);
-    check_launch("fro_norms_batched");
-}
-
 // X += alpha * I (r x r)
 __global__ void k_add_identity(double* X, int r, double alpha) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;

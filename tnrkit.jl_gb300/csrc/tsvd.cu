@@ -94,6 +94,28 @@ static void polar(Ctx& c, double* Q, int64_t m, int r) {
     }
 }
 
+// Q (m x r) <- Q L^-T with Q^T Q = L L^T (FP64 Gram and Cholesky): exactly orthonormal whatever
+// Q's departure from orthonormality (a tiny shift only if the Gram is numerically singular).
+// The split CholeskyQR3 can leave the noise directions of a numerically rank-deficient M far
+// from orthonormal, where the cubic polar step would not hold.
+static void orth_exact(Ctx& c, double* Q, int64_t m, int r) {
+    Buf G(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf L(c.pool.get(), (size_t)r * r * sizeof(double));
+    Buf T(c.pool.get(), (size_t)m * r * sizeof(double));
+    gemm_f64(c, true, false, r, r, m, 1.0, Q, m, 0, Q, m, 0, 0.0, G.d(), r, 0);
+    double shift = 0.0;
+    for (int attempt = 0;; ++attempt) {
+        copy_f64(c, L.d(), G.d(), (int64_t)r * r);
+        chol_inv(c, L.d(), r, shift);
+        int st = c.read_status_and_clear();
+        if (!(st & ST_CHOL_BREAKDOWN)) break;
+        TNR_REQUIRE(attempt < 8, TNR_ERR_NOT_CONVERGED, "orth_exact: basis Gram not positive definite");
+        shift = std::max(shift * 30.0, 1e-14);
+    }
+    gemm_f64(c, false, true, m, r, r, 1.0, Q, m, 0, L.d(), r, 0, 0.0, T.d(), m, 0);
+    copy_f64(c, Q, T.d(), m * (int64_t)r);
+}
+
 // Exact SVD of the tall X = op(M) (m x p, p <= 128): X V = Ux diag(s), Ux unit columns.
 // trans=false: X = M (ld m); trans=true: X = M^T with M stored p x m (ld p).
 // FP64 cleanup Jacobi of the final decompositions: rotations stop at 1e-12 of the diagonal,
@@ -447,8 +469,9 @@ static TsvdOut teigh_impl(Ctx& c, const double* M, int64_t n, int k, double* U, 
     out.iters = it;
     c.last_iters = it;
     if (debug_on()) fprintf(stderr, "[tnr] teigh n=%lld k=%d r=%d iters=%d\n", (long long)n, k, r, it);
-    // final Rayleigh-Ritz in FP64
-    polar(c, Q.d(), n, r);
+    // final Rayleigh-Ritz in FP64 on an exactly orthonormal basis
+    if (c.precision == TNR_PREC_F64) polar(c, Q.d(), n, r);
+    else orth_exact(c, Q.d(), n, r);
     gemm_bulk_a(c, PMt, true, false, n, r, n, 1.0, M, n, Q.d(), n, 0.0, Y.d(), n, one, true);
     gemm_f64(c, true, false, r, r, n, 1.0, Q.d(), n, 0, Y.d(), n, 0, 0.0, H.d(), r, 0);
     final_eigh(c, H.d(), r, W.d(), l.d());

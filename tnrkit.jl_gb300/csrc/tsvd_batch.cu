@@ -118,14 +118,14 @@ void copy_lead(Ctx& c, const double* in, int p, int k, int B, double* out) {
 
 }  // namespace
 
-// Split precision: the final Rayleigh-Ritz step of B lockstep instances.  Uq [B][m x r] is
-// orthonormal to FP32 level (CholeskyQR3 with FP32 Cholesky factors); its polar factor
-// Q' = Uq P, P = (I + E)^(-1/2) to fourth order in E = Uq^T Uq - I, is never formed: P is
-// folded into the r x r problems.  With Z = M^T Uq (the projection, on the tensor cores with chunked
-// accumulation), Z' = M^T Q' = Z P and Z'^T Z' = P^T (Z^T Z) P = Vb S^2 Vb^T, so
-// U = Uq (P Vb_k), S_k = the column norms of Z (P Vb_k) and Vt = (Z P Vb_k / S_k)^T.
+// Split precision: the final Rayleigh-Ritz step of B lockstep instances.  Uq [B][m x r] comes
+// from CholeskyQR3 with split Grams and FP32 Cholesky factors; the orthonormal basis Q' = Uq P,
+// P = L^-T with Uq^T Uq = L L^T (FP64), is never formed: P is folded into the r x r problems.
+// With Z = M^T Uq (the projection, on the tensor cores with chunked accumulation),
+// Z' = M^T Q' = Z P and Z'^T Z' = P^T (Z^T Z) P = Vb S^2 Vb^T, so U = Uq (P Vb_k),
+// S_k = the column norms of Z (P Vb_k) and Vt = (Z P Vb_k / S_k)^T.
 // The eigenvectors of the r x r Gram come from an FP32 Jacobi alignment (polar-corrected
-// in FP64) and an FP64 Jacobi cleanup.  FP64 GEMM work: two Grams over the long dimension
+// in FP64) and a mixed-precision Jacobi cleanup.  FP64 GEMM work: two Grams over the long dimension
 // and two rank-k products, against the plain path's polar step and one-sided final SVD
 // (four long-dimension products more).  A Gram of Z loses relative accuracy of singular
 // values below ~1e-8 of the largest (FP64 rounding of the squares), which is the noise floor
@@ -136,52 +136,29 @@ std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, i
     Buf P(c.pool.get(), (size_t)B * rr * sizeof(double));
     Buf E(c.pool.get(), (size_t)B * rr * sizeof(double));
     Buf E2(c.pool.get(), (size_t)B * rr * sizeof(double));
+    // P with (Uq P)^T (Uq P) = I: P = L^-T from the FP64 Cholesky of the exact Gram Uq^T Uq (a
+    // tiny shift only if it breaks down: numerically dependent noise columns).  It holds for any
+    // departure from orthonormality, which matters: on a numerically rank-deficient M the split
+    // CholeskyQR3 leaves the noise directions of Uq far from orthonormal (||Uq^T Uq - I|| ~ 0.2
+    // was seen), where a polar series in Uq^T Uq - I inflated sigma_1 by 1%.  P holds L^-1.
     gemm_f64(c, true, false, r, r, m, 1.0, Uq, m, Uq, m, 0.0, E.d(), r, strided(B, mr, mr, rr));
-    add_identity(c, E.d(), r, -1.0, B);
-    // The polar factor below is a series in E (error ~0.25 ||E||^5).  A numerically rank-deficient
-    // M leaves noise directions in the basis that the split CholeskyQR3 (split Grams, FP32
-    // factors) may orthonormalise poorly (||E|| ~ 0.2 was seen); a batch with ||E||_F above 1e-2
-    // first takes one FP64 CholeskyQR pass on its exact Gram I + E, after which E is at FP64
-    // rounding.
-    Buf enrm(c.pool.get(), (size_t)B * sizeof(double));
-    fro_norms_batched(c, E.d(), rr, B, enrm.d());
-    std::vector<double> em = to_host(c, enrm.d(), B);
-    Buf Uq2;
-    if (!em.empty() && *std::max_element(em.begin(), em.end()) > 1e-2) {
-        Uq2 = Buf(c.pool.get(), (size_t)B * mr * sizeof(double));
-        double shift = 0.0;
-        for (int attempt = 0;; ++attempt) {
-            copy_f64(c, E2.d(), E.d(), rr * B);
-            add_identity(c, E2.d(), r, 1.0 + shift, B);
-            chol_inv(c, E2.d(), r, 0.0, B);
-            int st = c.read_status_and_clear();
-            if (!(st & ST_CHOL_BREAKDOWN)) break;
-            TNR_REQUIRE(attempt < 8, TNR_ERR_NOT_CONVERGED, "final Rayleigh-Ritz: basis re-orthonormalisation failed");
-            shift = std::max(shift * 30.0, 1e-14);
-        }
-        gemm_f64(c, false, true, m, r, r, 1.0, Uq, m, E2.d(), r, 0.0, Uq2.d(), m, strided(B, mr, rr, mr));
-        Uq = Uq2.d();
-        gemm_f64(c, true, false, r, r, m, 1.0, Uq, m, Uq, m, 0.0, E.d(), r, strided(B, mr, mr, rr));
-        add_identity(c, E.d(), r, -1.0, B);
+    double shift = 0.0;
+    for (int attempt = 0;; ++attempt) {
+        copy_f64(c, P.d(), E.d(), rr * B);
+        chol_inv(c, P.d(), r, shift, B);
+        int st = c.read_status_and_clear();
+        if (!(st & ST_CHOL_BREAKDOWN)) break;
+        TNR_REQUIRE(attempt < 8, TNR_ERR_NOT_CONVERGED, "final Rayleigh-Ritz: basis Gram not positive definite");
+        shift = std::max(shift * 30.0, 1e-14);
     }
-    // P = (I + E)^(-1/2) = I + E (-1/2 + E (3/8 + E (-5/16 + 35/128 E))) (Horner, three r x r products)
-    lincomb2(c, P.d(), rr * B, 35.0 / 128.0, E.d(), 0.0, E.d());
-    add_identity(c, P.d(), r, -5.0 / 16.0, B);
-    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, P.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
-    add_identity(c, E2.d(), r, 3.0 / 8.0, B);
-    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, E2.d(), r, 0.0, P.d(), r, strided(B, rr, rr, rr));
-    add_identity(c, P.d(), r, -0.5, B);
-    gemm_f64(c, false, false, r, r, r, 1.0, E.d(), r, P.d(), r, 0.0, E2.d(), r, strided(B, rr, rr, rr));
-    add_identity(c, E2.d(), r, 1.0, B);
-    copy_f64(c, P.d(), E2.d(), rr * B);
     // the projection Z = M^T Uq (n x r)
     Buf Z(c.pool.get(), (size_t)B * nr * sizeof(double));
     gemm_bulk_a(c, PMt, true, false, n, r, m, 1.0, M, m, Uq, m, 0.0, Z.d(), n, strided(B, mn, mr, nr), true);
-    // Gp = P^T (Z^T Z) P
+    // Gp = P^T (Z^T Z) P = L^-1 (Z^T Z) L^-T
     Buf G(c.pool.get(), (size_t)B * rr * sizeof(double));
     gemm_f64(c, true, false, r, r, n, 1.0, Z.d(), n, Z.d(), n, 0.0, G.d(), r, strided(B, nr, nr, rr));
-    gemm_f64(c, false, false, r, r, r, 1.0, G.d(), r, P.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));
-    gemm_f64(c, true, false, r, r, r, 1.0, P.d(), r, E.d(), r, 0.0, G.d(), r, strided(B, rr, rr, rr));
+    gemm_f64(c, false, true, r, r, r, 1.0, G.d(), r, P.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));
+    gemm_f64(c, false, false, r, r, r, 1.0, P.d(), r, E.d(), r, 0.0, G.d(), r, strided(B, rr, rr, rr));
     // eigenvectors Vb of Gp: FP32 alignment W1 (made orthogonal in FP64), FP64 cleanup W2
     Buf W1(c.pool.get(), (size_t)B * rr * sizeof(double));
     Buf lam(c.pool.get(), (size_t)B * r * sizeof(double));
@@ -195,9 +172,9 @@ std::vector<double> final_rr_split(Ctx& c, const SplitA& PMt, const double* M, i
     // nearly diagonal, so the mixed-precision Jacobi (FP64 diagonal) holds FP64 accuracy
     jacobi_eigh_mixed(c, E2.d(), r, r, G.d(), lam.d(), B, rr, 1e-10, 1e-16);   // W2 into G
     gemm_f64(c, false, false, r, r, r, 1.0, W1.d(), r, G.d(), r, 0.0, E.d(), r, strided(B, rr, rr, rr));   // Vb
-    // PV = P Vb_k (r x k)
+    // PV = P Vb_k = L^-T Vb_k (r x k)
     Buf PV(c.pool.get(), (size_t)B * rk * sizeof(double));
-    gemm_f64(c, false, false, r, k, r, 1.0, P.d(), r, E.d(), r, 0.0, PV.d(), r, strided(B, rr, rr, rk));
+    gemm_f64(c, true, false, r, k, r, 1.0, P.d(), r, E.d(), r, 0.0, PV.d(), r, strided(B, rr, rr, rk));
     // U = Uq PV; Ub = Z PV = Vt^T S
     gemm_f64(c, false, false, m, k, r, 1.0, Uq, m, PV.d(), r, 0.0, U, m, strided(B, mr, rk, m * k));
     Buf Ub(c.pool.get(), (size_t)B * n * k * sizeof(double));
