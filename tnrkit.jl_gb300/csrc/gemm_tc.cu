@@ -528,16 +528,25 @@ __global__ void k_split_planes(SplitArgs a) {
             else tile[threadIdx.x][y] = v;
         }
         __syncthreads();
-        for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-            const int64_t i = i0 + y, k = k0 + threadIdx.x;
+        // 4 consecutive k of one row per thread (8 threads per row): 8-byte plane stores
+        // (Kp % 4 == 0, k0 % 32 == 0, so every group lies inside [0, Kp) or outside it)
+        {
+            const int tid = threadIdx.y * 32 + threadIdx.x;
+            const int y = tid >> 3, kq = (tid & 7) * 4;
+            const int64_t i = i0 + y, k = k0 + kq;
             if (i < a.rows && k < a.Kp) {
-                __nv_bfloat16 p0, p1, p2;
-                split3(tile[y][threadIdx.x], p0, p1, p2);
+                __nv_bfloat16 p0[4], p1[4], p2[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) split3(tile[y][kq + e], p0[e], p1[e], p2[e]);
                 const int64_t plane = a.rows * a.Kp;
                 __nv_bfloat16* D = a.dst + bi * 3 * plane + i * a.Kp + k;
-                D[0] = p0;
-                D[plane] = p1;
-                D[2 * plane] = p2;
+                uint2 u0, u1, u2;
+                memcpy(&u0, p0, 8);
+                memcpy(&u1, p1, 8);
+                memcpy(&u2, p2, 8);
+                *reinterpret_cast<uint2*>(D) = u0;
+                *reinterpret_cast<uint2*>(D + plane) = u1;
+                *reinterpret_cast<uint2*>(D + 2 * plane) = u2;
             }
         }
     }
