@@ -9,11 +9,17 @@ namespace tnr {
 
 constexpr int BM = 64, BN = 64, BK = 16;
 
-// one CTA: 64x64 tile of C, 256 threads, 4x4 outputs per thread
+// one CTA: 64x64 tile of C, 256 threads, 4x4 outputs per thread.  sym: C = op(A) op(B) is a Gram
+// (A == B, one of them transposed, beta = 0): tiles above the diagonal are skipped and those
+// below it also write their transpose (c_ij and c_ji are the same products in the same order,
+// so the result is the one of the full product bit for bit)
 __global__ void __launch_bounds__(256)
 k_dgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const double* __restrict__ A,
         int64_t lda, const double* __restrict__ B, int64_t ldb, double beta,
-        double* __restrict__ C, int64_t ldc, Batch2 bt, int ksplit, int64_t kchunk, double* __restrict__ part) {
+        double* __restrict__ C, int64_t ldc, Batch2 bt, int ksplit, int64_t kchunk, double* __restrict__ part,
+        bool sym) {
+    if (sym && blockIdx.x < blockIdx.y) return;
+    const bool mirror = sym && blockIdx.x > blockIdx.y;
     __shared__ double As[BK][BM + 1];
     __shared__ double Bs[BK][BN + 1];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -72,7 +78,10 @@ k_dgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const d
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 int64_t gi = i0 + tx + 16 * i, gj = j0 + ty + 16 * j;
-                if (gi < m && gj < n) P[gi + gj * m] = acc[i][j];
+                if (gi < m && gj < n) {
+                    P[gi + gj * m] = acc[i][j];
+                    if (mirror) P[gj + gi * m] = acc[i][j];
+                }
             }
         return;
     }
@@ -86,6 +95,7 @@ k_dgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, double alpha, const d
                 double v = alpha * acc[i][j];
                 if (beta != 0.0) v = fma(beta, C[gi + gj * ldc], v);
                 C[gi + gj * ldc] = v;
+                if (mirror) C[gj + gi * ldc] = v;
             }
         }
 }
@@ -131,9 +141,11 @@ void gemm_f64(Ctx& c, bool ta, bool tb, int64_t m, int64_t n, int64_t k, double 
     Buf part;
     if (ksplit > 1) part = Buf(c.pool.get(), (size_t)ksplit * batch * m * n * sizeof(double));
     dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)(batch * ksplit));
+    const bool sym = A == B && lda == ldb && ta != tb && m == n && beta == 0.0 && bt.sA1 == bt.sB1 &&
+                     bt.sA2 == bt.sB2 && gm > 1;
     int rec = prof_start(c.stream);
     k_dgemm<<<grid, 256, 0, c.stream>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, bt, ksplit,
-                                        kchunk, part.d());
+                                        kchunk, part.d(), sym);
     check_launch("dgemm");
     if (ksplit > 1) {
         int g = (int)std::min<int64_t>((m * n * batch + 255) / 256, (int64_t)sm_count() * 8);
