@@ -315,6 +315,8 @@ def test_new_entry_points_refuse_null_handles(tnr):
     assert L.tnr_get_impurity_tensor(None, 0, buf, 8, dims, ctypes.byref(nl)) == bad
     assert L.tnr_finalize_impurity(None, buf) == bad
     assert L.tnr_run_impurity(None, 8, 4, 1, buf, 8, ctypes.byref(n)) == bad
+    u64 = ctypes.c_uint64()
+    assert L.tnr_decomposition_stats(None, ctypes.byref(u64), ctypes.byref(u64), ctypes.byref(nl)) == bad
     h = ctypes.c_void_p()
     assert L.tnr_create(ctypes.byref(h), 10, 4, dims, buf, None) == bad       # unknown kind
     assert L.tnr_create(ctypes.byref(h), header_defines()["TNR_ATRG_3D"], 4, dims, buf, None) == bad   # 6 legs
@@ -339,3 +341,51 @@ def test_impurity_constructors_check_arguments(tnr):
     ragged = (ctypes.c_int64 * 4)(2, 2, 3, 2)
     assert L.tnr_create_impurity_trg(ctypes.byref(h), ragged, p, p, p, p, p, None) == bad
     assert not h.value
+
+
+def _split_top(args):
+    out, depth, cur = [], 0, ""
+    for ch in args:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return [a for a in out if a]
+
+
+def _header_prototypes():
+    protos = {}
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if not f.endswith(".h"):
+            continue
+        txt = open(os.path.join(ROOT, "include", f)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        txt = re.sub(r"//[^\n]*", "", txt)
+        for m in re.finditer(r"([A-Za-z_][\w \t\*]*?)\b(tnr_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;", txt):
+            args = " ".join(m.group(3).split())
+            n = 0 if args in ("", "void") else len(_split_top(args))
+            protos[m.group(2)] = (" ".join(m.group(1).split()), n)
+    return protos
+
+
+def test_julia_ccalls_match_header():
+    """Every ccall of the Julia binding names a declared entry point with the declared number of
+    arguments and a matching return type (the binding cannot run here: no Julia)."""
+    protos = _header_prototypes()
+    jl = open(os.path.join(ROOT, "tnrkit.jl_gb300", "julia", "TNRKitGB300.jl")).read()
+    calls = re.findall(r"ccall\(\(:(tnr_\w+),\s*libtnr\),\s*(\w+),\s*\((.*?)\)\s*,", jl, flags=re.S)
+    assert len(calls) >= 20
+    ret_map = {"Cint": "int", "Cvoid": "void", "Csize_t": "size_t", "UInt64": "uint64_t", "Cdouble": "double"}
+    for name, ret, args in calls:
+        assert name in protos, name
+        c_ret, c_n = protos[name]
+        assert len(_split_top(args)) == c_n, (name, args, c_n)
+        assert ret_map.get(ret, ret) == c_ret.replace("const ", "").strip() or \
+            (ret in ("Cstring", "Ptr{UInt8}") and "char" in c_ret), (name, ret, c_ret)

@@ -30,7 +30,7 @@ import TNRKit
 import TNRKit: run!, step!, finalize!, free_energy, maxiter, TNRScheme, cft_data, ground_state_degeneracy,
     gu_wen_ratio, central_charge
 
-export GPU, run_batch!, Server, submit!, result, TNR_PREC_F64, TNR_PREC_SPLIT
+export GPU, run_batch!, Server, submit!, result, decomposition_stats, TNR_PREC_F64, TNR_PREC_SPLIT
 
 const libtnr = get(ENV, "TNR_GB300_LIB", joinpath(@__DIR__, "..", "libtnr_gb300.so"))
 
@@ -249,6 +249,20 @@ function central_charge(g::GPU, n::Number)
     c = Ref{Float64}(0)
     check(ccall((:tnr_central_charge, libtnr), Cint, (Ptr{Cvoid}, Cdouble, Ref{Float64}), g.handle, n, c), g.handle)
     return c[]
+end
+
+"""
+    decomposition_stats(g) -> (decompositions, gap_fallbacks, max_iters)
+
+Diagnostic (`tnr_decomposition_stats`, no reference counterpart): truncated decompositions run on
+the handle, how many of them the spectral-gap fallback decomposed in full FP64, and the largest
+subspace-iteration count.
+"""
+function decomposition_stats(g::GPU)
+    nd, nf, mi = Ref{UInt64}(0), Ref{UInt64}(0), Ref{Cint}(0)
+    check(ccall((:tnr_decomposition_stats, libtnr), Cint, (Ptr{Cvoid}, Ref{UInt64}, Ref{UInt64}, Ref{Cint}),
+        g.handle, nd, nf, mi), g.handle)
+    return Int(nd[]), Int(nf[]), Int(mi[])
 end
 
 """
