@@ -1,12 +1,19 @@
 """Pins the CPU oracle against the reference's own golden values and test tolerances.
 
-Golden values: README.md:78-93 (BTRG, Z2 Ising, chi=16, 25 iterations) and the
-free-energy tolerances of test/schemes.jl and test/models.jl.
+Golden values: tests/golden/reference_golden.json, extracted from the reference's README.md
+(BTRG, Z2 Ising, chi=16, 25 iterations) and the free-energy checks of test/schemes.jl by
+tests/golden/make_golden.py (each entry records its file and line); the free-energy
+tolerances of test/models.jl are cited inline below.
 """
+import json
 import math
+import os
 
 import numpy as np
 import pytest
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                     "reference_golden.json"), encoding="utf-8"))
 
 
 def _f(o, scheme, chi, n, beta, sf):
@@ -16,23 +23,22 @@ def _f(o, scheme, chi, n, beta, sf):
 
 @pytest.mark.parametrize("symmetry", ["Z2", "Trivial"])
 def test_readme_btrg_golden(oracle, symmetry):
-    # README.md:78-93: 26 norms, f = -2.1096504926141826902647832, rel. err 3.1e-7
+    # README.md: 26 norms, the printed f to every digit FP64 holds, and its printed relative error
+    g = GOLDEN["readme_btrg"]
     o = oracle
-    data, f = _f(o, o.BTRG(o.classical_ising(o.ISING_BETA_C, symmetry)), 16, 25, o.ISING_BETA_C, 2.0)
-    assert len(data) == 26
-    assert f == pytest.approx(-2.1096504926141826902647832, rel=1e-14, abs=0)
-    assert abs((f - o.F_ONSAGER) / o.F_ONSAGER) == pytest.approx(3.1e-7, rel=0.01)
+    data, f = _f(o, o.BTRG(o.classical_ising(o.ISING_BETA_C, symmetry)), g["chi"], g["maxiter"], o.ISING_BETA_C, 2.0)
+    assert len(data) == g["maxiter"] + 1
+    assert f == pytest.approx(float(g["f"]), rel=1e-14, abs=0)
+    assert abs((f - o.F_ONSAGER) / o.F_ONSAGER) == pytest.approx(g["rel_err_onsager"], rel=0.01)
 
 
-@pytest.mark.parametrize("cls,chi,sf,rtol", [
-    ("TRG", 24, 2.0, 2e-6),     # test/schemes.jl:18-23
-    ("BTRG", 24, 2.0, 6e-8),    # test/schemes.jl:57-62
-    ("HOTRG", 16, 4.0, 6e-7),   # test/schemes.jl:94-99
-])
-def test_schemes_onsager(oracle, cls, chi, sf, rtol):
+@pytest.mark.parametrize("case", GOLDEN["schemes"], ids=lambda c: c["scheme"])
+def test_schemes_onsager(oracle, case):
+    # test/schemes.jl: each scheme's free energy against Onsager's at the reference's rtol
     o = oracle
-    _, f = _f(o, getattr(o, cls)(o.classical_ising()), chi, 25, o.ISING_BETA_C, sf)
-    assert f == pytest.approx(o.F_ONSAGER, rel=rtol)
+    _, f = _f(o, getattr(o, case["scheme"])(o.classical_ising()), case["chi"], case["maxiter"], o.ISING_BETA_C,
+              case["scalefactor"])
+    assert f == pytest.approx(o.F_ONSAGER, rel=case["rtol"])
 
 
 def test_models_trg16(oracle):
