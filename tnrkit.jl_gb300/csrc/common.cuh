@@ -348,7 +348,6 @@ void col_norms(Ctx& c, const double* X, int64_t m, int64_t n, int64_t ldx, doubl
 void gram_unit_diag(Ctx& c, double* G, int r, double* dscale, int batch = 1);
 void sum_squares(Ctx& c, const double* x, int64_t n, double* out);
 void scale_inplace(Ctx& c, double* x, int64_t n, const double* inv_scale_ptr);
-void fill_identity(Ctx& c, double* x, int64_t m, int64_t n);
 void copy_f64(Ctx& c, double* dst, const double* src, int64_t n);
 // Q (m x r, orthonormal columns spanning those of Y) by shifted CholeskyQR3; Y is overwritten
 void orth_scaled(Ctx& c, double* Y, int64_t m, int r, double* Q);

@@ -493,15 +493,6 @@ void scale_inplace(Ctx& c, double* x, int64_t n, const double* inv_scale_ptr) {
     check_launch("scale");
 }
 
-__global__ void k_identity(double* x, int64_t m, int64_t n) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x)
-        x[e] = (e % m) == (e / m) ? 1.0 : 0.0;
-}
-void fill_identity(Ctx& c, double* x, int64_t m, int64_t n) {
-    if (!m || !n) return;
-    k_identity<<<grid_for(m * n, 256), 256, 0, c.stream>>>(x, m, n);
-    check_launch("identity");
-}
 
 // X += alpha * I (r x r)
 __global__ void k_add_identity(double* X, int r, double alpha) {
