@@ -2,8 +2,8 @@
 
 This module is the oracle: a NumPy/SciPy restatement of the reference algorithm,
 operation for operation.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` may import it, and only as the checker or as the
-timed CPU restatement.  The product path (``tnrkit.jl_gb300``) never calls it.
+CPU-baseline leg of ``bench.py`` may import it, and only as the result to compare
+against or as the timed CPU restatement.  The product path (``tnrkit.jl_gb300``) never calls it.
 
 Reference: TNRKit.jl v0.5.1 (pure Julia).  The arithmetic the reference delegates
 to third-party packages that are not vendored with it is restated here from
