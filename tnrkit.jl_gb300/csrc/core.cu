@@ -238,10 +238,10 @@ struct PermArgs {
     int perm[MAXR];
 };
 
-// fastest axis kept in place: every thread writes consecutive output elements
+// generic element-wise permute (degenerate axes): every thread writes consecutive output elements
 __global__ void k_permute_rows(const double* __restrict__ in, double* __restrict__ out,
                                PermArgs a, int64_t total, const double* scale_ptr) {
-    double alpha = scale_ptr ? 1.0 / fabs(*scale_ptr) : 1.0;
+    const double alpha = scale_ptr ? 1.0 / fabs(*scale_ptr) : 1.0;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total;
          j += (int64_t)gridDim.x * blockDim.x) {
         int64_t rem = j, off = 0;
@@ -250,7 +250,36 @@ __global__ void k_permute_rows(const double* __restrict__ in, double* __restrict
             rem /= a.out_d[k];
             off += ik * a.in_s[a.perm[k]];
         }
-        out[j] = alpha * in[off];
+        out[j] = scale_ptr ? alpha * in[off] : in[off];
+    }
+}
+
+// fastest axis kept in place (perm[0] == 0): the tensor is a list of contiguous rows of d0
+// elements in both layouts; a warp copies one row, its input offset computed once by lane 0
+// (the mixed-radix division chain runs per row, not per element)
+__global__ void k_permute_rows0(const double* __restrict__ in, double* __restrict__ out,
+                                PermArgs a, int64_t nrows, const double* scale_ptr) {
+    const double alpha = scale_ptr ? 1.0 / fabs(*scale_ptr) : 1.0;
+    const int64_t d0 = a.in_d[0];
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.y + threadIdx.y; r < nrows;
+         r += (int64_t)gridDim.x * blockDim.y) {
+        long long off = 0;
+        if (threadIdx.x == 0) {
+            int64_t rem = r;
+            for (int k = 1; k < a.rank; ++k) {
+                const int64_t ik = rem % a.out_d[k];
+                rem /= a.out_d[k];
+                off += ik * a.in_s[a.perm[k]];
+            }
+        }
+        off = __shfl_sync(0xffffffffu, off, 0);
+        const double* src = in + off;
+        double* dst = out + r * d0;
+        if (scale_ptr) {
+            for (int64_t x = threadIdx.x; x < d0; x += 32) dst[x] = alpha * src[x];
+        } else {
+            for (int64_t x = threadIdx.x; x < d0; x += 32) dst[x] = src[x];
+        }
     }
 }
 
@@ -288,7 +317,8 @@ __global__ void k_permute_tiled(const double* __restrict__ in, double* __restric
         __syncthreads();
         for (int y = threadIdx.y; y < 32; y += blockDim.y) {
             int64_t ia = a0 + y, ib = b0 + threadIdx.x;
-            if (ia < dA && ib < dB) out[out_off + ia * sA_out + ib] = alpha * tile[threadIdx.x][y];
+            if (ia < dA && ib < dB)
+                out[out_off + ia * sA_out + ib] = scale_ptr ? alpha * tile[threadIdx.x][y] : tile[threadIdx.x][y];
         }
     }
 }
@@ -322,7 +352,15 @@ void permute(Ctx& c, const double* in, const int64_t* in_dims, int rank, const i
     }
     int axB = perm[0];
     int rec = prof_start(c.stream);
-    if (axB == 0 || in_dims[0] == 1 || in_dims[axB] == 1) {
+    if (axB == 0) {
+        const int64_t nrows = total / in_dims[0];
+        const int g = (int)std::min<int64_t>((nrows + 7) / 8, (int64_t)sm_count() * 16);
+        k_permute_rows0<<<g, dim3(32, 8), 0, c.stream>>>(in, out, a, nrows, scale_ptr);
+        check_launch("permute_rows0");
+        prof_stop(rec, c.stream, PROF_PERMUTE, 16.0 * total);
+        return;
+    }
+    if (in_dims[0] == 1 || in_dims[axB] == 1) {
         k_permute_rows<<<grid_for(total, 256), 256, 0, c.stream>>>(in, out, a, total, scale_ptr);
         check_launch("permute_rows");
         prof_stop(rec, c.stream, PROF_PERMUTE, 16.0 * total);
